@@ -1,0 +1,340 @@
+"""Benchmark of the in-place transpose path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl eithot|reference]
+
+Workload: the plain 4D in-place transpose of a (4, 20011, 8192, 2) int32
+tensor (5.25 GB) of seeded uniform random 32-bit values, permutation
+(1 3 2 4), sub-tensor count and alpha from the estimator.  A step is one
+in-place transpose of the whole tensor; the permutation moves the same bytes
+whatever they hold, so each step re-transposes the buffer as a fresh
+(4, 20011, 8192, 2) tensor.  The tensor (5.25 GB) is larger than L2
+(129 MB), so no flush is needed between steps.
+
+value: effective GB/s = 2 * bytes / device time per step (inputs resident).
+e2e:   the same metric through the C ABI with the tensor in pinned host
+       memory: every step copies it to the device, transposes, and copies
+       the result back.
+With N > 1 (torchrun) every rank runs its own replica (the path does not
+shard); value sums the ranks' bytes over the max-over-ranks time.
+--impl reference times the reference's CPU path (the oracle's restatement of
+TensorUtil::seq_tt) on the host cores on a bounded slice of the workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+DIMS = [4, 20011, 8192, 2]
+PERM = [1, 3, 2, 4]
+ELEM = 4
+SEED = 0xE17407
+METRIC = "bit-exact in-place GB/s (2·bytes/s) vs HBM peak; served p99 vs serial"
+WORKLOAD = "in-place 4D transpose (4,20011,8192,2) int32 perm (1 3 2 4), nb/alpha from the estimator"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="eithot", choices=["eithot", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic():
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f)
+    return {}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                t = [x.strip() for x in line.split(",")]
+                if len(t) < 9:
+                    continue
+                try:
+                    sm.append(float(t[1]))
+                    mx.append(float(t[2]))
+                except ValueError:
+                    continue
+                for name, v in zip(names, t[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(name)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(threads=0, budget_s=10.0):
+    """The reference's host permutation (oracle restatement of seq_tt) on a
+    slice of the workload: dims (4, 20011, 512, 2), 328 MB."""
+    import numpy as np
+    import oracle
+
+    dims = [4, 20011, 512, 2]
+    n = math.prod(dims)
+    src = oracle.fill_hash(n, ELEM, SEED)
+    oracle.permute(src, dims, PERM, ELEM, threads=threads)  # warm
+    times = []
+    t_end = time.perf_counter() + budget_s
+    while time.perf_counter() < t_end or len(times) < 2:
+        t0 = time.perf_counter()
+        oracle.permute(src, dims, PERM, ELEM, threads=threads)
+        times.append(time.perf_counter() - t0)
+        if len(times) >= 50:
+            break
+    t = statistics.median(times)
+    cores = oracle.max_threads() if threads <= 0 else threads
+    return {"value": 2.0 * n * ELEM / t / 1e9, "unit": "GB/s", "cores": cores, "kind": "port",
+            "sample": "oracle restatement of TensorUtil::seq_tt, out-of-place, on dims (4,20011,512,2) int32 "
+                      "(1/16 of the workload, 328 MB), median of %d runs" % len(times)}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    import numpy as np
+    import oracle
+
+    dims = [4, 20011, 512, 2]
+    n = math.prod(dims)
+    src = oracle.fill_hash(n, ELEM, SEED)
+    for _ in range(max(0, args.warmup)):
+        oracle.permute(src, dims, PERM, ELEM, threads=0)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.permute(src, dims, PERM, ELEM, threads=0)
+    dt = (time.perf_counter() - t0) / max(1, args.steps)
+    value = 2.0 * n * ELEM / dt / 1e9
+    cores = oracle.max_threads()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "i32", "data": "synthetic (seeded splitmix64 int32)",
+        "config": {"workload": WORKLOAD, "sample": "dims (4,20011,512,2), 1/16 of the workload", "dims": DIMS,
+                   "perm": PERM, "elem_bytes": ELEM},
+        "cpu_baseline": {"value": value, "unit": "GB/s", "cores": cores, "kind": "port",
+                         "sample": "reference host permutation (TensorUtil::seq_tt) restated in oracle/permute.c, "
+                                   "OpenMP over %d host threads, out-of-place on dims (4,20011,512,2) int32" % cores},
+        "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_eithot(args):
+    import torch
+    import eithot_gb300 as E
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local if world > 1 else 0)
+    torch.cuda.set_device(dev)
+
+    nb, alpha, _ = E.estimate(DIMS, PERM, ELEM)
+    n = math.prod(DIMS)
+    nbytes = n * ELEM
+    plan = E.plan(DIMS, PERM, nb, alpha)
+    cap = plan.padded_volume * ELEM
+    buf = torch.empty(cap, dtype=torch.uint8, device=dev)
+    # seeded random content, generated on the device
+    g = torch.Generator(device=dev)
+    g.manual_seed(SEED + rank)
+    buf.view(torch.int32)[: n].random_(generator=g)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        E.transpose_ptr(buf.data_ptr(), cap, DIMS, PERM, ELEM, nb, alpha, E.ORDER_MIXED, stream.cuda_stream)
+
+    # correctness of the first step on a sample of positions (full parity is
+    # in tests/test_gpu_parity.py)
+    import numpy as np
+    import oracle
+    before = buf[: nbytes].view(torch.int32).clone()
+    step()
+    torch.cuda.synchronize(dev)
+    rng = np.random.default_rng(1)
+    idx = torch.from_numpy(rng.integers(0, n, size=20000)).to(dev)
+    dst = torch.tensor([oracle.dest_index(DIMS, PERM, int(i)) for i in idx.cpu().numpy()], device=dev)
+    ok = bool(torch.equal(buf[: nbytes].view(torch.int32)[dst], before[idx]))
+    del before
+    if not ok:
+        raise SystemExit("bench: first step differs from the oracle permutation")
+
+    for _ in range(max(0, args.warmup) - 1):
+        step()
+    torch.cuda.synchronize(dev)
+
+    # timed region (device-resident), CUDA events on the launching stream;
+    # the library also brackets every pass with events on that stream
+    E.profile_reset()
+    E.set_profiling(True)
+    launches = 0
+    start = torch.cuda.Event(enable_timing=True)
+    stop = torch.cuda.Event(enable_timing=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(dev.index) as clk:
+        start.record(stream)
+        for _ in range(args.steps):
+            step()
+            launches += E.last_stats()["n_launches"]
+        stop.record(stream)
+        torch.cuda.synchronize(dev)
+    clocks = clk.summary()
+    total_ms = start.elapsed_time(stop)
+    per_pass = {}
+    for p in E.profile():
+        d = per_pass.setdefault(p["name"], {"ms": 0.0, "n": 0, "bytes": p["bytes"]})
+        d["ms"] += p["ms"]
+        d["n"] += 1
+    E.set_profiling(False)
+    E.profile_reset()
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = world * 2.0 * nbytes / (ms_per_step / 1e3) / 1e9
+
+    # end-to-end through the C ABI from pinned host memory
+    host = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    host.copy_(buf[: nbytes])
+    e2e_steps = max(1, args.e2e_steps)
+    torch.cuda.synchronize(dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        buf[: nbytes].copy_(host, non_blocking=True)
+        step()
+        host.copy_(buf[: nbytes], non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+    e2e_value = world * 2.0 * nbytes / (e2e_ms / 1e3) / 1e9
+
+    peak, peak_kind = load_peaks()
+    dominant = max(per_pass.items(), key=lambda kv: kv[1]["ms"]) if per_pass else None
+    roofline = None
+    if dominant:
+        name, d = dominant
+        avg_ms = d["ms"] / d["n"]
+        achieved = d["bytes"] / (avg_ms / 1e3) / 1e9
+        traffic = load_traffic().get(name.split(" ")[0])
+        roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": achieved / peak, "traffic": traffic, "kernel": name,
+                    "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind if peak_kind == "measured"
+                    else "fallback 6.8 TB/s",
+                    "passes": {k: {"avg_ms": v["ms"] / v["n"], "gbs": v["bytes"] / (v["ms"] / v["n"] / 1e3) / 1e9}
+                               for k, v in per_pass.items()}}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "i32", "data": "synthetic (seeded uniform random int32)",
+            "config": {"workload": WORKLOAD, "dims": DIMS, "perm": PERM, "elem_bytes": ELEM, "nb": nb,
+                       "alpha": alpha, "bytes": nbytes,
+                       "l2": "no flush: the 5.25 GB tensor is larger than the 129 MB L2",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "e2e": {"value": e2e_value, "unit": "GB/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                    "ms_per_step": e2e_ms},
+            "gpu_launches": launches,
+            "roofline": roofline,
+            "clocks": clocks,
+        }
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline()
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_eithot(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

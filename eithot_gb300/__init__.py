@@ -1,0 +1,210 @@
+"""EITHOT-GB300: in-place high-order tensor transposition on GB300 (sm_103a).
+
+Python mirror of the reference interface for this path.  The reference's
+entry point is ``inplace::transpose(data, source, rank, dim, permutation,
+sizeofType, num_block, ALPHA)`` (ITNT/include/transpose.h:8) driven by the
+``test_inplace dims... perm(1-based)... elem nb alpha`` tuple
+(ITNT/src/test_inplace.cpp:142-158); :func:`transpose` takes the same tuple and
+forwards to the C ABI in ``include/eithot.h`` (``libeithot.so``).  All device
+work is the library's own sm_103a kernels; there is no CPU or library
+fallback: if the shared library is missing the import raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+from typing import List, Optional, Sequence
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "_lib", "libeithot.so")
+
+OK, EINVAL, ENOMEM, ETIMEOUT, ECUDA, EUNSUPPORTED, EBUSY = range(7)
+ORDER_MIXED, ORDER_PRE, ORDER_POST = 0, 1, 2
+STEP_ROUND, STEP_PARTITION, STEP_JOIN, STEP_PAD_PRE, STEP_PAD_POST = range(5)
+
+
+class EithotError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__("eithot error %d: %s" % (code, msg))
+        self.code = code
+
+
+class _Step(ctypes.Structure):
+    _fields_ = [("role", ctypes.c_int), ("code", ctypes.c_int), ("rank", ctypes.c_int),
+                ("perm", ctypes.c_int * 4), ("dims", ctypes.c_int64 * 4)]
+
+
+class _PlanInfo(ctypes.Structure):
+    _fields_ = [("order_used", ctypes.c_int), ("num_sub_tensors", ctypes.c_int),
+                ("decompose_dim", ctypes.c_int), ("padded", ctypes.c_int),
+                ("padded_dim_size", ctypes.c_int64), ("volume", ctypes.c_int64),
+                ("padded_volume", ctypes.c_int64), ("sub_tensor_elems", ctypes.c_int64),
+                ("n_steps", ctypes.c_int)]
+
+
+class _Stats(ctypes.Structure):
+    _fields_ = [("workspace_bytes", ctypes.c_size_t), ("free_before", ctypes.c_size_t),
+                ("free_after_alloc", ctypes.c_size_t), ("n_passes", ctypes.c_int),
+                ("n_launches", ctypes.c_int), ("algorithmic_bytes", ctypes.c_double)]
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libeithot.so is not built (%s); run "
+                          "`python -c 'import __graft_entry__ as g; g.build()'`" % LIB_PATH)
+    lib = ctypes.CDLL(LIB_PATH)
+    I64P = ctypes.POINTER(ctypes.c_int64)
+    IP = ctypes.POINTER(ctypes.c_int)
+    lib.eithot_plan.argtypes = [ctypes.c_int, I64P, IP, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                ctypes.POINTER(_PlanInfo), ctypes.POINTER(_Step), ctypes.c_int]
+    lib.eithot_transpose.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, I64P, IP,
+                                     ctypes.c_size_t, ctypes.c_int, ctypes.c_double, ctypes.c_void_p]
+    lib.eithot_transpose_ex.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, I64P, IP,
+                                        ctypes.c_size_t, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                        ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+    lib.eithot_workspace_size.argtypes = [ctypes.c_int, I64P, IP, ctypes.c_size_t, ctypes.c_int,
+                                          ctypes.c_double, ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]
+    lib.eithot_estimate.argtypes = [ctypes.c_int, I64P, IP, ctypes.c_size_t, ctypes.c_int,
+                                    ctypes.c_double, ctypes.c_size_t, ctypes.c_int, IP,
+                                    ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_size_t)]
+    lib.eithot_last_error.restype = ctypes.c_char_p
+    lib.eithot_profile_get.argtypes = [ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t,
+                                       ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+    lib.eithot_last_stats.argtypes = [ctypes.POINTER(_Stats)]
+    return lib
+
+
+lib = _load()
+
+
+def _arrays(dims: Sequence[int], perm: Sequence[int]):
+    r = len(dims)
+    if len(perm) != r:
+        raise EithotError(EINVAL, "dims and permutation differ in length")
+    return r, (ctypes.c_int64 * r)(*[int(d) for d in dims]), (ctypes.c_int * r)(*[int(p) for p in perm])
+
+
+def _check(rc: int):
+    if rc != OK:
+        raise EithotError(rc, lib.eithot_last_error().decode())
+
+
+@dataclass
+class Step:
+    role: int
+    code: int
+    dims: List[int]
+    perm: List[int]
+
+
+@dataclass
+class PlanInfo:
+    order_used: int
+    num_sub_tensors: int
+    decompose_dim: int
+    padded: bool
+    padded_dim_size: int
+    volume: int
+    padded_volume: int
+    sub_tensor_elems: int
+    steps: List[Step]
+
+
+def plan(dims: Sequence[int], perm: Sequence[int], num_sub_tensors: int = 1, alpha: float = 0.01,
+         order: int = ORDER_MIXED) -> PlanInfo:
+    """The decomposition the library will execute (host only)."""
+    r, d, p = _arrays(dims, perm)
+    info = _PlanInfo()
+    _check(lib.eithot_plan(r, d, p, num_sub_tensors, alpha, order, ctypes.byref(info), None, 0))
+    steps = (_Step * max(1, info.n_steps))()
+    _check(lib.eithot_plan(r, d, p, num_sub_tensors, alpha, order, ctypes.byref(info), steps, info.n_steps))
+    out = []
+    for i in range(info.n_steps):
+        s = steps[i]
+        if s.role in (STEP_PAD_PRE, STEP_PAD_POST):
+            out.append(Step(s.role, 0, [s.dims[0], s.dims[1], s.dims[2]], []))
+        else:
+            out.append(Step(s.role, s.code, list(s.dims[:s.rank]), list(s.perm[:s.rank])))
+    return PlanInfo(info.order_used, info.num_sub_tensors, info.decompose_dim, bool(info.padded),
+                    info.padded_dim_size, info.volume, info.padded_volume, info.sub_tensor_elems, out)
+
+
+def workspace_size(dims, perm, elem_size, num_sub_tensors=1, alpha=0.01, order=ORDER_MIXED) -> int:
+    r, d, p = _arrays(dims, perm)
+    out = ctypes.c_size_t()
+    _check(lib.eithot_workspace_size(r, d, p, elem_size, num_sub_tensors, alpha, order, ctypes.byref(out)))
+    return out.value
+
+
+def estimate(dims, perm, elem_size, num_sub_tensors=1, alpha=0.01, smem_per_block=0, padding_blocks=0):
+    """Nd_estimation's answer: (nb, alpha, modelled extra bytes)."""
+    r, d, p = _arrays(dims, perm)
+    nb = ctypes.c_int()
+    a = ctypes.c_double()
+    ex = ctypes.c_size_t()
+    _check(lib.eithot_estimate(r, d, p, elem_size, num_sub_tensors, alpha, smem_per_block,
+                               padding_blocks, ctypes.byref(nb), ctypes.byref(a), ctypes.byref(ex)))
+    return nb.value, a.value, ex.value
+
+
+def transpose_ptr(ptr: int, capacity_bytes: int, dims, perm, elem_size: int, num_sub_tensors: int = 1,
+                  alpha: float = 0.01, order: int = ORDER_MIXED, stream: Optional[int] = None,
+                  workspace_ptr: int = 0, workspace_bytes: int = 0) -> None:
+    """In-place transpose of the tensor at device address `ptr` (C ABI call)."""
+    r, d, p = _arrays(dims, perm)
+    _check(lib.eithot_transpose_ex(ctypes.c_void_p(ptr), capacity_bytes, r, d, p, elem_size,
+                                   num_sub_tensors, alpha, order,
+                                   ctypes.c_void_p(workspace_ptr) if workspace_ptr else None,
+                                   workspace_bytes, ctypes.c_void_p(stream) if stream else None))
+
+
+def transpose(tensor, dims, perm, num_sub_tensors: int = 1, alpha: float = 0.01,
+              order: int = ORDER_MIXED, elem_size: Optional[int] = None, stream=None):
+    """In-place transpose of a CUDA torch tensor holding the row-major
+    (dims[0] fastest) tensor; returns the same tensor (its storage now holds
+    the permuted tensor).  The whole storage of `tensor` is the capacity the
+    padded form may use."""
+    import torch  # device memory and streams only
+
+    if not tensor.is_cuda:
+        raise EithotError(EINVAL, "tensor must live on a CUDA device")
+    es = elem_size or tensor.element_size()
+    cap = tensor.numel() * tensor.element_size()
+    if stream is None:
+        stream = torch.cuda.current_stream(tensor.device)
+    sptr = stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+    with torch.cuda.device(tensor.device):
+        transpose_ptr(tensor.data_ptr(), cap, dims, perm, es, num_sub_tensors, alpha, order, sptr)
+    return tensor
+
+
+def last_stats() -> dict:
+    s = _Stats()
+    _check(lib.eithot_last_stats(ctypes.byref(s)))
+    return {k: getattr(s, k) for k, _ in _Stats._fields_}
+
+
+def output_dims(dims: Sequence[int], perm: Sequence[int]) -> List[int]:
+    return [int(dims[p - 1]) for p in perm]
+
+
+def set_profiling(enable: bool) -> None:
+    """Record CUDA events around every pass of subsequent calls (this thread)."""
+    _check(lib.eithot_set_profiling(1 if enable else 0))
+
+
+def profile_reset() -> None:
+    _check(lib.eithot_profile_reset())
+
+
+def profile() -> List[dict]:
+    """Per-pass (name, ms, bytes) of the last profiled call; synchronise the
+    stream first."""
+    out = []
+    name = ctypes.create_string_buffer(256)
+    for i in range(lib.eithot_profile_count()):
+        ms, by = ctypes.c_double(), ctypes.c_double()
+        _check(lib.eithot_profile_get(i, name, 256, ctypes.byref(ms), ctypes.byref(by)))
+        out.append({"name": name.value.decode(), "ms": ms.value, "bytes": by.value})
+    return out

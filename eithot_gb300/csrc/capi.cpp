@@ -1,0 +1,321 @@
+// The C ABI (include/eithot.h) and the reference-signature shim.
+#include "eithot.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "estimator.h"
+#include "exec.h"
+#include "passes.h"
+#include "plan.h"
+
+namespace {
+
+thread_local std::string g_err;
+thread_local eithot_stats g_stats;
+thread_local bool g_profile = false;
+thread_local std::vector<cudaEvent_t> g_events;
+thread_local size_t g_events_used = 0;
+thread_local std::vector<std::pair<size_t, size_t>> g_spans;
+thread_local std::vector<std::string> g_pass_names;
+thread_local std::vector<double> g_pass_bytes;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+bool elem_ok(size_t e) { return e >= 1 && e <= 64; }
+
+// Scratch for a pass list: at least one staged item of every pass, at most
+// what lets each pass run as a single group, capped at alpha * bytes when
+// that cap still covers the minimum.
+size_t choose_workspace(const std::vector<eithot::Pass>& passes, const eithot::DeviceCaps& caps,
+                        double alpha, double bytes) {
+    size_t lo = 0, ideal = 0;
+    for (const auto& p : passes) {
+        lo = std::max(lo, eithot::pass_workspace_bytes(p, caps));
+        ideal = std::max(ideal, eithot::pass_workspace_ideal(p, caps));
+    }
+    if (lo == 0) return 0;
+    const double cap = alpha * bytes;
+    size_t ws = ideal;
+    if (static_cast<double>(ws) > cap) ws = static_cast<size_t>(cap);
+    ws = std::max(ws, lo);
+    return (ws + 255) / 256 * 256;
+}
+
+int device_caps(eithot::DeviceCaps* caps) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail(EITHOT_ECUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    std::string err;
+    if (!eithot::query_caps(dev, caps, &err)) return fail(EITHOT_ECUDA, "device query: " + err);
+    return EITHOT_OK;
+}
+
+int build(int rank, const int64_t* dims, const int* perm, size_t elem, int nb, double alpha,
+          int order, const eithot::DeviceCaps& caps, eithot::NdPlan* plan,
+          std::vector<eithot::Pass>* passes) {
+    if (!elem_ok(elem)) return fail(EITHOT_EINVAL, "elem_size must be in [1, 64] bytes");
+    std::string err;
+    if (!eithot::make_nd_plan(rank, dims, perm, nb, alpha, order, plan, &err)) return fail(EITHOT_EINVAL, err);
+    if (static_cast<double>(plan->padded_volume) * static_cast<double>(elem) > 1.15e18)
+        return fail(EITHOT_EINVAL, "tensor too large");
+    if (!eithot::lower_plan(*plan, elem, caps, passes, &err)) return fail(EITHOT_EINVAL, err);
+    return EITHOT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* eithot_last_error(void) { return g_err.c_str(); }
+
+int eithot_version(void) { return 100; }
+
+int eithot_set_profiling(int enable) {
+    g_profile = enable != 0;
+    return EITHOT_OK;
+}
+
+int eithot_profile_reset(void) {
+    g_events_used = 0;
+    g_spans.clear();
+    g_pass_names.clear();
+    g_pass_bytes.clear();
+    return EITHOT_OK;
+}
+
+int eithot_profile_count(void) { return static_cast<int>(g_pass_names.size()); }
+
+int eithot_profile_get(int i, char* name, size_t name_len, double* ms, double* bytes_moved) {
+    if (i < 0 || i >= static_cast<int>(g_pass_names.size()))
+        return fail(EITHOT_EINVAL, "profile index out of range");
+    if (name && name_len) {
+        std::strncpy(name, g_pass_names[i].c_str(), name_len);
+        name[name_len - 1] = 0;
+    }
+    if (bytes_moved) *bytes_moved = g_pass_bytes[i];
+    if (ms) {
+        float t = 0.f;
+        cudaError_t e = cudaEventElapsedTime(&t, g_events[g_spans[i].first], g_events[g_spans[i].second]);
+        if (e != cudaSuccess) return fail(EITHOT_ECUDA, std::string("profile: ") + cudaGetErrorString(e));
+        *ms = t;
+    }
+    return EITHOT_OK;
+}
+
+int eithot_last_stats(eithot_stats* out) {
+    if (!out) return fail(EITHOT_EINVAL, "null stats");
+    *out = g_stats;
+    return EITHOT_OK;
+}
+
+int eithot_plan(int rank, const int64_t* dims, const int* perm_1based, int num_sub_tensors,
+                double alpha, int reorder_type, eithot_plan_info* info, eithot_step* steps,
+                int max_steps) {
+    eithot::NdPlan plan;
+    std::string err;
+    if (!eithot::make_nd_plan(rank, dims, perm_1based, num_sub_tensors, alpha, reorder_type, &plan, &err))
+        return fail(EITHOT_EINVAL, err);
+    if (info) {
+        info->order_used = plan.order_used;
+        info->num_sub_tensors = plan.nb;
+        info->decompose_dim = plan.decompose_pos;
+        info->padded = plan.padded ? 1 : 0;
+        info->padded_dim_size = plan.padded ? plan.padded_dim : 0;
+        info->volume = plan.volume;
+        info->padded_volume = plan.padded_volume;
+        info->sub_tensor_elems = plan.sub_volume;
+        info->n_steps = static_cast<int>(plan.steps.size());
+    }
+    for (int i = 0; steps && i < max_steps && i < static_cast<int>(plan.steps.size()); ++i) {
+        const auto& s = plan.steps[i];
+        eithot_step& o = steps[i];
+        std::memset(&o, 0, sizeof(o));
+        o.role = s.role;
+        if (s.role == eithot::kPadPre || s.role == eithot::kPadPost) {
+            o.code = 0;
+            o.rank = 0;
+            o.dims[0] = s.pad_pos;
+            o.dims[1] = s.pad_orig;
+            o.dims[2] = s.pad_size;
+        } else {
+            o.code = s.op.code();
+            o.rank = s.op.rank;
+            for (int k = 0; k < s.op.rank; ++k) {
+                o.dims[k] = s.op.dims[k];
+                o.perm[k] = s.op.perm[k];
+            }
+        }
+    }
+    return EITHOT_OK;
+}
+
+int eithot_workspace_size(int rank, const int64_t* dims, const int* perm_1based, size_t elem_size,
+                          int num_sub_tensors, double alpha, int reorder_type, size_t* bytes_out) {
+    if (!bytes_out) return fail(EITHOT_EINVAL, "null bytes_out");
+    eithot::DeviceCaps caps;
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) {
+        std::string err;
+        if (!eithot::query_caps(dev, &caps, &err)) caps = eithot::DeviceCaps();
+    } else {
+        cudaGetLastError();
+    }
+    eithot::NdPlan plan;
+    std::vector<eithot::Pass> passes;
+    int rc = build(rank, dims, perm_1based, elem_size, num_sub_tensors, alpha, reorder_type, caps, &plan, &passes);
+    if (rc) return rc;
+    *bytes_out = choose_workspace(passes, caps, alpha, static_cast<double>(plan.volume) * elem_size);
+    return EITHOT_OK;
+}
+
+int eithot_transpose_ex(void* d_data, size_t capacity_bytes, int rank, const int64_t* dims,
+                        const int* perm_1based, size_t elem_size, int num_sub_tensors, double alpha,
+                        int reorder_type, void* d_workspace, size_t workspace_bytes, void* stream) {
+    std::memset(&g_stats, 0, sizeof(g_stats));
+    if (!d_data) return fail(EITHOT_EINVAL, "null data pointer");
+    eithot::DeviceCaps caps;
+    int rc = device_caps(&caps);
+    if (rc) return rc;
+    {
+        cudaPointerAttributes attr;
+        cudaError_t e = cudaPointerGetAttributes(&attr, d_data);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(EITHOT_EINVAL, std::string("data pointer: ") + cudaGetErrorString(e));
+        }
+        if (attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged)
+            return fail(EITHOT_EINVAL, "data must be device or managed memory");
+    }
+    eithot::NdPlan plan;
+    std::vector<eithot::Pass> passes;
+    rc = build(rank, dims, perm_1based, elem_size, num_sub_tensors, alpha, reorder_type, caps, &plan, &passes);
+    if (rc) return rc;
+    const double need = static_cast<double>(plan.padded_volume) * static_cast<double>(elem_size);
+    if (need > static_cast<double>(capacity_bytes))
+        return fail(EITHOT_EINVAL, "buffer capacity is smaller than the (padded) tensor");
+    const double bytes = static_cast<double>(plan.volume) * static_cast<double>(elem_size);
+    g_stats.algorithmic_bytes = 2.0 * bytes;
+
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    size_t min_ws = 0;
+    for (const auto& p : passes) min_ws = std::max(min_ws, eithot::pass_workspace_bytes(p, caps));
+    eithot::ExecContext ctx;
+    ctx.caps = caps;
+    ctx.stream = st;
+    ctx.profile = g_profile;
+    ctx.events_used = g_events_used;
+    ctx.events = &g_events;
+    ctx.spans = &g_spans;
+    ctx.names = &g_pass_names;
+    ctx.bytes = &g_pass_bytes;
+    size_t fb = 0, tb = 0;
+    cudaMemGetInfo(&fb, &tb);
+    g_stats.free_before = fb;
+    bool owned = false;
+    if (d_workspace) {
+        if (workspace_bytes < min_ws) return fail(EITHOT_ENOMEM, "caller workspace is smaller than eithot_workspace_size()");
+        ctx.scratch = static_cast<uint8_t*>(d_workspace);
+        ctx.scratch_bytes = workspace_bytes;
+    } else {
+        const size_t ws = choose_workspace(passes, caps, alpha, bytes);
+        if (ws > 0) {
+            void* p = nullptr;
+            cudaError_t e = cudaMallocAsync(&p, ws, st);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                return fail(EITHOT_ENOMEM, std::string("workspace allocation: ") + cudaGetErrorString(e));
+            }
+            ctx.scratch = static_cast<uint8_t*>(p);
+            ctx.scratch_bytes = ws;
+            owned = true;
+        }
+    }
+    cudaMemGetInfo(&fb, &tb);
+    g_stats.free_after_alloc = fb;
+    g_stats.workspace_bytes = ctx.scratch_bytes;
+    rc = eithot::run_passes(static_cast<uint8_t*>(d_data), passes, ctx);
+    g_events_used = ctx.events_used;
+    if (owned) cudaFreeAsync(ctx.scratch, st);
+    g_stats.n_passes = ctx.passes;
+    g_stats.n_launches = ctx.launches;
+    if (rc) return fail(rc, ctx.err);
+    return EITHOT_OK;
+}
+
+int eithot_transpose(void* d_data, size_t capacity_bytes, int rank, const int64_t* dims,
+                     const int* perm_1based, size_t elem_size, int num_sub_tensors, double alpha,
+                     void* stream) {
+    return eithot_transpose_ex(d_data, capacity_bytes, rank, dims, perm_1based, elem_size,
+                               num_sub_tensors, alpha, EITHOT_ORDER_MIXED, nullptr, 0, stream);
+}
+
+int eithot_estimate(int rank, const int64_t* dims, const int* perm_1based, size_t elem_size,
+                    int num_sub_tensors, double alpha, size_t smem_per_block, int padding_blocks,
+                    int* nb_out, double* alpha_out, size_t* extra_bytes_out) {
+    (void)num_sub_tensors;  // the reference estimator ignores the requested nb
+    eithot::NdPlan plan;
+    std::string err;
+    if (!eithot::make_nd_plan(rank, dims, perm_1based, 1, alpha, EITHOT_ORDER_MIXED, &plan, &err))
+        return fail(EITHOT_EINVAL, err);
+    if (!elem_ok(elem_size)) return fail(EITHOT_EINVAL, "elem_size must be in [1, 64] bytes");
+    if (smem_per_block == 0 || padding_blocks <= 0) {
+        int dev = 0, v = 0, sms = 152;
+        size_t smem = 49152;
+        if (cudaGetDevice(&dev) == cudaSuccess) {
+            if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlock, dev) == cudaSuccess) smem = v;
+            if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess) sms = v;
+        } else {
+            cudaGetLastError();
+        }
+        if (smem_per_block == 0) smem_per_block = smem;
+        if (padding_blocks <= 0) padding_blocks = 2 * sms;
+    }
+    eithot::Estimate est;
+    std::vector<int64_t> d(dims, dims + rank);
+    std::vector<int> p(perm_1based, perm_1based + rank);
+    eithot::estimate(d, p, elem_size, alpha, smem_per_block, static_cast<uint64_t>(padding_blocks), &est);
+    if (nb_out) *nb_out = est.nb;
+    if (alpha_out) *alpha_out = est.alpha;
+    if (extra_bytes_out) *extra_bytes_out = est.final_tmp;
+    return EITHOT_OK;
+}
+
+}  // extern "C"
+
+namespace inplace {
+
+void transpose(void* data, int source, int rank, void* dim, void* permutation, size_t sizeofType,
+               int num_block, double LARGE_RATIO) {
+    if (rank < 1 || !data || !dim || !permutation) {
+        std::fprintf(stderr, "inplace::transpose: invalid arguments\n");
+        return;
+    }
+    const int* d = static_cast<const int*>(dim);
+    const int* p = static_cast<const int*>(permutation);
+    std::vector<int64_t> dims(d, d + rank);
+    std::vector<int> perm(rank);
+    for (int i = 0; i < rank; ++i) perm[i] = p[i] + 1;
+    uint8_t* base = static_cast<uint8_t*>(data) + static_cast<size_t>(source) * sizeofType;
+    int rc = eithot_transpose(base, SIZE_MAX, rank, dims.data(), perm.data(), sizeofType, num_block,
+                              LARGE_RATIO, nullptr);
+    if (rc == EITHOT_OK) {
+        cudaError_t e = cudaStreamSynchronize(nullptr);
+        if (e != cudaSuccess) {
+            std::fprintf(stderr, "inplace::transpose: %s\n", cudaGetErrorString(e));
+            return;
+        }
+    } else {
+        std::fprintf(stderr, "inplace::transpose: %s\n", eithot_last_error());
+    }
+}
+
+}  // namespace inplace

@@ -1,0 +1,182 @@
+// The extra-memory estimator: EITHOT's Nd_estimation procedure
+// (Nd_memory_estimation/src/test_inplace.cpp:19-147) over the temp-size
+// model of the reference's kernels (Nd_memory_estimation/src/col_op.cu,
+// row_op.cu, Nd_padding.cu and the 2D/3D/4D drivers).  It answers "which nb
+// and alpha would the reference choose" so that callers which feed the
+// estimator's output into the transpose (as Benchmark/Bench.sh does) get the
+// same tuple; the scratch this library itself needs is eithot_workspace_size.
+#include "estimator.h"
+
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+
+#include "plan.h"
+
+namespace eithot {
+
+namespace {
+
+int msb(int64_t x) { return static_cast<int>(std::log2(static_cast<double>(x))); }
+
+struct Model {
+    uint64_t st;
+    uint64_t smem;
+
+    // _2d::col_op and _3d::_213::col_op
+    uint64_t col2d(int64_t d1, int64_t d2, bool rotate) const {
+        if (smem / (st * d2) >= 16) return 0;
+        const uint64_t nt = (rotate || msb(d1) > 18) ? 256 : 32;
+        return st * nt * d2;
+    }
+    // row gather / scatter of _2d and _3d::_213
+    uint64_t row2d(int64_t d1) const {
+        if (2 * d1 * st <= smem / 32) return 0;
+        if (st * d1 <= smem) return 0;
+        return st * d1;
+    }
+    uint64_t col132(int64_t d1, int64_t d2, bool rotate) const {
+        if (2 * st * d1 * d2 <= smem / 32) return 0;
+        if (st * d1 * d2 <= smem) return 0;
+        if (smem / (st * d2) >= 16) return 0;
+        const uint64_t nt = (rotate || msb(d1) > 18) ? 256 : 32;
+        return st * nt * d2;
+    }
+    uint64_t row132(int64_t d1, int64_t d3) const {
+        return st * d1 * d3 <= smem ? 0 : st * d1 * d3;
+    }
+    static int64_t gcd(int64_t a, int64_t b) { return std::gcd(a, b); }
+
+    // c2r(d1, d2) of the 2D and 213 families: view d2 rows x d1 cols
+    uint64_t c2r_2d(int64_t d1, int64_t d2) const {
+        uint64_t t = gcd(d2, d1) > 1 ? col2d(d1, d2, true) : 0;
+        return std::max({t, row2d(d1), col2d(d1, d2, false)});
+    }
+    uint64_t r2c_2d(int64_t d1, int64_t d2) const {
+        uint64_t t = std::max(col2d(d1, d2, false), row2d(d1));
+        if (gcd(d1, d2) > 1) t = std::max(t, col2d(d1, d2, true));
+        return t;
+    }
+    uint64_t t2d(int64_t d1, int64_t d2) const { return d1 >= d2 ? c2r_2d(d1, d2) : r2c_2d(d2, d1); }
+
+    uint64_t c2r_132(int64_t d1, int64_t d2, int64_t d3) const {
+        uint64_t t = gcd(d2, d3) > 1 ? col132(d1, d2, true) : 0;
+        return std::max({t, row132(d1, d3), col132(d1, d2, false)});
+    }
+    uint64_t r2c_132(int64_t d1, int64_t d2, int64_t d3) const {
+        uint64_t t = std::max(col132(d1, d2, false), row132(d1, d3));
+        if (gcd(d3, d2) > 1) t = std::max(t, col132(d1, d2, true));
+        return t;
+    }
+
+    uint64_t t213(int64_t d1, int64_t d2, int64_t d3) const {
+        if (d3 >= 8) return row2d(d1 * d2);
+        return d1 > d2 ? c2r_2d(d1, d2) : r2c_2d(d2, d1);
+    }
+    uint64_t t132(int64_t d1, int64_t d2, int64_t d3) const {
+        if (d1 >= 48) return col2d(d1, d2 * d3, false);
+        if (d1 > 12) return d2 > d3 ? c2r_132(d1, d3, d2) : r2c_132(d1, d2, d3);
+        if (d2 >= d3) return std::max(t2d(d1 * d2, d3), row2d(d3 * d1));
+        return std::max(row2d(d1 * d2), t2d(d2, d1 * d3));
+    }
+    uint64_t t1324(int64_t d1, int64_t d2, int64_t d3, int64_t d4) const {
+        if (d1 >= 96) return col2d(d1, d2 * d3 * d4, false);
+        if (d4 >= 4) return row2d(d1 * d2 * d3);
+        if (d2 >= d3) return std::max(t213(d1 * d2, d3, d4), t213(d3, d1, d2 * d4));
+        return std::max({row2d(d1 * d2), t2d(d2, d1 * d3 * d4), col2d(d1 * d3, d4 * d2, false)});
+    }
+    uint64_t low(const LowOp& op) const {
+        const int64_t* d = op.dims;
+        switch (op.code()) {
+            case 21: return t2d(d[0], d[1]);
+            case 231: return t2d(d[0], d[1] * d[2]);
+            case 312: return t2d(d[0] * d[1], d[2]);
+            case 213: return t213(d[0], d[1], d[2]);
+            case 132: return t132(d[0], d[1], d[2]);
+            case 1324: return t1324(d[0], d[1], d[2], d[3]);
+            default: return 0;
+        }
+    }
+    uint64_t series(const std::vector<int64_t>& dims, const std::vector<int>& perm) const {
+        std::vector<LowOp> ops;
+        plan_series(dims, perm, kOrderMixed, &ops);
+        uint64_t t = 0;
+        for (auto& o : ops) t = std::max(t, low(o));
+        return t;
+    }
+};
+
+}  // namespace
+
+bool estimate(const std::vector<int64_t>& dims, const std::vector<int>& perm, uint64_t elem_size,
+              double alpha, uint64_t smem_per_block, uint64_t pad_blocks, Estimate* out) {
+    const int rank = static_cast<int>(dims.size());
+    Model m{elem_size == 4 ? 4u : 8u, smem_per_block};
+    const uint64_t st = m.st;
+    int64_t vol = 1;
+    for (auto d : dims) vol *= d;
+    const uint64_t data_size = static_cast<uint64_t>(vol) * st;
+    const int maxpos = static_cast<int>(std::max_element(dims.begin(), dims.end()) - dims.begin());
+    uint64_t transpose_tmp = m.series(dims, perm);
+    out->init_tmp = transpose_tmp;
+    const int percent = static_cast<int>(static_cast<double>(transpose_tmp) / static_cast<double>(data_size) / alpha);
+    int nb = percent <= 0 ? 1 : static_cast<int>(std::pow(2.0, std::ceil(std::log2(static_cast<double>(percent)))));
+    if (nb == 0) nb = 1;
+    if (transpose_tmp > 0) alpha = std::max(alpha, 1.0 / std::sqrt(static_cast<double>(vol) / 32.0));
+    const int64_t large = static_cast<int64_t>(32.0 / alpha);
+    if (!(dims[maxpos] > large && nb > 1)) {
+        out->nb = nb;
+        out->alpha = std::ceil(alpha * 100.0) / 100.0;
+        out->final_tmp = transpose_tmp;
+        out->decomposed = false;
+        return true;
+    }
+    const bool pad = dims[maxpos] % nb != 0;
+    uint64_t padding_tmp = 0;
+    if (pad) {
+        const int64_t pd = (dims[maxpos] / nb + 1) * nb;
+        padding_tmp = static_cast<uint64_t>(vol / dims[maxpos] * (pd - dims[maxpos])) * st;
+    }
+    transpose_tmp /= static_cast<uint64_t>(nb);
+    if (pad) padding_tmp = std::max<uint64_t>(padding_tmp, st * pad_blocks * 1024);
+    int64_t ds = 1;
+    for (int i = 0; i <= maxpos; ++i) ds *= dims[i];
+    uint64_t decompose_tmp = m.t132(ds / nb, nb, vol / ds);
+    int q = 0;
+    int64_t ds2 = 1;
+    for (int i = 0; i < rank; ++i) {
+        ds2 *= dims[perm[i] - 1];
+        if (perm[i] - 1 == maxpos) { q = i; break; }
+    }
+    (void)q;
+    decompose_tmp = std::max(decompose_tmp, m.t132(ds2 / nb, vol / ds2, nb));
+    uint64_t final_tmp = padding_tmp + std::max(decompose_tmp, transpose_tmp);
+    double ratio = static_cast<double>(final_tmp) / static_cast<double>(data_size);
+    if (ratio > alpha) {
+        uint64_t new_final = final_tmp;
+        int new_nb = nb;
+        while (final_tmp >= new_final && nb > 1) {
+            nb = new_nb;
+            final_tmp = new_final;
+            new_nb /= 2;
+            // The reference divides by new_nb == 0 here (SIGFPE) on the
+            // iteration that exits the loop; nb and final_tmp are final.
+            if (new_nb == 0) break;
+            const int64_t pd = (dims[maxpos] / new_nb + 1) * new_nb;
+            padding_tmp = static_cast<uint64_t>(vol / dims[maxpos] * (pd - dims[maxpos])) * st;
+            transpose_tmp *= 2;
+            decompose_tmp /= 2;
+            new_final = padding_tmp + std::max(decompose_tmp, transpose_tmp);
+        }
+        ratio = static_cast<double>(final_tmp) / static_cast<double>(data_size);
+        ratio = std::ceil(ratio * 100.0) / 100.0;
+        alpha = std::max(ratio, alpha);
+    }
+    out->nb = nb;
+    out->alpha = alpha;
+    out->final_tmp = final_tmp;
+    out->decomposed = true;
+    return true;
+}
+
+}  // namespace eithot

@@ -1,0 +1,54 @@
+// Executor interface: runs lowered passes on a stream.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "passes.h"
+
+namespace eithot {
+
+enum Status {
+    EITHOT_STATUS_OK = 0,
+    EITHOT_STATUS_INVALID = 1,
+    EITHOT_STATUS_NOMEM = 2,
+    EITHOT_STATUS_TIMEOUT = 3,
+    EITHOT_STATUS_CUDA = 4,
+    EITHOT_STATUS_UNSUPPORTED = 5,
+    EITHOT_STATUS_BUSY = 6,
+};
+
+struct ExecContext {
+    DeviceCaps caps;
+    cudaStream_t stream = nullptr;
+    uint8_t* scratch = nullptr;
+    size_t scratch_bytes = 0;
+    int launches = 0;
+    int passes = 0;
+    std::string err;
+    // When profiling, one event is recorded on `stream` before the first pass
+    // and after every pass (events[i], events[i+1] bracket pass i).
+    bool profile = false;
+    size_t events_used = 0;
+    std::vector<cudaEvent_t>* events = nullptr;
+    std::vector<std::pair<size_t, size_t>>* spans = nullptr;
+    std::vector<std::string>* names = nullptr;
+    std::vector<double>* bytes = nullptr;
+};
+
+// Minimum scratch one pass needs (one staged item), and the scratch that
+// lets it run in a single group.
+size_t pass_workspace_bytes(const Pass& p, const DeviceCaps& caps);
+size_t pass_workspace_ideal(const Pass& p, const DeviceCaps& caps);
+
+// Launches every pass in order on ctx.stream.  Returns a Status.
+int run_passes(uint8_t* data, const std::vector<Pass>& passes, ExecContext& ctx);
+
+bool query_caps(int device, DeviceCaps* caps, std::string* err);
+
+}  // namespace eithot

@@ -1,0 +1,708 @@
+// sm_103a data-movement kernels of the in-place passes, and the executor
+// that launches them for a list of passes (see passes.h).
+//
+// Each kernel moves "units" of U bytes (U in {1,2,4,8,16}, chosen from the
+// alignment of every address the pass touches); an element of E bytes is
+// split into strips of w bytes (whole elements up to 128 B) and a strip into
+// w/U units.  Row and column passes stage one item (a row strip, or a
+// column-tile strip over all rows) in shared memory, synchronise the block
+// and write the permuted item back; when an item does not fit on chip it is
+// staged in global scratch by a grid-wide copy-in launch followed by a
+// copy-out launch, one group of items at a time (stream order replaces any
+// device-wide barrier).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "exec.h"
+#include "fn_build.h"
+#include "index_math.cuh"
+#include "passes.h"
+
+namespace eithot {
+
+namespace {
+
+constexpr int kThreads = 512;
+
+template <int S> struct UnitOf;
+template <> struct UnitOf<1> { using T = uint8_t; };
+template <> struct UnitOf<2> { using T = uint16_t; };
+template <> struct UnitOf<4> { using T = uint32_t; };
+template <> struct UnitOf<8> { using T = uint2; };
+template <> struct UnitOf<16> { using T = uint4; };
+
+// Strip geometry shared by the kernels: `upw` units per full strip; the
+// last strip of an element holds `last_upw` units.
+struct StripGeom {
+    uint64_t E, w, nstrips, upw, last_upw;
+    FastDiv div_upw, div_strips;
+};
+
+// ---------------------------------------------------------------------------
+// Slab transpose: B matrices of R x C elements, one strip of one matrix per
+// work item, staged with a padded pitch so the transposed reads are
+// conflict-free.
+// ---------------------------------------------------------------------------
+struct SlabArgs {
+    uint8_t* base;
+    uint64_t B, R, C, pitch, items;
+    StripGeom g;
+    FastDiv div_C, div_R;
+};
+
+template <int US>
+__global__ void __launch_bounds__(kThreads) k_slab(SlabArgs a) {
+    using U = typename UnitOf<US>::T;
+    extern __shared__ __align__(16) uint8_t smem[];
+    const uint64_t pieces = a.R * a.C;
+    const uint64_t units = pieces * a.g.upw;
+    const uint64_t mat_bytes = pieces * a.g.E;
+    for (uint64_t it = blockIdx.x; it < a.items; it += gridDim.x) {
+        uint64_t b, s;
+        a.g.div_strips.divmod(it, b, s);
+        const uint64_t lim = (s + 1 == a.g.nstrips) ? a.g.last_upw : a.g.upw;
+        uint8_t* mat = a.base + b * mat_bytes + s * a.g.w;
+        for (uint64_t x = threadIdx.x; x < units; x += blockDim.x) {
+            uint64_t p, u;
+            a.g.div_upw.divmod(x, p, u);
+            if (u >= lim) continue;
+            uint64_t r, c;
+            a.div_C.divmod(p, r, c);
+            const U v = *reinterpret_cast<const U*>(mat + p * a.g.E + u * US);
+            *reinterpret_cast<U*>(smem + r * a.pitch + c * a.g.w + u * US) = v;
+        }
+        __syncthreads();
+        for (uint64_t x = threadIdx.x; x < units; x += blockDim.x) {
+            uint64_t o, u;
+            a.g.div_upw.divmod(x, o, u);
+            if (u >= lim) continue;
+            uint64_t c, r;  // output o = c*R + r holds input (r, c)
+            a.div_R.divmod(o, c, r);
+            const U v = *reinterpret_cast<const U*>(smem + r * a.pitch + c * a.g.w + u * US);
+            *reinterpret_cast<U*>(mat + o * a.g.E + u * US) = v;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Row pass staged on chip: item = one strip of one row (cols pieces).
+// ---------------------------------------------------------------------------
+struct RowArgs {
+    uint8_t* base;
+    uint64_t rows, cols, items;
+    StripGeom g;
+    FastDiv div_rows;
+};
+
+template <int US, typename Fn, bool kScatter>
+__global__ void __launch_bounds__(kThreads) k_row_smem(RowArgs a, Fn fn) {
+    using U = typename UnitOf<US>::T;
+    extern __shared__ __align__(16) uint8_t smem[];
+    const uint64_t units = a.cols * a.g.upw;
+    const uint64_t row_bytes = a.cols * a.g.E;
+    for (uint64_t it = blockIdx.x; it < a.items; it += gridDim.x) {
+        uint64_t bi, s;
+        a.g.div_strips.divmod(it, bi, s);
+        const uint64_t i = a.div_rows.mod(bi);
+        const uint64_t lim = (s + 1 == a.g.nstrips) ? a.g.last_upw : a.g.upw;
+        uint8_t* row = a.base + bi * row_bytes + s * a.g.w;
+        for (uint64_t x = threadIdx.x; x < units; x += blockDim.x) {
+            uint64_t j, u;
+            a.g.div_upw.divmod(x, j, u);
+            if (u >= lim) continue;
+            const U v = *reinterpret_cast<const U*>(row + j * a.g.E + u * US);
+            const uint64_t slot = kScatter ? fn(i, j) : j;
+            *reinterpret_cast<U*>(smem + slot * a.g.w + u * US) = v;
+        }
+        __syncthreads();
+        for (uint64_t x = threadIdx.x; x < units; x += blockDim.x) {
+            uint64_t j, u;
+            a.g.div_upw.divmod(x, j, u);
+            if (u >= lim) continue;
+            const uint64_t slot = kScatter ? j : fn(i, j);
+            const U v = *reinterpret_cast<const U*>(smem + slot * a.g.w + u * US);
+            *reinterpret_cast<U*>(row + j * a.g.E + u * US) = v;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Column pass staged on chip: item = one strip of a tile of tw adjacent
+// columns over all rows.
+// ---------------------------------------------------------------------------
+struct ColArgs {
+    uint8_t* base;
+    uint64_t rows, cols, tw, ntiles, pitch, items;
+    StripGeom g;
+    FastDiv div_tiles, div_rowunits;  // rowunits = tw * upw
+};
+
+template <int US, typename Fn>
+__global__ void __launch_bounds__(kThreads) k_col_smem(ColArgs a, Fn fn) {
+    using U = typename UnitOf<US>::T;
+    extern __shared__ __align__(16) uint8_t smem[];
+    const uint64_t rowunits = a.tw * a.g.upw;
+    const uint64_t units = a.rows * rowunits;
+    const uint64_t row_bytes = a.cols * a.g.E;
+    const uint64_t mat_bytes = a.rows * row_bytes;
+    for (uint64_t it = blockIdx.x; it < a.items; it += gridDim.x) {
+        uint64_t bt, s, b, t;
+        a.g.div_strips.divmod(it, bt, s);
+        a.div_tiles.divmod(bt, b, t);
+        const uint64_t col0 = t * a.tw;
+        const uint64_t tcols = min(a.tw, a.cols - col0);
+        const uint64_t lim = (s + 1 == a.g.nstrips) ? a.g.last_upw : a.g.upw;
+        uint8_t* mat = a.base + b * mat_bytes + col0 * a.g.E + s * a.g.w;
+        for (uint64_t x = threadIdx.x; x < units; x += blockDim.x) {
+            uint64_t i, r, c, u;
+            a.div_rowunits.divmod(x, i, r);
+            a.g.div_upw.divmod(r, c, u);
+            if (c >= tcols || u >= lim) continue;
+            const U v = *reinterpret_cast<const U*>(mat + i * row_bytes + c * a.g.E + u * US);
+            *reinterpret_cast<U*>(smem + i * a.pitch + c * a.g.w + u * US) = v;
+        }
+        __syncthreads();
+        for (uint64_t x = threadIdx.x; x < units; x += blockDim.x) {
+            uint64_t i, r, c, u;
+            a.div_rowunits.divmod(x, i, r);
+            a.g.div_upw.divmod(r, c, u);
+            if (c >= tcols || u >= lim) continue;
+            const uint64_t src = fn(i, col0 + c);
+            const U v = *reinterpret_cast<const U*>(smem + src * a.pitch + c * a.g.w + u * US);
+            *reinterpret_cast<U*>(mat + i * row_bytes + c * a.g.E + u * US) = v;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Grid-staged row / column passes for items larger than shared memory.
+// Items [it0, it0 + n) are copied to scratch (item-major, natural layout
+// for gathers, permuted layout for scatters) by k_*_stage_in, then written
+// back by k_*_stage_out; each launch spreads all units over the grid.
+// ---------------------------------------------------------------------------
+struct StageRowArgs {
+    uint8_t* base;
+    uint8_t* scratch;
+    uint64_t rows, cols, it0, n;
+    StripGeom g;
+    FastDiv div_rows, div_itemunits;  // itemunits = cols * upw
+};
+
+template <int US, typename Fn, bool kScatter, bool kIn>
+__global__ void __launch_bounds__(kThreads) k_row_stage(StageRowArgs a, Fn fn) {
+    using U = typename UnitOf<US>::T;
+    const uint64_t item_units = a.cols * a.g.upw;
+    const uint64_t total = a.n * item_units;
+    const uint64_t row_bytes = a.cols * a.g.E;
+    const uint64_t item_bytes = a.cols * a.g.w;
+    for (uint64_t x = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; x < total;
+         x += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t gi, rem, j, u;
+        a.div_itemunits.divmod(x, gi, rem);
+        a.g.div_upw.divmod(rem, j, u);
+        uint64_t bi, s;
+        a.g.div_strips.divmod(a.it0 + gi, bi, s);
+        const uint64_t lim = (s + 1 == a.g.nstrips) ? a.g.last_upw : a.g.upw;
+        if (u >= lim) continue;
+        const uint64_t i = a.div_rows.mod(bi);
+        uint8_t* row = a.base + bi * row_bytes + s * a.g.w;
+        uint8_t* st = a.scratch + gi * item_bytes;
+        if (kIn) {
+            const uint64_t slot = kScatter ? fn(i, j) : j;
+            *reinterpret_cast<U*>(st + slot * a.g.w + u * US) =
+                *reinterpret_cast<const U*>(row + j * a.g.E + u * US);
+        } else {
+            const uint64_t slot = kScatter ? j : fn(i, j);
+            *reinterpret_cast<U*>(row + j * a.g.E + u * US) =
+                *reinterpret_cast<const U*>(st + slot * a.g.w + u * US);
+        }
+    }
+}
+
+struct StageColArgs {
+    uint8_t* base;
+    uint8_t* scratch;
+    uint64_t rows, cols, tw, ntiles, it0, n;
+    StripGeom g;
+    FastDiv div_tiles, div_itemunits, div_rowunits;  // itemunits = rows*tw*upw
+};
+
+template <int US, typename Fn, bool kIn>
+__global__ void __launch_bounds__(kThreads) k_col_stage(StageColArgs a, Fn fn) {
+    using U = typename UnitOf<US>::T;
+    const uint64_t rowunits = a.tw * a.g.upw;
+    const uint64_t item_units = a.rows * rowunits;
+    const uint64_t total = a.n * item_units;
+    const uint64_t row_bytes = a.cols * a.g.E;
+    const uint64_t mat_bytes = a.rows * row_bytes;
+    const uint64_t spitch = a.tw * a.g.w;
+    const uint64_t item_bytes = a.rows * spitch;
+    for (uint64_t x = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; x < total;
+         x += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t gi, rem, i, r2, c, u;
+        a.div_itemunits.divmod(x, gi, rem);
+        a.div_rowunits.divmod(rem, i, r2);
+        a.g.div_upw.divmod(r2, c, u);
+        uint64_t bt, s, b, t;
+        a.g.div_strips.divmod(a.it0 + gi, bt, s);
+        a.div_tiles.divmod(bt, b, t);
+        const uint64_t col0 = t * a.tw;
+        const uint64_t lim = (s + 1 == a.g.nstrips) ? a.g.last_upw : a.g.upw;
+        if (col0 + c >= a.cols || u >= lim) continue;
+        uint8_t* mat = a.base + b * mat_bytes + col0 * a.g.E + s * a.g.w;
+        uint8_t* st = a.scratch + gi * item_bytes;
+        if (kIn) {
+            *reinterpret_cast<U*>(st + i * spitch + c * a.g.w + u * US) =
+                *reinterpret_cast<const U*>(mat + i * row_bytes + c * a.g.E + u * US);
+        } else {
+            const uint64_t src = fn(i, col0 + c);
+            *reinterpret_cast<U*>(mat + i * row_bytes + c * a.g.E + u * US) =
+                *reinterpret_cast<const U*>(st + src * spitch + c * a.g.w + u * US);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Block copy: blocks s in [s0, s0+count) of `blk` bytes move from
+// src + s*sp to dst + s*dp.  The host guarantees that no destination of the
+// launch overlaps a source of the launch.
+// ---------------------------------------------------------------------------
+struct BlockArgs {
+    const uint8_t* src;
+    uint8_t* dst;
+    uint64_t blk, sp, dp, s0, count;
+    FastDiv div_blkunits;
+};
+
+template <int US>
+__global__ void __launch_bounds__(kThreads) k_block_copy(BlockArgs a) {
+    using U = typename UnitOf<US>::T;
+    const uint64_t bu = a.blk / US;
+    const uint64_t total = a.count * bu;
+    for (uint64_t x = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; x < total;
+         x += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t k, u;
+        a.div_blkunits.divmod(x, k, u);
+        const uint64_t s = a.s0 + k;
+        *reinterpret_cast<U*>(a.dst + s * a.dp + u * US) =
+            *reinterpret_cast<const U*>(a.src + s * a.sp + u * US);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+
+uint64_t pow2_div(uint64_t v) {
+    uint64_t u = 1;
+    while (u < 16 && v % (u * 2) == 0) u *= 2;
+    return u;
+}
+
+uint64_t unit_for(std::initializer_list<uint64_t> vals) {
+    uint64_t u = 16;
+    for (uint64_t v : vals) u = std::min(u, pow2_div(v));
+    return u;
+}
+
+StripGeom make_strips(uint64_t E, uint64_t w, uint64_t U, uint64_t outer, uint64_t extra_units_bound) {
+    StripGeom g;
+    g.E = E;
+    g.w = w;
+    g.nstrips = (E + w - 1) / w;
+    g.upw = w / U;
+    const uint64_t last = E - (g.nstrips - 1) * w;
+    g.last_upw = last / U;
+    g.div_upw = FastDiv::make(g.upw, extra_units_bound);
+    g.div_strips = FastDiv::make(g.nstrips, outer * g.nstrips);
+    return g;
+}
+
+int grid_for(const void* kernel, size_t smem, uint64_t items, const ExecContext& ctx) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem);
+    if (per_sm < 1) per_sm = 1;
+    const uint64_t cap = static_cast<uint64_t>(per_sm) * ctx.caps.sms;
+    return static_cast<int>(std::max<uint64_t>(1, std::min<uint64_t>(items, cap)));
+}
+
+int grid_for_elems(uint64_t total, const ExecContext& ctx) {
+    const uint64_t blocks = (total + kThreads - 1) / kThreads;
+    const uint64_t cap = static_cast<uint64_t>(ctx.caps.sms) * 4;
+    return static_cast<int>(std::max<uint64_t>(1, std::min<uint64_t>(blocks, cap)));
+}
+
+cudaError_t prep_smem(const void* kernel, size_t smem) {
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                static_cast<int>(smem));
+}
+
+#define EI_CHECK(expr)                                                    \
+    do {                                                                  \
+        cudaError_t e__ = (expr);                                         \
+        if (e__ != cudaSuccess) {                                         \
+            ctx.err = std::string(#expr) + ": " + cudaGetErrorString(e__); \
+            return EITHOT_STATUS_CUDA;                                    \
+        }                                                                 \
+    } while (0)
+
+// ---- slab ----------------------------------------------------------------
+template <int US>
+int launch_slab(uint8_t* data, const Pass& p, ExecContext& ctx) {
+    SlabArgs a;
+    a.base = data + p.offset;
+    a.B = p.batches; a.R = p.rows; a.C = p.cols;
+    a.pitch = slab_pitch(p.cols, p.strip);
+    const uint64_t upw = p.strip / US;
+    a.g = make_strips(p.elem, p.strip, US, p.batches, p.rows * p.cols * upw);
+    a.items = p.batches * a.g.nstrips;
+    a.div_C = FastDiv::make(p.cols, p.rows * p.cols);
+    a.div_R = FastDiv::make(p.rows, p.rows * p.cols);
+    const size_t smem = slab_smem_bytes(p.rows, p.cols, p.strip);
+    const void* k = reinterpret_cast<const void*>(&k_slab<US>);
+    EI_CHECK(prep_smem(k, smem));
+    const int grid = grid_for(k, smem, a.items, ctx);
+    k_slab<US><<<grid, kThreads, smem, ctx.stream>>>(a);
+    EI_CHECK(cudaGetLastError());
+    ctx.launches++;
+    return 0;
+}
+
+// ---- rows ------------------------------------------------------------------
+template <int US, typename Fn, bool kScatter>
+int launch_row(uint8_t* data, const Pass& p, const Fn& fn, ExecContext& ctx) {
+    const size_t cap = smem_cap_of(ctx.caps);
+    const Staging st = plan_row_staging(p.cols, p.elem, cap);
+    const uint64_t upw = st.w / US;
+    const StripGeom g = make_strips(p.elem, st.w, US, p.batches * p.rows, p.cols * upw);
+    const uint64_t items = p.batches * p.rows * g.nstrips;
+    if (st.on_chip) {
+        RowArgs a;
+        a.base = data + p.offset;
+        a.rows = p.rows; a.cols = p.cols; a.items = items;
+        a.g = g;
+        a.div_rows = FastDiv::make(p.rows, p.batches * p.rows);
+        const size_t smem = p.cols * st.w;
+        const void* k = reinterpret_cast<const void*>(&k_row_smem<US, Fn, kScatter>);
+        EI_CHECK(prep_smem(k, smem));
+        const int grid = grid_for(k, smem, items, ctx);
+        k_row_smem<US, Fn, kScatter><<<grid, kThreads, smem, ctx.stream>>>(a, fn);
+        EI_CHECK(cudaGetLastError());
+        ctx.launches++;
+        return 0;
+    }
+    const uint64_t item_bytes = p.cols * st.w;
+    if (ctx.scratch_bytes < item_bytes || ctx.scratch == nullptr) {
+        ctx.err = "workspace too small for a staged row pass";
+        return EITHOT_STATUS_NOMEM;
+    }
+    const uint64_t per_group = std::max<uint64_t>(1, ctx.scratch_bytes / item_bytes);
+    StageRowArgs a;
+    a.base = data + p.offset;
+    a.scratch = ctx.scratch;
+    a.rows = p.rows; a.cols = p.cols;
+    a.g = g;
+    a.div_rows = FastDiv::make(p.rows, p.batches * p.rows);
+    a.div_itemunits = FastDiv::make(p.cols * upw, per_group * p.cols * upw);
+    for (uint64_t it0 = 0; it0 < items; it0 += per_group) {
+        a.it0 = it0;
+        a.n = std::min<uint64_t>(per_group, items - it0);
+        const int grid = grid_for_elems(a.n * p.cols * upw, ctx);
+        k_row_stage<US, Fn, kScatter, true><<<grid, kThreads, 0, ctx.stream>>>(a, fn);
+        k_row_stage<US, Fn, kScatter, false><<<grid, kThreads, 0, ctx.stream>>>(a, fn);
+        EI_CHECK(cudaGetLastError());
+        ctx.launches += 2;
+    }
+    return 0;
+}
+
+// ---- columns ---------------------------------------------------------------
+template <int US, typename Fn>
+int launch_col(uint8_t* data, const Pass& p, const Fn& fn, ExecContext& ctx) {
+    const size_t cap = smem_cap_of(ctx.caps);
+    const Staging st = plan_col_staging(p.rows, p.elem, cap);
+    const uint64_t upw = st.w / US;
+    const uint64_t ntiles = (p.cols + st.tw - 1) / st.tw;
+    const StripGeom g = make_strips(p.elem, st.w, US, p.batches * ntiles, p.rows * st.tw * upw);
+    const uint64_t items = p.batches * ntiles * g.nstrips;
+    if (st.on_chip) {
+        ColArgs a;
+        a.base = data + p.offset;
+        a.rows = p.rows; a.cols = p.cols; a.tw = st.tw; a.ntiles = ntiles; a.pitch = st.pitch;
+        a.items = items;
+        a.g = g;
+        a.div_tiles = FastDiv::make(ntiles, p.batches * ntiles);
+        a.div_rowunits = FastDiv::make(st.tw * upw, p.rows * st.tw * upw);
+        const size_t smem = st.item_bytes;
+        const void* k = reinterpret_cast<const void*>(&k_col_smem<US, Fn>);
+        EI_CHECK(prep_smem(k, smem));
+        const int grid = grid_for(k, smem, items, ctx);
+        k_col_smem<US, Fn><<<grid, kThreads, smem, ctx.stream>>>(a, fn);
+        EI_CHECK(cudaGetLastError());
+        ctx.launches++;
+        return 0;
+    }
+    const uint64_t item_bytes = p.rows * st.tw * st.w;
+    if (ctx.scratch_bytes < item_bytes || ctx.scratch == nullptr) {
+        ctx.err = "workspace too small for a staged column pass";
+        return EITHOT_STATUS_NOMEM;
+    }
+    const uint64_t per_group = std::max<uint64_t>(1, ctx.scratch_bytes / item_bytes);
+    StageColArgs a;
+    a.base = data + p.offset;
+    a.scratch = ctx.scratch;
+    a.rows = p.rows; a.cols = p.cols; a.tw = st.tw; a.ntiles = ntiles;
+    a.g = g;
+    a.div_tiles = FastDiv::make(ntiles, p.batches * ntiles);
+    const uint64_t item_units = p.rows * st.tw * upw;
+    a.div_itemunits = FastDiv::make(item_units, per_group * item_units);
+    a.div_rowunits = FastDiv::make(st.tw * upw, item_units);
+    for (uint64_t it0 = 0; it0 < items; it0 += per_group) {
+        a.it0 = it0;
+        a.n = std::min<uint64_t>(per_group, items - it0);
+        const int grid = grid_for_elems(a.n * item_units, ctx);
+        k_col_stage<US, Fn, true><<<grid, kThreads, 0, ctx.stream>>>(a, fn);
+        k_col_stage<US, Fn, false><<<grid, kThreads, 0, ctx.stream>>>(a, fn);
+        EI_CHECK(cudaGetLastError());
+        ctx.launches += 2;
+    }
+    return 0;
+}
+
+// ---- block moves -------------------------------------------------------------
+template <int US>
+int copy_blocks(const uint8_t* src, uint8_t* dst, uint64_t blk, uint64_t sp, uint64_t dp,
+                uint64_t s0, uint64_t count, ExecContext& ctx) {
+    if (count == 0 || blk == 0) return 0;
+    BlockArgs a;
+    a.src = src; a.dst = dst; a.blk = blk; a.sp = sp; a.dp = dp; a.s0 = s0; a.count = count;
+    a.div_blkunits = FastDiv::make(blk / US, count * (blk / US));
+    const int grid = grid_for_elems(count * (blk / US), ctx);
+    k_block_copy<US><<<grid, kThreads, 0, ctx.stream>>>(a);
+    EI_CHECK(cudaGetLastError());
+    ctx.launches++;
+    return 0;
+}
+
+// Moves blocks s = 1..n-1 (block 0 never moves) from s*sp to s*dp in place.
+// Spreading (dp > sp) proceeds from the last block down, compacting from
+// the first block up, so a launch never overwrites a block that has not
+// been moved yet; a launch whose blocks would overlap themselves goes
+// through scratch.
+template <int US>
+int block_move(uint8_t* data, const Pass& p, ExecContext& ctx) {
+    const uint64_t n = p.n_blocks, blk = p.block, sp = p.src_pitch, dp = p.dst_pitch;
+    if (n <= 1 || sp == dp) return 0;
+    const uint64_t scratch_blocks = ctx.scratch ? ctx.scratch_bytes / blk : 0;
+    int rc;
+    if (dp > sp) {
+        uint64_t s = n - 1;  // highest block not yet moved
+        while (s >= 1) {
+            if (s * (dp - sp) >= blk) {
+                // blocks [lo, s] whose destinations lie above every source among them
+                uint64_t lo = (s * sp + blk + dp - 1) / dp;
+                lo = std::max<uint64_t>(1, std::min(lo, s));
+                if ((rc = copy_blocks<US>(data, data, blk, sp, dp, lo, s - lo + 1, ctx))) return rc;
+                s = lo - 1;
+            } else {
+                if (scratch_blocks == 0) { ctx.err = "workspace too small for padding"; return EITHOT_STATUS_NOMEM; }
+                const uint64_t lo = s + 1 > scratch_blocks ? std::max<uint64_t>(1, s + 1 - scratch_blocks) : 1;
+                const uint64_t cnt = s - lo + 1;
+                if ((rc = copy_blocks<US>(data + lo * sp, ctx.scratch, blk, sp, blk, 0, cnt, ctx))) return rc;
+                if ((rc = copy_blocks<US>(ctx.scratch, data + lo * dp, blk, blk, dp, 0, cnt, ctx))) return rc;
+                s = lo - 1;
+            }
+        }
+    } else {
+        uint64_t s = 1;  // lowest block not yet moved
+        while (s < n) {
+            if (s * (sp - dp) >= blk) {
+                // blocks [s, hi) whose destinations all lie below the lowest
+                // source among them: (hi-1)*dp + blk <= s*sp
+                uint64_t hi = (s * sp - blk) / dp + 1;
+                hi = std::min<uint64_t>(std::max<uint64_t>(hi, s + 1), n);
+                if ((rc = copy_blocks<US>(data, data, blk, sp, dp, s, hi - s, ctx))) return rc;
+                s = hi;
+            } else {
+                if (scratch_blocks == 0) { ctx.err = "workspace too small for padding"; return EITHOT_STATUS_NOMEM; }
+                const uint64_t cnt = std::min<uint64_t>(scratch_blocks, n - s);
+                if ((rc = copy_blocks<US>(data + s * sp, ctx.scratch, blk, sp, blk, 0, cnt, ctx))) return rc;
+                if ((rc = copy_blocks<US>(ctx.scratch, data + s * dp, blk, blk, dp, 0, cnt, ctx))) return rc;
+                s += cnt;
+            }
+        }
+    }
+    return 0;
+}
+
+// ---- dispatch ------------------------------------------------------------------
+template <int US>
+int run_pass_u(uint8_t* data, const Pass& p, ExecContext& ctx) {
+    switch (p.type) {
+        case kSlabTranspose: return launch_slab<US>(data, p, ctx);
+        case kRowGather:
+            return launch_row<US, FnRowShuffle, false>(data, p, make_rowshuffle(p), ctx);
+        case kRowScatter:
+            return launch_row<US, FnRowShuffle, true>(data, p, make_rowshuffle(p), ctx);
+        case kColGather:
+            switch (p.fn) {
+                case kFnC2RPreRot: return launch_col<US, FnC2RPreRot>(data, p, make_prerot(p), ctx);
+                case kFnC2RColShuffle: return launch_col<US, FnC2RColShuffle>(data, p, make_c2r_colshuf(p), ctx);
+                case kFnR2CColShuffle: return launch_col<US, FnR2CColShuffle>(data, p, make_r2c_colshuf(p), ctx);
+                case kFnR2CPostRot: return launch_col<US, FnR2CPostRot>(data, p, make_postrot(p), ctx);
+                default: break;
+            }
+            break;
+        case kBlockMove: return block_move<US>(data, p, ctx);
+        default: break;
+    }
+    ctx.err = "internal: unknown pass";
+    return EITHOT_STATUS_INVALID;
+}
+
+uint64_t pass_unit(const uint8_t* data, const Pass& p, size_t smem_cap) {
+    const uint64_t addr = reinterpret_cast<uintptr_t>(data) + p.offset;
+    switch (p.type) {
+        case kSlabTranspose:
+            return unit_for({addr, p.elem, p.strip, p.elem % p.strip == 0 ? p.strip : p.elem % p.strip});
+        case kRowGather:
+        case kRowScatter: {
+            const Staging st = plan_row_staging(p.cols, p.elem, smem_cap);
+            return unit_for({addr, p.elem, st.w, p.elem % st.w == 0 ? st.w : p.elem % st.w});
+        }
+        case kColGather: {
+            const Staging st = plan_col_staging(p.rows, p.elem, smem_cap);
+            return unit_for({addr, p.elem, st.w, st.pitch, p.elem % st.w == 0 ? st.w : p.elem % st.w});
+        }
+        case kBlockMove:
+            return unit_for({addr, p.block, p.src_pitch, p.dst_pitch});
+        default:
+            return 1;
+    }
+}
+
+}  // namespace
+
+size_t pass_workspace_bytes(const Pass& p, const DeviceCaps& caps) {
+    const size_t cap = smem_cap_of(caps);
+    switch (p.type) {
+        case kRowGather:
+        case kRowScatter: {
+            const Staging st = plan_row_staging(p.cols, p.elem, cap);
+            return st.on_chip ? 0 : p.cols * st.w;
+        }
+        case kColGather: {
+            const Staging st = plan_col_staging(p.rows, p.elem, cap);
+            return st.on_chip ? 0 : p.rows * st.tw * st.w;
+        }
+        case kBlockMove: {
+            // scratch is needed only where a block's shift is smaller than
+            // the block itself
+            const uint64_t sh = p.dst_pitch > p.src_pitch ? p.dst_pitch - p.src_pitch : p.src_pitch - p.dst_pitch;
+            if (p.n_blocks <= 1 || sh == 0) return 0;
+            return sh >= p.block ? 0 : p.block;
+        }
+        default:
+            return 0;
+    }
+}
+
+size_t pass_workspace_ideal(const Pass& p, const DeviceCaps& caps) {
+    const size_t cap = smem_cap_of(caps);
+    switch (p.type) {
+        case kRowGather:
+        case kRowScatter: {
+            const Staging st = plan_row_staging(p.cols, p.elem, cap);
+            if (st.on_chip) return 0;
+            const uint64_t ns = (p.elem + st.w - 1) / st.w;
+            return p.batches * p.rows * ns * p.cols * st.w;
+        }
+        case kColGather: {
+            const Staging st = plan_col_staging(p.rows, p.elem, cap);
+            if (st.on_chip) return 0;
+            const uint64_t ns = (p.elem + st.w - 1) / st.w;
+            const uint64_t nt = (p.cols + st.tw - 1) / st.tw;
+            return p.batches * nt * ns * p.rows * st.tw * st.w;
+        }
+        case kBlockMove:
+            return pass_workspace_bytes(p, caps) ? p.block * std::max<uint64_t>(1, p.n_blocks - 1) : 0;
+        default:
+            return 0;
+    }
+}
+
+int run_passes(uint8_t* data, const std::vector<Pass>& passes, ExecContext& ctx) {
+    const size_t cap = smem_cap_of(ctx.caps);
+    // Profiling appends one event before the first pass and one after each
+    // pass to the caller's pool; pass k spans events (first + k, first + k + 1).
+    size_t ev = ctx.profile ? ctx.events_used : 0;
+    auto record = [&]() -> int {
+        if (!ctx.profile) return 0;
+        if (ev == ctx.events->size()) {
+            cudaEvent_t e;
+            EI_CHECK(cudaEventCreate(&e));
+            ctx.events->push_back(e);
+        }
+        EI_CHECK(cudaEventRecord((*ctx.events)[ev++], ctx.stream));
+        return 0;
+    };
+    if (ctx.profile) {
+        if (int rc = record()) return rc;
+    }
+    for (const Pass& p : passes) {
+        const uint64_t U = pass_unit(data, p, cap);
+        int rc;
+        switch (U) {
+            case 16: rc = run_pass_u<16>(data, p, ctx); break;
+            case 8: rc = run_pass_u<8>(data, p, ctx); break;
+            case 4: rc = run_pass_u<4>(data, p, ctx); break;
+            case 2: rc = run_pass_u<2>(data, p, ctx); break;
+            default: rc = run_pass_u<1>(data, p, ctx); break;
+        }
+        if (rc) return rc;
+        ctx.passes++;
+        if (ctx.profile) {
+            if ((rc = record())) return rc;
+            ctx.spans->push_back({ev - 2, ev - 1});
+            ctx.names->push_back(p.what);
+            const double moved = p.type == kBlockMove
+                ? 2.0 * static_cast<double>(p.block) * static_cast<double>(p.n_blocks > 0 ? p.n_blocks - 1 : 0)
+                : 2.0 * static_cast<double>(p.batches) * p.rows * p.cols * p.elem;
+            ctx.bytes->push_back(moved);
+        }
+    }
+    if (ctx.profile) ctx.events_used = ev;
+    return 0;
+}
+
+bool query_caps(int device, DeviceCaps* caps, std::string* err) {
+    static std::mutex mu;
+    static std::vector<std::pair<int, DeviceCaps>> cache;
+    std::lock_guard<std::mutex> lock(mu);
+    for (auto& e : cache) if (e.first == device) { *caps = e.second; return true; }
+    DeviceCaps c;
+    int v = 0;
+    cudaError_t e = cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device);
+    if (e != cudaSuccess) { *err = cudaGetErrorString(e); return false; }
+    c.sms = v;
+    e = cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    if (e != cudaSuccess) { *err = cudaGetErrorString(e); return false; }
+    c.smem_optin = static_cast<size_t>(v);
+    e = cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device);
+    if (e != cudaSuccess) { *err = cudaGetErrorString(e); return false; }
+    c.smem_per_sm = static_cast<size_t>(v);
+    cache.emplace_back(device, c);
+    *caps = c;
+    return true;
+}
+
+}  // namespace eithot

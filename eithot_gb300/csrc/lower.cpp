@@ -1,0 +1,241 @@
+// Lowering of an N-d plan to device passes (see passes.h).
+#include "passes.h"
+
+#include <algorithm>
+#include <sstream>
+
+namespace eithot {
+
+void gcd_inverse(uint64_t a, uint64_t b, uint64_t* g, uint64_t* inv) {
+    // Extended Euclid on (a, b); inv = a^-1 mod b when gcd == 1, 0 if b == 1.
+    __int128 r0 = static_cast<__int128>(a), r1 = static_cast<__int128>(b);
+    __int128 s0 = 1, s1 = 0;
+    while (r1 != 0) {
+        const __int128 qt = r0 / r1;
+        const __int128 r2 = r0 - qt * r1;
+        r0 = r1; r1 = r2;
+        const __int128 s2 = s0 - qt * s1;
+        s0 = s1; s1 = s2;
+    }
+    *g = static_cast<uint64_t>(r0);
+    if (r0 != 1 || b <= 1) { *inv = 0; return; }
+    __int128 x = s0 % static_cast<__int128>(b);
+    if (x < 0) x += b;
+    *inv = static_cast<uint64_t>(x);
+}
+
+size_t smem_cap_of(const DeviceCaps& caps) {
+    // Leave room for the block's static shared memory and the driver's
+    // per-block reservation.
+    return caps.smem_optin > 2048 ? caps.smem_optin - 2048 : caps.smem_optin;
+}
+
+uint64_t strip_width(uint64_t E) { return E <= 128 ? E : 128; }
+
+namespace {
+uint64_t pow2_divisor(uint64_t v, uint64_t cap) {
+    uint64_t u = 1;
+    while (u < cap && v % (u * 2) == 0) u *= 2;
+    return u;
+}
+}  // namespace
+
+uint64_t slab_pitch(uint64_t C, uint64_t w) {
+    const uint64_t g = std::max<uint64_t>(4, pow2_divisor(w, 16));
+    uint64_t pitch = (C * w + g - 1) / g * g;
+    if ((pitch / g) % 2 == 0) pitch += g;
+    return pitch;
+}
+
+size_t slab_smem_bytes(uint64_t R, uint64_t C, uint64_t w) { return R * slab_pitch(C, w); }
+
+Staging plan_row_staging(uint64_t cols, uint64_t E, size_t cap) {
+    Staging s;
+    const uint64_t w0 = strip_width(E);
+    for (uint64_t w : {w0, uint64_t(64), uint64_t(32)}) {
+        if (w > w0 || w < std::min<uint64_t>(E, 32)) continue;
+        if (cols * w <= cap) {
+            s.w = w; s.item_bytes = cols * w; s.on_chip = true;
+            return s;
+        }
+    }
+    s.w = w0;
+    s.item_bytes = cols * w0;
+    s.on_chip = false;
+    return s;
+}
+
+Staging plan_col_staging(uint64_t rows, uint64_t E, size_t cap) {
+    Staging s;
+    for (uint64_t tb : {uint64_t(128), uint64_t(64), uint64_t(32)}) {
+        uint64_t w, tw;
+        if (E <= tb) { w = E; tw = std::max<uint64_t>(1, tb / E); }
+        else { w = tb; tw = 1; }
+        const uint64_t pitch = slab_pitch(tw, w);
+        if (rows * pitch <= cap) {
+            s.w = w; s.tw = tw; s.pitch = pitch; s.item_bytes = rows * pitch; s.on_chip = true;
+            return s;
+        }
+    }
+    // Global staging: 128-byte row pieces.
+    s.w = E <= 128 ? E : 128;
+    s.tw = E <= 128 ? std::max<uint64_t>(1, 128 / E) : 1;
+    s.pitch = s.tw * s.w;
+    s.item_bytes = rows * s.pitch;
+    s.on_chip = false;
+    return s;
+}
+
+Xpose xpose_of(const LowOp& op, uint64_t elem, uint64_t n_sub, uint64_t base_offset) {
+    Xpose x;
+    x.offset = base_offset;
+    const uint64_t* d = reinterpret_cast<const uint64_t*>(op.dims);
+    switch (op.code()) {
+        case 21:   x.B = n_sub;        x.R = d[1];        x.C = d[0];        x.E = elem; break;
+        case 213:  x.B = n_sub * d[2]; x.R = d[1];        x.C = d[0];        x.E = elem; break;
+        case 132:  x.B = n_sub;        x.R = d[2];        x.C = d[1];        x.E = d[0] * elem; break;
+        case 1324: x.B = n_sub * d[3]; x.R = d[2];        x.C = d[1];        x.E = d[0] * elem; break;
+        case 231:  x.B = n_sub;        x.R = d[1] * d[2]; x.C = d[0];        x.E = elem; break;
+        case 312:  x.B = n_sub;        x.R = d[2];        x.C = d[0] * d[1]; x.E = elem; break;
+        default:   x.B = 0; break;  // never produced by the planner
+    }
+    return x;
+}
+
+namespace {
+
+double row_cost(uint64_t cols, uint64_t E, size_t cap) {
+    return plan_row_staging(cols, E, cap).on_chip ? 1.0 : 2.0;
+}
+double col_cost(uint64_t rows, uint64_t E, size_t cap) {
+    return plan_col_staging(rows, E, cap).on_chip ? 1.0 : 2.0;
+}
+
+std::string geom(const char* name, uint64_t B, uint64_t r, uint64_t c, uint64_t E) {
+    std::ostringstream os;
+    os << name << " B=" << B << " rows=" << r << " cols=" << c << " E=" << E;
+    return os.str();
+}
+
+}  // namespace
+
+void lower_xpose(const Xpose& x, const DeviceCaps& caps, std::vector<Pass>* passes) {
+    if (x.B == 0 || x.R <= 1 || x.C <= 1) return;  // identity
+    const size_t cap = smem_cap_of(caps);
+    const uint64_t w0 = strip_width(x.E);
+    for (uint64_t w : {w0, uint64_t(64), uint64_t(32)}) {
+        if (w > w0 || w < std::min<uint64_t>(x.E, 32)) continue;
+        if (slab_smem_bytes(x.R, x.C, w) <= cap) {
+            Pass p;
+            p.type = kSlabTranspose;
+            p.offset = x.offset;
+            p.batches = x.B; p.rows = x.R; p.cols = x.C; p.elem = x.E;
+            p.strip = w;
+            p.what = geom("slab", x.B, x.R, x.C, x.E);
+            passes->push_back(p);
+            return;
+        }
+    }
+    // Catanzaro: c2r on the R x C view, or r2c on the C x R view.
+    uint64_t g, inv;
+    gcd_inverse(x.R, x.C, &g, &inv);
+    const double c2r = (g > 1 ? col_cost(x.R, x.E, cap) : 0.0) + row_cost(x.C, x.E, cap) + col_cost(x.R, x.E, cap);
+    const double r2c = col_cost(x.C, x.E, cap) + row_cost(x.R, x.E, cap) + (g > 1 ? col_cost(x.C, x.E, cap) : 0.0);
+    const bool use_c2r = (c2r < r2c) || (c2r == r2c && x.C >= x.R);
+    Pass base;
+    base.offset = x.offset;
+    base.batches = x.B;
+    base.elem = x.E;
+    if (use_c2r) {
+        const uint64_t m = x.R, n = x.C;
+        uint64_t unused, k;
+        gcd_inverse(m / g, n / g, &unused, &k);  // k = (m/g)^-1 mod (n/g)
+        base.rows = m; base.cols = n;
+        base.m = m; base.n = n; base.c = g; base.k = k; base.a = m / g; base.b = n / g;
+        if (g > 1) {
+            Pass p = base; p.type = kColGather; p.fn = kFnC2RPreRot;
+            p.what = geom("c2r-prerotate", x.B, m, n, x.E);
+            passes->push_back(p);
+        }
+        Pass p1 = base; p1.type = kRowGather; p1.fn = kFnRowShuffle;
+        p1.what = geom("c2r-rowshuffle", x.B, m, n, x.E);
+        passes->push_back(p1);
+        Pass p2 = base; p2.type = kColGather; p2.fn = kFnC2RColShuffle;
+        p2.what = geom("c2r-colshuffle", x.B, m, n, x.E);
+        passes->push_back(p2);
+    } else {
+        const uint64_t m = x.C, n = x.R;  // the output's view: C rows x R cols
+        uint64_t unused, q, k;
+        gcd_inverse(n / g, m / g, &unused, &q);  // q = (n/g)^-1 mod (m/g)
+        gcd_inverse(m / g, n / g, &unused, &k);  // k = (m/g)^-1 mod (n/g)
+        base.rows = m; base.cols = n;
+        base.m = m; base.n = n; base.c = g; base.k = k; base.q = q; base.a = m / g; base.b = n / g;
+        Pass p0 = base; p0.type = kColGather; p0.fn = kFnR2CColShuffle;
+        p0.what = geom("r2c-colshuffle", x.B, m, n, x.E);
+        passes->push_back(p0);
+        Pass p1 = base; p1.type = kRowScatter; p1.fn = kFnRowShuffle;
+        p1.what = geom("r2c-rowscatter", x.B, m, n, x.E);
+        passes->push_back(p1);
+        if (g > 1) {
+            Pass p2 = base; p2.type = kColGather; p2.fn = kFnR2CPostRot;
+            p2.what = geom("r2c-postrotate", x.B, m, n, x.E);
+            passes->push_back(p2);
+        }
+    }
+}
+
+bool lower_plan(const NdPlan& plan, uint64_t elem, const DeviceCaps& caps,
+                std::vector<Pass>* passes, std::string* err) {
+    for (const NdStep& st : plan.steps) {
+        switch (st.role) {
+            case kPadPre: {
+                const auto& d = st.pad_layout;
+                const int p = st.pad_pos;
+                uint64_t lo = 1, hi = 1;
+                for (int i = 0; i < p; ++i) lo *= d[i];
+                for (size_t i = p + 1; i < d.size(); ++i) hi *= d[i];
+                Pass ps;
+                ps.type = kBlockMove;
+                ps.block = lo * d[p] * elem;
+                ps.n_blocks = hi;
+                ps.src_pitch = lo * d[p] * elem;
+                ps.dst_pitch = lo * st.pad_size * elem;
+                ps.what = "pad-spread";
+                passes->push_back(ps);
+                break;
+            }
+            case kPadPost: {
+                const auto& d = st.pad_layout;
+                const int q = st.pad_pos;
+                uint64_t lo = 1, hi = 1;
+                for (int i = 0; i < q; ++i) lo *= d[i];
+                for (size_t i = q + 1; i < d.size(); ++i) hi *= d[i];
+                Pass ps;
+                ps.type = kBlockMove;
+                ps.block = lo * st.pad_orig * elem;
+                ps.n_blocks = hi;
+                ps.src_pitch = lo * st.pad_size * elem;
+                ps.dst_pitch = lo * st.pad_orig * elem;
+                ps.what = "pad-compact";
+                passes->push_back(ps);
+                break;
+            }
+            case kPartition:
+            case kJoin:
+                lower_xpose(xpose_of(st.op, elem, 1, 0), caps, passes);
+                break;
+            case kRound: {
+                const Xpose x = xpose_of(st.op, elem, static_cast<uint64_t>(plan.nb), 0);
+                if (x.B == 0) { *err = "internal: unsupported low-order permutation"; return false; }
+                lower_xpose(x, caps, passes);
+                break;
+            }
+            default:
+                *err = "internal: unknown step";
+                return false;
+        }
+    }
+    return true;
+}
+
+}  // namespace eithot

@@ -1,0 +1,103 @@
+// Device passes: the lowering of an N-d plan into in-place data movements.
+//
+// Every low-order transpose of the series, and the partition / join steps,
+// is a batched in-place transpose X(B, R, C, E): B contiguous R x C
+// row-major matrices of E-byte elements each become C x R.  X is executed
+// either as one "slab" pass (each matrix staged whole on chip) or as the
+// two/three Catanzaro passes (c2r on the R x C view or r2c on the C x R
+// view).  Padding steps are block moves.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "plan.h"
+
+namespace eithot {
+
+enum PassType {
+    kSlabTranspose = 0,  // each of B matrices (R x C) transposed on chip
+    kRowGather = 1,      // out[i][j] = in[i][f(i,j)]
+    kRowScatter = 2,     // out[i][f(i,j)] = in[i][j]
+    kColGather = 3,      // out[i][j] = in[g(i,j)][j]
+    kBlockMove = 4,      // n_blocks blocks of `block` bytes: s*src_pitch -> s*dst_pitch
+};
+
+enum FnType {
+    kFnNone = 0,
+    kFnRowShuffle = 1,
+    kFnC2RPreRot = 2,
+    kFnC2RColShuffle = 3,
+    kFnR2CColShuffle = 4,
+    kFnR2CPostRot = 5,
+};
+
+struct Pass {
+    int type = kSlabTranspose;
+    int fn = kFnNone;
+    uint64_t offset = 0;                 // byte offset of the first batch
+    uint64_t batches = 1, rows = 1, cols = 1, elem = 1;
+    // Catanzaro parameters of the view (m rows x n cols)
+    uint64_t m = 0, n = 0, c = 1, k = 0, a = 0, b = 0, q = 0;
+    uint64_t strip = 0;                  // slab passes: strip width in bytes
+    // block moves
+    uint64_t block = 0, n_blocks = 0, src_pitch = 0, dst_pitch = 0;
+    std::string what;
+};
+
+// One batched in-place transpose.
+struct Xpose {
+    uint64_t offset = 0, B = 1, R = 1, C = 1, E = 1;
+};
+
+// Device resources the lowering and the executor size against.
+struct DeviceCaps {
+    int sms = 152;
+    size_t smem_optin = 232448;      // max dynamic shared memory per block (227 KiB)
+    size_t smem_per_sm = 233472;
+    int max_cluster = 8;             // portable cluster size
+};
+
+// Shared memory the single-CTA kernels may use per block.
+size_t smem_cap_of(const DeviceCaps& caps);
+
+// How one item of a row or column pass is staged.  A row item is one strip
+// (w bytes of every element) of one row; a column item is one strip of a
+// tile of `tw` adjacent columns over all rows.
+struct Staging {
+    uint64_t w = 0;        // strip width in bytes
+    uint64_t tw = 1;       // columns per item (column passes)
+    uint64_t pitch = 0;    // bytes per staged row (column passes)
+    uint64_t item_bytes = 0;
+    bool on_chip = false;  // fits one CTA's shared memory
+};
+
+Staging plan_row_staging(uint64_t cols, uint64_t E, size_t smem_cap);
+Staging plan_col_staging(uint64_t rows, uint64_t E, size_t smem_cap);
+
+// Lowers every step of `plan` for element size `elem` into passes.
+bool lower_plan(const NdPlan& plan, uint64_t elem, const DeviceCaps& caps,
+                std::vector<Pass>* passes, std::string* err);
+
+// Lowers one batched transpose (exposed for tests).
+void lower_xpose(const Xpose& x, const DeviceCaps& caps, std::vector<Pass>* passes);
+
+// Maps one low-order op acting on `n_sub` back-to-back sub-tensors onto a
+// batched transpose.
+Xpose xpose_of(const LowOp& op, uint64_t elem, uint64_t n_sub, uint64_t base_offset);
+
+// Extended Euclid: gcd and the inverse of a mod b (0 when b == 1).
+void gcd_inverse(uint64_t a, uint64_t b, uint64_t* g, uint64_t* inv);
+
+// Slab transposes stage an R x C matrix of w-byte pieces with a padded row
+// pitch so that the transposed reads hit distinct banks.
+uint64_t slab_pitch(uint64_t C, uint64_t w);
+size_t slab_smem_bytes(uint64_t R, uint64_t C, uint64_t w);
+
+// Strip width (bytes) for elements of E bytes: whole elements up to 128 B,
+// 128-byte strips of larger elements.
+uint64_t strip_width(uint64_t E);
+
+}  // namespace eithot

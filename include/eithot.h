@@ -1,0 +1,178 @@
+/*
+ * eithot.h — C ABI of the GB300 (sm_103a) in-place high-order tensor transposer.
+ *
+ * Layout convention (identical to EITHOT): a tensor of rank r with dims
+ * (d0, d1, ..., d{r-1}) is stored with d0 the fastest-varying axis
+ * (stride 1), d1 next, and so on (ITNT/src/Nd_transpose.cpp:53-59,
+ * ITNT/src/tensor_util.cpp:27-29).  A permutation p (1-based at this ABI,
+ * as on the reference's command line, ITNT/src/test_inplace.cpp:142-158)
+ * produces the tensor whose output axis j is input axis p[j]-1; output
+ * dims are (d{p0-1}, d{p1-1}, ...).
+ *
+ * Every entry point returns an int status (EITHOT_OK on success) and never
+ * exits the process; eithot_last_error() returns a message for the calling
+ * thread's most recent failure.  Device work is issued on the caller's
+ * stream (a cudaStream_t passed as void*; NULL = legacy default stream) and
+ * is stream-ordered: no entry point synchronises the device except where
+ * stated.
+ */
+#ifndef EITHOT_H_
+#define EITHOT_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define EITHOT_OK            0
+#define EITHOT_EINVAL        1  /* bad dims / perm / element size / capacity */
+#define EITHOT_ENOMEM        2  /* workspace could not be allocated or is too small */
+#define EITHOT_ETIMEOUT      3  /* a bounded device wait gave up */
+#define EITHOT_ECUDA         4  /* a CUDA runtime call failed */
+#define EITHOT_EUNSUPPORTED  5  /* valid request outside what this build handles */
+#define EITHOT_EBUSY         6  /* admission refused (served form) */
+
+/* ---- REORDER_TYPE (ITNT/src/Nd_transpose.cpp:22-28) ------------------- */
+#define EITHOT_ORDER_MIXED   0  /* reference default: fewer non-linearized rounds wins, tie -> post */
+#define EITHOT_ORDER_PRE     1
+#define EITHOT_ORDER_POST    2
+
+/* ---- step roles in a plan --------------------------------------------- */
+#define EITHOT_STEP_ROUND     0  /* one low-order transpose of the series */
+#define EITHOT_STEP_PARTITION 1  /* NdPartition: 132 linearisation (ITNT/src/Nd_decompose.cpp:49-56) */
+#define EITHOT_STEP_JOIN      2  /* NdJoin (ITNT/src/Nd_decompose.cpp:66-82) */
+#define EITHOT_STEP_PAD_PRE   3  /* Nd_padding_pre_process (ITNT/src/Nd_padding.cu:103-161) */
+#define EITHOT_STEP_PAD_POST  4  /* Nd_padding_post_process (ITNT/src/Nd_padding.cu:169-223) */
+
+/* One low-order step of a plan.  For ROUND/PARTITION/JOIN, `code` is the
+ * decimal-encoded 1-based low-order permutation (21, 132, 213, 231, 312,
+ * 1324) exactly as the reference's Low_order_transpose switch reads it
+ * (ITNT/src/Nd_transpose.cpp:62-99) and dims/perm describe that low-order
+ * tensor.  A ROUND step applies to every sub-tensor (`num_sub_tensors` of
+ * them, contiguous, `sub_tensor_elems` elements each).  For PAD steps,
+ * dims[0] = decomposed-dim position, dims[1] = original size, dims[2] =
+ * padded size. */
+typedef struct eithot_step {
+    int     role;
+    int     code;
+    int     rank;
+    int     perm[4];
+    int64_t dims[4];
+} eithot_step;
+
+typedef struct eithot_plan_info {
+    int     order_used;        /* EITHOT_ORDER_PRE or EITHOT_ORDER_POST */
+    int     num_sub_tensors;   /* applied (forced to 1 below the 32/alpha gate) */
+    int     decompose_dim;     /* -1 when the tensor is not partitioned */
+    int     padded;            /* 1 when the decomposed dim is padded */
+    int64_t padded_dim_size;
+    int64_t volume;            /* elements of the tensor */
+    int64_t padded_volume;     /* elements while padded (== volume if not) */
+    int64_t sub_tensor_elems;
+    int     n_steps;           /* total steps (may exceed max_steps passed in) */
+} eithot_plan_info;
+
+/* Execution statistics of the last eithot_transpose* call on this thread. */
+typedef struct eithot_stats {
+    size_t  workspace_bytes;   /* device scratch the call used */
+    size_t  free_before;       /* cudaMemGetInfo free bytes at entry */
+    size_t  free_after_alloc;  /* cudaMemGetInfo free bytes once scratch was allocated */
+    int     n_passes;          /* device passes launched (excl. no-ops) */
+    int     n_launches;        /* kernel launches issued */
+    double  algorithmic_bytes; /* 2 * volume * elem_size */
+} eithot_stats;
+
+/* ---- planning (host only, no GPU needed) ------------------------------ */
+
+/* Replaces the planning half of _Nd::transpose / Series_Low_order_transpose
+ * (ITNT/src/Nd_transpose.cpp:160-304, permutation_util.cpp:300-374): the
+ * same pre/post/mixed decomposition, sub-tensor gate (max dim > 32/alpha and
+ * nb > 1) and padding decision, in 64-bit arithmetic.  Writes up to
+ * max_steps steps; info->n_steps reports the full count. */
+int eithot_plan(int rank, const int64_t* dims, const int* perm_1based,
+                int num_sub_tensors, double alpha, int reorder_type,
+                eithot_plan_info* info, eithot_step* steps, int max_steps);
+
+/* ---- the transpose ---------------------------------------------------- */
+
+/* Replaces inplace::transpose (ITNT/include/transpose.h:8,
+ * ITNT/src/transpose.cpp:21-30).  In-place permutation of the tensor at
+ * d_data.  elem_size in {1,2,4,8} (the reference accepts 4 and 8 only).
+ * capacity_bytes is the size of the caller's buffer: when the plan pads the
+ * decomposed dim (nb > 1, dim % nb != 0) the padded tensor must fit, exactly
+ * as the reference requires caller slack (ITNT/src/test_inplace.cpp:11,22).
+ * Scratch is taken from the stream-ordered allocator (cudaMallocAsync) and
+ * bounded by alpha * bytes where the tensor is large enough for that bound
+ * to hold; the call returns before the device work completes. */
+int eithot_transpose(void* d_data, size_t capacity_bytes, int rank,
+                     const int64_t* dims, const int* perm_1based,
+                     size_t elem_size, int num_sub_tensors, double alpha,
+                     void* stream);
+
+/* As eithot_transpose with an explicit REORDER_TYPE and an optional
+ * caller-owned workspace (d_workspace may be NULL: the library allocates).
+ * When a workspace is given it must hold eithot_workspace_size() bytes. */
+int eithot_transpose_ex(void* d_data, size_t capacity_bytes, int rank,
+                        const int64_t* dims, const int* perm_1based,
+                        size_t elem_size, int num_sub_tensors, double alpha,
+                        int reorder_type, void* d_workspace,
+                        size_t workspace_bytes, void* stream);
+
+/* Device scratch bytes eithot_transpose_ex needs for this request. */
+int eithot_workspace_size(int rank, const int64_t* dims, const int* perm_1based,
+                          size_t elem_size, int num_sub_tensors, double alpha,
+                          int reorder_type, size_t* bytes_out);
+
+/* ---- the extra-memory estimator --------------------------------------- */
+
+/* Replaces Nd_estimation (Nd_memory_estimation/src/test_inplace.cpp:19-147):
+ * the reference's own procedure (max temp over rounds, nb = 2^ceil(log2(
+ * tmp/size/alpha)), alpha raised to 1/sqrt(vol/32), padding/partition/join
+ * costs, nb halving) evaluated with the reference kernels' cost model for a
+ * device with `smem_per_block` bytes of default shared memory per block and
+ * `padding_blocks` resident 1024-thread blocks (pass 0 for either to query
+ * the current device).  Outputs the nb and alpha the reference would write
+ * to proper_input.txt and its modelled extra bytes.  elem_size is treated as
+ * the reference does (4 -> 4-byte, otherwise 8-byte). */
+int eithot_estimate(int rank, const int64_t* dims, const int* perm_1based,
+                    size_t elem_size, int num_sub_tensors, double alpha,
+                    size_t smem_per_block, int padding_blocks,
+                    int* nb_out, double* alpha_out, size_t* extra_bytes_out);
+
+/* ---- per-pass profiling -------------------------------------------------
+ * No reference counterpart (the reference times only whole calls,
+ * ITNT/src/test_inplace.cpp:43-69).  When enabled for the calling thread,
+ * every eithot_transpose* call records a CUDA event on the caller's stream
+ * before its first pass and after each pass, appending to a list that
+ * eithot_profile_reset clears; once the stream is synchronised,
+ * eithot_profile_get returns listed pass i's name, its event-timed duration
+ * in ms and the bytes it reads plus writes. */
+int eithot_set_profiling(int enable);
+int eithot_profile_reset(void);
+int eithot_profile_count(void);
+int eithot_profile_get(int i, char* name, size_t name_len, double* ms, double* bytes_moved);
+
+/* ---- misc ------------------------------------------------------------- */
+const char* eithot_last_error(void);
+int eithot_last_stats(eithot_stats* out);
+int eithot_version(void);
+
+#ifdef __cplusplus
+}  /* extern "C" */
+
+/* Source-compatible drop-in for the reference's C++ entry point
+ * (ITNT/include/transpose.h:6-8): 0-based int permutation, int dims, device
+ * pointer `data` advanced by `source` elements, legacy default stream,
+ * synchronous like the reference.  sizeofType 4 or 8 as in the reference
+ * (other sizes are accepted too).  Errors are printed to stderr and leave
+ * the data untouched where possible; the reference exits instead. */
+namespace inplace {
+void transpose(void* data, int source, int rank, void* dim, void* permutation,
+               size_t sizeofType, int num_block, double LARGE_RATIO);
+}
+#endif
+
+#endif  /* EITHOT_H_ */

@@ -1,0 +1,123 @@
+// Test infrastructure: applies the library's lowered pass list on host
+// memory with the same index maps the kernels use (eithot_gb300/csrc/
+// fn_build.h, index_math.cuh).  It checks the planner -> lowering ->
+// index-map chain on the CPU; the device kernels are checked separately by
+// the GPU tests.  Never loaded by the product.
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fn_build.h"
+#include "passes.h"
+#include "plan.h"
+
+using namespace eithot;
+
+namespace {
+
+thread_local std::string g_err;
+
+template <typename Fn>
+void col_gather(uint8_t* base, const Pass& p, const Fn& fn) {
+    const uint64_t E = p.elem, R = p.rows, C = p.cols;
+    std::vector<uint8_t> tmp(R * E);
+    for (uint64_t b = 0; b < p.batches; ++b) {
+        uint8_t* m = base + b * R * C * E;
+        for (uint64_t j = 0; j < C; ++j) {
+            for (uint64_t i = 0; i < R; ++i) std::memcpy(&tmp[i * E], m + (i * C + j) * E, E);
+            for (uint64_t i = 0; i < R; ++i) std::memcpy(m + (i * C + j) * E, &tmp[fn(i, j) * E], E);
+        }
+    }
+}
+
+void apply(uint8_t* data, const Pass& p) {
+    uint8_t* base = data + p.offset;
+    const uint64_t E = p.elem;
+    switch (p.type) {
+        case kSlabTranspose: {
+            const uint64_t R = p.rows, C = p.cols;
+            std::vector<uint8_t> tmp(R * C * E);
+            for (uint64_t b = 0; b < p.batches; ++b) {
+                uint8_t* m = base + b * R * C * E;
+                std::memcpy(tmp.data(), m, R * C * E);
+                for (uint64_t o = 0; o < R * C; ++o) {
+                    const uint64_t c = o / R, r = o % R;
+                    std::memcpy(m + o * E, &tmp[(r * C + c) * E], E);
+                }
+            }
+            break;
+        }
+        case kRowGather:
+        case kRowScatter: {
+            const FnRowShuffle fn = make_rowshuffle(p);
+            std::vector<uint8_t> tmp(p.cols * E);
+            for (uint64_t bi = 0; bi < p.batches * p.rows; ++bi) {
+                const uint64_t i = bi % p.rows;
+                uint8_t* row = base + bi * p.cols * E;
+                std::memcpy(tmp.data(), row, p.cols * E);
+                for (uint64_t j = 0; j < p.cols; ++j) {
+                    if (p.type == kRowGather) std::memcpy(row + j * E, &tmp[fn(i, j) * E], E);
+                    else std::memcpy(row + fn(i, j) * E, &tmp[j * E], E);
+                }
+            }
+            break;
+        }
+        case kColGather:
+            switch (p.fn) {
+                case kFnC2RPreRot: col_gather(base, p, make_prerot(p)); break;
+                case kFnC2RColShuffle: col_gather(base, p, make_c2r_colshuf(p)); break;
+                case kFnR2CColShuffle: col_gather(base, p, make_r2c_colshuf(p)); break;
+                case kFnR2CPostRot: col_gather(base, p, make_postrot(p)); break;
+            }
+            break;
+        case kBlockMove:
+            if (p.dst_pitch > p.src_pitch) {
+                for (uint64_t s = p.n_blocks; s-- > 1;)
+                    std::memmove(data + s * p.dst_pitch, data + s * p.src_pitch, p.block);
+            } else {
+                for (uint64_t s = 1; s < p.n_blocks; ++s)
+                    std::memmove(data + s * p.dst_pitch, data + s * p.src_pitch, p.block);
+            }
+            break;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* hs_last_error() { return g_err.c_str(); }
+
+// Returns the number of passes applied, or -1 on error.
+int hs_transpose(void* data, size_t capacity, int rank, const int64_t* dims, const int* perm,
+                 size_t elem, int nb, double alpha, int order) {
+    NdPlan plan;
+    if (!make_nd_plan(rank, dims, perm, nb, alpha, order, &plan, &g_err)) return -1;
+    if (static_cast<double>(plan.padded_volume) * elem > static_cast<double>(capacity)) {
+        g_err = "capacity";
+        return -1;
+    }
+    std::vector<Pass> passes;
+    DeviceCaps caps;
+    if (!lower_plan(plan, elem, caps, &passes, &g_err)) return -1;
+    for (const Pass& p : passes) apply(static_cast<uint8_t*>(data), p);
+    return static_cast<int>(passes.size());
+}
+
+// Writes a one-line description per pass into buf (newline separated).
+int hs_describe(char* buf, size_t len, int rank, const int64_t* dims, const int* perm, size_t elem,
+                int nb, double alpha, int order) {
+    NdPlan plan;
+    if (!make_nd_plan(rank, dims, perm, nb, alpha, order, &plan, &g_err)) return -1;
+    std::vector<Pass> passes;
+    DeviceCaps caps;
+    if (!lower_plan(plan, elem, caps, &passes, &g_err)) return -1;
+    std::string s;
+    for (const Pass& p : passes) s += p.what + "\n";
+    std::strncpy(buf, s.c_str(), len);
+    if (len) buf[len - 1] = 0;
+    return static_cast<int>(passes.size());
+}
+
+}  // extern "C"

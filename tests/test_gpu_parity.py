@@ -1,0 +1,163 @@
+"""Parity of the sm_103a path with the oracle, through the C ABI
+(eithot_transpose_ex via eithot_gb300.transpose_ptr) on device memory.
+Bit-exact: every byte of the output equals the oracle's out-of-place
+permutation of the same seeded input."""
+import ctypes
+import itertools
+import math
+import random
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def dev():
+    return torch.device("cuda:0")
+
+
+def run_case(E, dims, perm, elem, nb=1, alpha=0.01, order=0, slack=1.0, seed=1, offset=0, stream=None):
+    n = math.prod(dims)
+    host = oracle.fill_hash(n, elem, seed)
+    cap = int(n * elem * slack) + 256
+    buf = torch.zeros(cap + offset, dtype=torch.uint8, device=dev())
+    buf[offset:offset + n * elem] = torch.from_numpy(host).to(dev())
+    s = stream or torch.cuda.current_stream()
+    E.transpose_ptr(buf.data_ptr() + offset, cap, dims, perm, elem, nb, alpha, order, s.cuda_stream)
+    s.synchronize()
+    got = buf[offset:offset + n * elem].cpu().numpy()
+    want = oracle.permute(host, dims, perm, elem)
+    if not np.array_equal(got, want):
+        bad = np.nonzero(got != want)[0]
+        raise AssertionError("mismatch %s perm %s elem %d: %d bad bytes, first at %d"
+                             % (dims, perm, elem, bad.size, bad[0]))
+    return E.last_stats()
+
+
+def test_config1_iota_2d(E):
+    """3001 x 4096 int32 iota, perm (2 1), nb 1, alpha 0.01: byte-exact vs the
+    oracle and the reference's verify_inplace known answer."""
+    dims, perm = [3001, 4096], [2, 1]
+    n = 3001 * 4096
+    a = np.arange(n, dtype=np.int32)
+    t = torch.from_numpy(a.copy()).to(dev())
+    E.transpose(t, dims, perm, 1, 0.01)
+    torch.cuda.synchronize()
+    got = t.cpu().numpy()
+    want = oracle.permute(a.view(np.uint8), dims, perm, 4).view(np.int32)
+    assert np.array_equal(got, want)
+    rng = np.random.default_rng(0)
+    for i in rng.integers(0, n, size=4000):
+        assert got[oracle.dest_index(dims, perm, int(i))] == i
+
+
+@pytest.mark.parametrize("rank", [2, 3, 4])
+@pytest.mark.parametrize("elem", [1, 2, 4, 8])
+def test_all_permutations_small(E, rank, elem):
+    rng = random.Random(rank * 10 + elem)
+    for perm in itertools.permutations(range(1, rank + 1)):
+        dims = [rng.choice([1, 2, 3, 5, 7, 8, 16, 33, 64]) for _ in range(rank)]
+        run_case(E, dims, list(perm), elem, seed=rng.randrange(1 << 30))
+
+
+@pytest.mark.parametrize("rank", [5, 6])
+def test_random_high_rank(E, rank):
+    rng = random.Random(rank)
+    for _ in range(40):
+        perm = list(range(1, rank + 1))
+        rng.shuffle(perm)
+        dims = [rng.choice([2, 3, 4, 5, 7, 9, 12]) for _ in range(rank)]
+        run_case(E, dims, perm, rng.choice([1, 2, 4, 8]), order=rng.choice([0, 1, 2]))
+
+
+@pytest.mark.parametrize("R,C,elem", [(3001, 4096, 4), (4096, 3001, 4), (2048, 1536, 4), (1000, 999, 2),
+                                      (64, 80000, 4), (80000, 64, 4), (5000, 60, 16), (40, 2000, 24),
+                                      (700, 1400, 1), (9973, 1024, 8)])
+def test_catanzaro_2d(E, R, C, elem):
+    run_case(E, [C, R], [2, 1], elem)
+
+
+@pytest.mark.parametrize("dims,perm", [([60000, 300], [2, 1]), ([300, 60000], [2, 1]),
+                                       ([4, 20011, 819, 2], [1, 3, 2, 4]), ([17, 30011, 37], [1, 3, 2]),
+                                       ([3, 50000, 41], [3, 2, 1])])
+def test_rows_and_columns_beyond_shared_memory(E, dims, perm):
+    run_case(E, dims, perm, 4)
+
+
+@pytest.mark.parametrize("dims,perm,nb,alpha", [
+    ([7248, 50], [2, 1], 4, 0.02), ([3301, 7, 5], [3, 1, 2], 3, 0.01), ([5, 3302, 6], [2, 3, 1], 4, 0.01),
+    ([6, 4, 3401], [3, 2, 1], 2, 0.01), ([40, 3203, 3], [1, 3, 2], 8, 0.01), ([3, 3301, 2, 5], [4, 2, 1, 3], 16, 0.01)])
+@pytest.mark.parametrize("elem", [2, 4, 8])
+def test_subtensors_and_padding(E, dims, perm, nb, alpha, elem):
+    run_case(E, dims, perm, elem, nb, alpha, slack=1.1)
+
+
+def test_wide_elements(E):
+    run_case(E, [700, 3, 600], [1, 3, 2], 2)
+    run_case(E, [64, 6, 5, 70], [1, 3, 2, 4], 4)
+    run_case(E, [1500, 2, 300], [1, 3, 2], 4)
+    run_case(E, [16384, 25, 4, 3], [1, 3, 2, 4], 2)
+
+
+def test_unaligned_base_and_odd_elements(E):
+    run_case(E, [33, 17, 9], [2, 3, 1], 4, offset=4)
+    run_case(E, [33, 17, 9], [3, 1, 2], 2, offset=2)
+    run_case(E, [31, 1000, 3], [1, 3, 2], 1, offset=1)
+    run_case(E, [5, 701, 3], [3, 2, 1], 3)
+    run_case(E, [2, 3001, 40], [1, 3, 2], 6)
+
+
+def test_side_stream(E):
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        run_case(E, [3001, 128, 3], [3, 1, 2], 4, stream=s)
+
+
+def test_reorder_types_agree(E):
+    for order in (0, 1, 2):
+        run_case(E, [12, 5, 40, 7, 3], [5, 3, 1, 4, 2], 2, order=order)
+
+
+def test_capacity_is_enforced(E):
+    dims, perm = [3301, 7, 5], [3, 1, 2]
+    n = math.prod(dims)
+    buf = torch.zeros(n * 4, dtype=torch.uint8, device=dev())
+    with pytest.raises(E.EithotError) as ei:
+        E.transpose_ptr(buf.data_ptr(), n * 4, dims, perm, 4, 3, 0.01)
+    assert ei.value.code == E.EINVAL
+
+
+def test_reference_signature_shim(E):
+    """inplace::transpose(void*, int source, int rank, void* dim, void* perm
+    (0-based), size_t, int nb, double alpha) — the reference's C++ entry."""
+    fn = getattr(E.lib, "_ZN7inplace9transposeEPviiS0_S0_mid")
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                   ctypes.c_size_t, ctypes.c_int, ctypes.c_double]
+    dims, perm = [300, 41, 7], [2, 3, 1]
+    n = math.prod(dims)
+    host = oracle.fill_hash(n, 4, 3)
+    src = 5  # the reference's `source` element offset
+    t = torch.zeros(n + src, dtype=torch.int32, device=dev())
+    t[src:] = torch.from_numpy(host.view(np.int32)).to(dev())
+    d = (ctypes.c_int * 3)(*dims)
+    p = (ctypes.c_int * 3)(*[x - 1 for x in perm])
+    fn(ctypes.c_void_p(t.data_ptr()), src, 3, d, p, 4, 1, 0.01)
+    got = t[src:].cpu().numpy().view(np.uint8)
+    assert np.array_equal(got, oracle.permute(host, dims, perm, 4))
+
+
+@pytest.mark.slow
+def test_config2_full_size(E):
+    """(4, 20011, 8192, 2) int32, perm (1 3 2 4), nb/alpha from the
+    estimator, extra device memory within alpha * bytes."""
+    dims, perm = [4, 20011, 8192, 2], [1, 3, 2, 4]
+    nb, alpha, _ = E.estimate(dims, perm, 4)
+    st = run_case(E, dims, perm, 4, nb, alpha, seed=0xE17407)
+    n = math.prod(dims)
+    assert st["workspace_bytes"] <= alpha * n * 4 * 1.0001
+    assert st["free_before"] - st["free_after_alloc"] <= alpha * n * 4 * 1.05 + (64 << 20)

@@ -1,0 +1,57 @@
+"""The lowered pass list applied on the CPU with the kernels' index maps
+(tests/native/hostsim.cpp) reproduces the oracle permutation: checks the
+planner -> lowering -> index-map chain without a GPU."""
+import ctypes
+import itertools
+import math
+import random
+
+import numpy as np
+import pytest
+
+import oracle
+
+
+def run(hostsim, dims, perm, elem, nb=1, alpha=0.01, order=0, slack=1.0, seed=0):
+    r = len(dims)
+    n = math.prod(dims)
+    a = oracle.fill_hash(n, elem, seed)
+    cap = int(n * elem * slack) + 64
+    buf = np.zeros(cap, dtype=np.uint8)
+    buf[:n * elem] = a
+    D = (ctypes.c_int64 * r)(*dims)
+    P = (ctypes.c_int * r)(*perm)
+    k = hostsim.hs_transpose(buf.ctypes.data, cap, r, D, P, elem, nb, alpha, order)
+    assert k >= 0, hostsim.hs_last_error()
+    return np.array_equal(buf[:n * elem], oracle.permute(a, dims, perm, elem))
+
+
+@pytest.mark.parametrize("rank", [2, 3, 4, 5])
+def test_all_permutations(hostsim, rank):
+    rng = random.Random(rank)
+    for perm in itertools.permutations(range(1, rank + 1)):
+        dims = [rng.choice([1, 2, 3, 5, 7, 8, 12, 13, 24]) for _ in range(rank)]
+        for elem in (1, 2, 4, 8, 12):
+            for order in (0, 1, 2):
+                assert run(hostsim, dims, list(perm), elem, order=order), (dims, perm, elem, order)
+
+
+@pytest.mark.parametrize("R,C,E", [(3001, 4096, 4), (300, 700, 4), (1000, 999, 2), (64, 8000, 8),
+                                   (5000, 60, 16), (40, 2000, 24), (2048, 1536, 4), (700, 1400, 1)])
+def test_catanzaro_2d(hostsim, R, C, E):
+    assert run(hostsim, [C, R], [2, 1], E)
+
+
+@pytest.mark.parametrize("dims,perm,nb,alpha", [
+    ([7248, 50], [2, 1], 4, 0.02), ([3301, 7, 5], [3, 1, 2], 3, 0.01), ([5, 3302, 6], [2, 3, 1], 4, 0.01),
+    ([6, 4, 3401], [3, 2, 1], 2, 0.01), ([40, 3203, 3], [1, 3, 2], 8, 0.01), ([3, 3301, 2, 5], [4, 2, 1, 3], 16, 0.01)])
+@pytest.mark.parametrize("elem", [2, 4, 8])
+def test_subtensors_and_padding(hostsim, dims, perm, nb, alpha, elem):
+    assert run(hostsim, dims, perm, elem, nb, alpha, slack=1.1)
+
+
+def test_large_elements(hostsim):
+    # 132 / 1324 with wide carried dims (strip staging), partition-like shapes
+    assert run(hostsim, [700, 3, 600], [1, 3, 2], 2)
+    assert run(hostsim, [64, 6, 5, 70], [1, 3, 2, 4], 4)
+    assert run(hostsim, [1500, 2, 300], [1, 3, 2], 4)
