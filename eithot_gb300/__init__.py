@@ -208,3 +208,11 @@ def profile() -> List[dict]:
         _check(lib.eithot_profile_get(i, name, 256, ctypes.byref(ms), ctypes.byref(by)))
         out.append({"name": name.value.decode(), "ms": ms.value, "bytes": by.value})
     return out
+
+
+def index_faults() -> int:
+    """Index-map results outside their row/column since the last call
+    (kernels skip them); synchronises the device."""
+    v = ctypes.c_uint()
+    _check(lib.eithot_index_faults(ctypes.byref(v)))
+    return v.value

@@ -111,6 +111,12 @@ int eithot_profile_get(int i, char* name, size_t name_len, double* ms, double* b
     return EITHOT_OK;
 }
 
+int eithot_index_faults(unsigned int* count) {
+    if (!count) return fail(EITHOT_EINVAL, "null count");
+    if (eithot::read_index_faults(count)) return fail(EITHOT_ECUDA, "reading the index-fault counter failed");
+    return EITHOT_OK;
+}
+
 int eithot_last_stats(eithot_stats* out) {
     if (!out) return fail(EITHOT_EINVAL, "null stats");
     *out = g_stats;

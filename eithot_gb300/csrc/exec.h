@@ -51,4 +51,8 @@ int run_passes(uint8_t* data, const std::vector<Pass>& passes, ExecContext& ctx)
 
 bool query_caps(int device, DeviceCaps* caps, std::string* err);
 
+// Count of index-map results that fell outside their row/column since the
+// last read (the kernels skip such accesses).  Synchronises the device.
+int read_index_faults(unsigned int* out);
+
 }  // namespace eithot

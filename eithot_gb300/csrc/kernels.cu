@@ -30,6 +30,17 @@ namespace {
 
 constexpr int kThreads = 512;
 
+// Set when an index map returns a position outside its row or column; the
+// access is skipped instead of faulting.  Read (and cleared) by
+// eithot_index_faults().
+__device__ unsigned int g_index_faults = 0;
+
+__device__ __forceinline__ bool in_range(uint64_t v, uint64_t n) {
+    if (v < n) return true;
+    atomicAdd(&g_index_faults, 1u);
+    return false;
+}
+
 template <int S> struct UnitOf;
 template <> struct UnitOf<1> { using T = uint8_t; };
 template <> struct UnitOf<2> { using T = uint16_t; };
@@ -119,6 +130,7 @@ __global__ void __launch_bounds__(kThreads) k_row_smem(RowArgs a, Fn fn) {
             if (u >= lim) continue;
             const U v = *reinterpret_cast<const U*>(row + j * a.g.E + u * US);
             const uint64_t slot = kScatter ? fn(i, j) : j;
+            if (!in_range(slot, a.cols)) continue;
             *reinterpret_cast<U*>(smem + slot * a.g.w + u * US) = v;
         }
         __syncthreads();
@@ -127,6 +139,7 @@ __global__ void __launch_bounds__(kThreads) k_row_smem(RowArgs a, Fn fn) {
             a.g.div_upw.divmod(x, j, u);
             if (u >= lim) continue;
             const uint64_t slot = kScatter ? j : fn(i, j);
+            if (!in_range(slot, a.cols)) continue;
             const U v = *reinterpret_cast<const U*>(smem + slot * a.g.w + u * US);
             *reinterpret_cast<U*>(row + j * a.g.E + u * US) = v;
         }
@@ -176,6 +189,7 @@ __global__ void __launch_bounds__(kThreads) k_col_smem(ColArgs a, Fn fn) {
             a.g.div_upw.divmod(r, c, u);
             if (c >= tcols || u >= lim) continue;
             const uint64_t src = fn(i, col0 + c);
+            if (!in_range(src, a.rows)) continue;
             const U v = *reinterpret_cast<const U*>(smem + src * a.pitch + c * a.g.w + u * US);
             *reinterpret_cast<U*>(mat + i * row_bytes + c * a.g.E + u * US) = v;
         }
@@ -218,10 +232,12 @@ __global__ void __launch_bounds__(kThreads) k_row_stage(StageRowArgs a, Fn fn) {
         uint8_t* st = a.scratch + gi * item_bytes;
         if (kIn) {
             const uint64_t slot = kScatter ? fn(i, j) : j;
+            if (!in_range(slot, a.cols)) continue;
             *reinterpret_cast<U*>(st + slot * a.g.w + u * US) =
                 *reinterpret_cast<const U*>(row + j * a.g.E + u * US);
         } else {
             const uint64_t slot = kScatter ? j : fn(i, j);
+            if (!in_range(slot, a.cols)) continue;
             *reinterpret_cast<U*>(row + j * a.g.E + u * US) =
                 *reinterpret_cast<const U*>(st + slot * a.g.w + u * US);
         }
@@ -265,6 +281,7 @@ __global__ void __launch_bounds__(kThreads) k_col_stage(StageColArgs a, Fn fn) {
                 *reinterpret_cast<const U*>(mat + i * row_bytes + c * a.g.E + u * US);
         } else {
             const uint64_t src = fn(i, col0 + c);
+            if (!in_range(src, a.rows)) continue;
             *reinterpret_cast<U*>(mat + i * row_bytes + c * a.g.E + u * US) =
                 *reinterpret_cast<const U*>(st + src * spitch + c * a.g.w + u * US);
         }
@@ -682,6 +699,14 @@ int run_passes(uint8_t* data, const std::vector<Pass>& passes, ExecContext& ctx)
     }
     if (ctx.profile) ctx.events_used = ev;
     return 0;
+}
+
+int read_index_faults(unsigned int* out) {
+    unsigned int v = 0, zero = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(&v, g_index_faults, sizeof(v));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_index_faults, &zero, sizeof(zero));
+    *out = v;
+    return e == cudaSuccess ? 0 : EITHOT_STATUS_CUDA;
 }
 
 bool query_caps(int device, DeviceCaps* caps, std::string* err) {

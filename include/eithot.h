@@ -155,6 +155,13 @@ int eithot_profile_reset(void);
 int eithot_profile_count(void);
 int eithot_profile_get(int i, char* name, size_t name_len, double* ms, double* bytes_moved);
 
+/* ---- self-check --------------------------------------------------------
+ * No reference counterpart.  Every kernel checks that each index-map result
+ * lies inside its row or column; a result outside is skipped (never
+ * dereferenced) and counted.  Returns and clears the count; synchronises
+ * the device. */
+int eithot_index_faults(unsigned int* count);
+
 /* ---- misc ------------------------------------------------------------- */
 const char* eithot_last_error(void);
 int eithot_last_stats(eithot_stats* out);

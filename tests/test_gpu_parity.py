@@ -30,6 +30,7 @@ def run_case(E, dims, perm, elem, nb=1, alpha=0.01, order=0, slack=1.0, seed=1, 
     s = stream or torch.cuda.current_stream()
     E.transpose_ptr(buf.data_ptr() + offset, cap, dims, perm, elem, nb, alpha, order, s.cuda_stream)
     s.synchronize()
+    assert E.index_faults() == 0
     got = buf[offset:offset + n * elem].cpu().numpy()
     want = oracle.permute(host, dims, perm, elem)
     if not np.array_equal(got, want):
