@@ -51,6 +51,9 @@ def parse():
     ap.add_argument("--impl", default="eithot", choices=["eithot", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--dims", default=None,
+                    help="comma-separated dims overriding the workload (small cases for ncu captures)")
     return ap.parse_args()
 
 
@@ -192,9 +195,34 @@ def run_reference(args):
     return 0
 
 
+def end_to_end(args, E, buf, nbytes, stream, step, dev, world):
+    """Host buffers: per step, pinned H2D copy, the C-ABI transpose, D2H."""
+    import torch
+    host = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    host.copy_(buf[: nbytes])
+    steps = max(1, args.e2e_steps)
+    torch.cuda.synchronize(dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        buf[: nbytes].copy_(host, non_blocking=True)
+        step()
+        host.copy_(buf[: nbytes], non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / steps
+    return {"value": world * 2.0 * nbytes / (ms / 1e3) / 1e9, "unit": "GB/s", "h2d_bytes_per_step": nbytes,
+            "d2h_bytes_per_step": nbytes, "ms_per_step": ms}
+
+
 def run_eithot(args):
     import torch
     import eithot_gb300 as E
+
+    global DIMS
+    if args.dims:
+        DIMS = [int(x) for x in args.dims.split(",")]
 
     rank, world, local = dist_env()
     if world > 1:
@@ -274,21 +302,9 @@ def run_eithot(args):
     value = world * 2.0 * nbytes / (ms_per_step / 1e3) / 1e9
 
     # end-to-end through the C ABI from pinned host memory
-    host = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
-    host.copy_(buf[: nbytes])
-    e2e_steps = max(1, args.e2e_steps)
-    torch.cuda.synchronize(dev)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(e2e_steps):
-        buf[: nbytes].copy_(host, non_blocking=True)
-        step()
-        host.copy_(buf[: nbytes], non_blocking=True)
-    e1.record(stream)
-    torch.cuda.synchronize(dev)
-    e2e_ms = e0.elapsed_time(e1) / e2e_steps
-    e2e_value = world * 2.0 * nbytes / (e2e_ms / 1e3) / 1e9
+    e2e = None
+    if not args.no_e2e:
+        e2e = end_to_end(args, E, buf, nbytes, stream, step, dev, world)
 
     peak, peak_kind = load_peaks()
     dominant = max(per_pass.items(), key=lambda kv: kv[1]["ms"]) if per_pass else None
@@ -314,8 +330,7 @@ def run_eithot(args):
                        "alpha": alpha, "bytes": nbytes,
                        "l2": "no flush: the 5.25 GB tensor is larger than the 129 MB L2",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
-            "e2e": {"value": e2e_value, "unit": "GB/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
-                    "ms_per_step": e2e_ms},
+            "e2e": e2e,
             "gpu_launches": launches,
             "roofline": roofline,
             "clocks": clocks,

@@ -10,6 +10,7 @@
 // staged in global scratch by a grid-wide copy-in launch followed by a
 // copy-out launch, one group of items at a time (stream order replaces any
 // device-wide barrier).
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -39,6 +40,28 @@ __device__ __forceinline__ bool in_range(uint64_t v, uint64_t n) {
     if (v < n) return true;
     atomicAdd(&g_index_faults, 1u);
     return false;
+}
+
+namespace cg = cooperative_groups;
+
+// Global -> shared copy of one unit.  4/8/16-byte units use cp.async so a
+// thread keeps many loads in flight; 1/2-byte units go through registers.
+template <int US, typename U>
+__device__ __forceinline__ void copy_in(uint8_t* sdst, const uint8_t* gsrc) {
+    if constexpr (US >= 4) {
+        const uint32_t sa = static_cast<uint32_t>(__cvta_generic_to_shared(sdst));
+        if constexpr (US == 16)
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gsrc) : "memory");
+        else
+            asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(sa), "l"(gsrc), "n"(US) : "memory");
+    } else {
+        *reinterpret_cast<U*>(sdst) = *reinterpret_cast<const U*>(gsrc);
+    }
+}
+
+template <int US>
+__device__ __forceinline__ void copy_in_wait() {
+    if constexpr (US >= 4) asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
 }
 
 template <int S> struct UnitOf;
@@ -85,9 +108,9 @@ __global__ void __launch_bounds__(kThreads) k_slab(SlabArgs a) {
             if (u >= lim) continue;
             uint64_t r, c;
             a.div_C.divmod(p, r, c);
-            const U v = *reinterpret_cast<const U*>(mat + p * a.g.E + u * US);
-            *reinterpret_cast<U*>(smem + r * a.pitch + c * a.g.w + u * US) = v;
+            copy_in<US, U>(smem + r * a.pitch + c * a.g.w + u * US, mat + p * a.g.E + u * US);
         }
+        copy_in_wait<US>();
         __syncthreads();
         for (uint64_t x = threadIdx.x; x < units; x += blockDim.x) {
             uint64_t o, u;
@@ -103,70 +126,104 @@ __global__ void __launch_bounds__(kThreads) k_slab(SlabArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// Row pass staged on chip: item = one strip of one row (cols pieces).
+// Row pass staged in the distributed shared memory of a K-CTA cluster: item
+// = one strip of one row; CTA k of the cluster owns pieces [k*P, (k+1)*P).
+// Gather: each CTA loads its own pieces, the cluster synchronises, then each
+// CTA writes its pieces reading f(i,j) from whichever CTA holds it.
+// Scatter: each CTA loads its pieces and stores piece j into the CTA that
+// owns f(i,j); after the cluster barrier each CTA writes its own range.
 // ---------------------------------------------------------------------------
 struct RowArgs {
     uint8_t* base;
-    uint64_t rows, cols, items;
+    uint64_t rows, cols, items, P;
     StripGeom g;
-    FastDiv div_rows;
+    FastDiv div_rows, div_P;
 };
 
 template <int US, typename Fn, bool kScatter>
-__global__ void __launch_bounds__(kThreads) k_row_smem(RowArgs a, Fn fn) {
+__global__ void __launch_bounds__(kThreads) k_row_cluster(RowArgs a, Fn fn) {
     using U = typename UnitOf<US>::T;
     extern __shared__ __align__(16) uint8_t smem[];
-    const uint64_t units = a.cols * a.g.upw;
+    cg::cluster_group cl = cg::this_cluster();
+    const unsigned K = cl.num_blocks();
+    const unsigned kr = cl.block_rank();
+    const uint64_t cid = blockIdx.x / K, ncl = gridDim.x / K;
+    const uint64_t j0 = kr * a.P;
+    const uint64_t jn = min(a.cols, j0 + a.P);
+    const uint64_t my_units = (jn > j0 ? jn - j0 : 0) * a.g.upw;
     const uint64_t row_bytes = a.cols * a.g.E;
-    for (uint64_t it = blockIdx.x; it < a.items; it += gridDim.x) {
+    for (uint64_t it = cid; it < a.items; it += ncl) {
         uint64_t bi, s;
         a.g.div_strips.divmod(it, bi, s);
         const uint64_t i = a.div_rows.mod(bi);
         const uint64_t lim = (s + 1 == a.g.nstrips) ? a.g.last_upw : a.g.upw;
         uint8_t* row = a.base + bi * row_bytes + s * a.g.w;
-        for (uint64_t x = threadIdx.x; x < units; x += blockDim.x) {
-            uint64_t j, u;
-            a.g.div_upw.divmod(x, j, u);
+        for (uint64_t x = threadIdx.x; x < my_units; x += blockDim.x) {
+            uint64_t jj, u;
+            a.g.div_upw.divmod(x, jj, u);
             if (u >= lim) continue;
-            const U v = *reinterpret_cast<const U*>(row + j * a.g.E + u * US);
-            const uint64_t slot = kScatter ? fn(i, j) : j;
-            if (!in_range(slot, a.cols)) continue;
-            *reinterpret_cast<U*>(smem + slot * a.g.w + u * US) = v;
+            const uint64_t j = j0 + jj;
+            if constexpr (kScatter) {
+                const U v = *reinterpret_cast<const U*>(row + j * a.g.E + u * US);
+                const uint64_t dst = fn(i, j);
+                if (!in_range(dst, a.cols)) continue;
+                uint64_t owner, off;
+                a.div_P.divmod(dst, owner, off);
+                *cl.map_shared_rank(reinterpret_cast<U*>(smem + off * a.g.w + u * US), static_cast<unsigned>(owner)) = v;
+            } else {
+                copy_in<US, U>(smem + jj * a.g.w + u * US, row + j * a.g.E + u * US);
+            }
         }
-        __syncthreads();
-        for (uint64_t x = threadIdx.x; x < units; x += blockDim.x) {
-            uint64_t j, u;
-            a.g.div_upw.divmod(x, j, u);
+        if constexpr (!kScatter) copy_in_wait<US>();
+        cl.sync();
+        for (uint64_t x = threadIdx.x; x < my_units; x += blockDim.x) {
+            uint64_t jj, u;
+            a.g.div_upw.divmod(x, jj, u);
             if (u >= lim) continue;
-            const uint64_t slot = kScatter ? j : fn(i, j);
-            if (!in_range(slot, a.cols)) continue;
-            const U v = *reinterpret_cast<const U*>(smem + slot * a.g.w + u * US);
+            const uint64_t j = j0 + jj;
+            U v;
+            if constexpr (kScatter) {
+                v = *reinterpret_cast<const U*>(smem + jj * a.g.w + u * US);
+            } else {
+                const uint64_t src = fn(i, j);
+                if (!in_range(src, a.cols)) continue;
+                uint64_t owner, off;
+                a.div_P.divmod(src, owner, off);
+                v = *cl.map_shared_rank(reinterpret_cast<const U*>(smem + off * a.g.w + u * US),
+                                        static_cast<unsigned>(owner));
+            }
             *reinterpret_cast<U*>(row + j * a.g.E + u * US) = v;
         }
-        __syncthreads();
+        cl.sync();
     }
 }
 
 // ---------------------------------------------------------------------------
-// Column pass staged on chip: item = one strip of a tile of tw adjacent
-// columns over all rows.
+// Column pass staged in a K-CTA cluster: item = one strip of a tile of tw
+// adjacent columns over all rows; CTA k owns rows [k*Q, (k+1)*Q).
 // ---------------------------------------------------------------------------
 struct ColArgs {
     uint8_t* base;
-    uint64_t rows, cols, tw, ntiles, pitch, items;
+    uint64_t rows, cols, tw, ntiles, pitch, items, Q;
     StripGeom g;
-    FastDiv div_tiles, div_rowunits;  // rowunits = tw * upw
+    FastDiv div_tiles, div_rowunits, div_Q;  // rowunits = tw * upw
 };
 
 template <int US, typename Fn>
-__global__ void __launch_bounds__(kThreads) k_col_smem(ColArgs a, Fn fn) {
+__global__ void __launch_bounds__(kThreads) k_col_cluster(ColArgs a, Fn fn) {
     using U = typename UnitOf<US>::T;
     extern __shared__ __align__(16) uint8_t smem[];
+    cg::cluster_group cl = cg::this_cluster();
+    const unsigned K = cl.num_blocks();
+    const unsigned kr = cl.block_rank();
+    const uint64_t cid = blockIdx.x / K, ncl = gridDim.x / K;
+    const uint64_t r0 = kr * a.Q;
+    const uint64_t rn = min(a.rows, r0 + a.Q);
     const uint64_t rowunits = a.tw * a.g.upw;
-    const uint64_t units = a.rows * rowunits;
+    const uint64_t my_units = (rn > r0 ? rn - r0 : 0) * rowunits;
     const uint64_t row_bytes = a.cols * a.g.E;
     const uint64_t mat_bytes = a.rows * row_bytes;
-    for (uint64_t it = blockIdx.x; it < a.items; it += gridDim.x) {
+    for (uint64_t it = cid; it < a.items; it += ncl) {
         uint64_t bt, s, b, t;
         a.g.div_strips.divmod(it, bt, s);
         a.div_tiles.divmod(bt, b, t);
@@ -174,26 +231,31 @@ __global__ void __launch_bounds__(kThreads) k_col_smem(ColArgs a, Fn fn) {
         const uint64_t tcols = min(a.tw, a.cols - col0);
         const uint64_t lim = (s + 1 == a.g.nstrips) ? a.g.last_upw : a.g.upw;
         uint8_t* mat = a.base + b * mat_bytes + col0 * a.g.E + s * a.g.w;
-        for (uint64_t x = threadIdx.x; x < units; x += blockDim.x) {
-            uint64_t i, r, c, u;
-            a.div_rowunits.divmod(x, i, r);
+        for (uint64_t x = threadIdx.x; x < my_units; x += blockDim.x) {
+            uint64_t ii, r, c, u;
+            a.div_rowunits.divmod(x, ii, r);
             a.g.div_upw.divmod(r, c, u);
             if (c >= tcols || u >= lim) continue;
-            const U v = *reinterpret_cast<const U*>(mat + i * row_bytes + c * a.g.E + u * US);
-            *reinterpret_cast<U*>(smem + i * a.pitch + c * a.g.w + u * US) = v;
+            copy_in<US, U>(smem + ii * a.pitch + c * a.g.w + u * US,
+                           mat + (r0 + ii) * row_bytes + c * a.g.E + u * US);
         }
-        __syncthreads();
-        for (uint64_t x = threadIdx.x; x < units; x += blockDim.x) {
-            uint64_t i, r, c, u;
-            a.div_rowunits.divmod(x, i, r);
+        copy_in_wait<US>();
+        cl.sync();
+        for (uint64_t x = threadIdx.x; x < my_units; x += blockDim.x) {
+            uint64_t ii, r, c, u;
+            a.div_rowunits.divmod(x, ii, r);
             a.g.div_upw.divmod(r, c, u);
             if (c >= tcols || u >= lim) continue;
+            const uint64_t i = r0 + ii;
             const uint64_t src = fn(i, col0 + c);
             if (!in_range(src, a.rows)) continue;
-            const U v = *reinterpret_cast<const U*>(smem + src * a.pitch + c * a.g.w + u * US);
+            uint64_t owner, off;
+            a.div_Q.divmod(src, owner, off);
+            const U v = *cl.map_shared_rank(reinterpret_cast<const U*>(smem + off * a.pitch + c * a.g.w + u * US),
+                                            static_cast<unsigned>(owner));
             *reinterpret_cast<U*>(mat + i * row_bytes + c * a.g.E + u * US) = v;
         }
-        __syncthreads();
+        cl.sync();
     }
 }
 
@@ -363,6 +425,39 @@ cudaError_t prep_smem(const void* kernel, size_t smem) {
                                 static_cast<int>(smem));
 }
 
+// Launches `kernel` as clusters of K CTAs, as many clusters as can be
+// resident at once (at most `items`).
+template <typename... KArgs, typename... Args>
+cudaError_t launch_clusters(void (*kernel)(KArgs...), int K, size_t smem, uint64_t items,
+                            ExecContext& ctx, Args&&... args) {
+    const void* kp = reinterpret_cast<const void*>(kernel);
+    cudaError_t e = prep_smem(kp, smem);
+    if (e != cudaSuccess) return e;
+    if (K > 8) {
+        e = cudaFuncSetAttribute(kp, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        if (e != cudaSuccess) return e;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = K;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = ctx.stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cfg.gridDim = dim3(K * 1024);
+    int max_clusters = 0;
+    e = cudaOccupancyMaxActiveClusters(&max_clusters, kp, &cfg);
+    if (e != cudaSuccess) return e;
+    if (max_clusters < 1) return cudaErrorLaunchOutOfResources;
+    const uint64_t nclusters = std::min<uint64_t>(items, static_cast<uint64_t>(max_clusters));
+    cfg.gridDim = dim3(static_cast<unsigned>(nclusters * K));
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 #define EI_CHECK(expr)                                                    \
     do {                                                                  \
         cudaError_t e__ = (expr);                                         \
@@ -406,13 +501,12 @@ int launch_row(uint8_t* data, const Pass& p, const Fn& fn, ExecContext& ctx) {
         RowArgs a;
         a.base = data + p.offset;
         a.rows = p.rows; a.cols = p.cols; a.items = items;
+        a.P = (p.cols + st.K - 1) / st.K;
         a.g = g;
         a.div_rows = FastDiv::make(p.rows, p.batches * p.rows);
-        const size_t smem = p.cols * st.w;
-        const void* k = reinterpret_cast<const void*>(&k_row_smem<US, Fn, kScatter>);
-        EI_CHECK(prep_smem(k, smem));
-        const int grid = grid_for(k, smem, items, ctx);
-        k_row_smem<US, Fn, kScatter><<<grid, kThreads, smem, ctx.stream>>>(a, fn);
+        a.div_P = FastDiv::make(a.P, p.cols);
+        const size_t smem = a.P * st.w;
+        EI_CHECK(launch_clusters(k_row_cluster<US, Fn, kScatter>, st.K, smem, items, ctx, a, fn));
         EI_CHECK(cudaGetLastError());
         ctx.launches++;
         return 0;
@@ -456,14 +550,13 @@ int launch_col(uint8_t* data, const Pass& p, const Fn& fn, ExecContext& ctx) {
         a.base = data + p.offset;
         a.rows = p.rows; a.cols = p.cols; a.tw = st.tw; a.ntiles = ntiles; a.pitch = st.pitch;
         a.items = items;
+        a.Q = (p.rows + st.K - 1) / st.K;
         a.g = g;
         a.div_tiles = FastDiv::make(ntiles, p.batches * ntiles);
         a.div_rowunits = FastDiv::make(st.tw * upw, p.rows * st.tw * upw);
-        const size_t smem = st.item_bytes;
-        const void* k = reinterpret_cast<const void*>(&k_col_smem<US, Fn>);
-        EI_CHECK(prep_smem(k, smem));
-        const int grid = grid_for(k, smem, items, ctx);
-        k_col_smem<US, Fn><<<grid, kThreads, smem, ctx.stream>>>(a, fn);
+        a.div_Q = FastDiv::make(a.Q, p.rows);
+        const size_t smem = a.Q * st.pitch;
+        EI_CHECK(launch_clusters(k_col_cluster<US, Fn>, st.K, smem, items, ctx, a, fn));
         EI_CHECK(cudaGetLastError());
         ctx.launches++;
         return 0;

@@ -49,39 +49,64 @@ uint64_t slab_pitch(uint64_t C, uint64_t w) {
 
 size_t slab_smem_bytes(uint64_t R, uint64_t C, uint64_t w) { return R * slab_pitch(C, w); }
 
+namespace {
+// Per-CTA staging target: three CTAs' worth fit one SM, so the load phase of
+// one cluster overlaps the write-back phase of another on the same SM.
+constexpr uint64_t kTargetCtaBytes = 72 * 1024;
+constexpr int kClusterSizes[] = {1, 2, 4, 8, 16};
+}  // namespace
+
 Staging plan_row_staging(uint64_t cols, uint64_t E, size_t cap) {
     Staging s;
     const uint64_t w0 = strip_width(E);
-    for (uint64_t w : {w0, uint64_t(64), uint64_t(32)}) {
-        if (w > w0 || w < std::min<uint64_t>(E, 32)) continue;
-        if (cols * w <= cap) {
-            s.w = w; s.item_bytes = cols * w; s.on_chip = true;
-            return s;
+    for (uint64_t limit : {kTargetCtaBytes, static_cast<uint64_t>(cap)}) {
+        for (uint64_t w : {w0, uint64_t(64), uint64_t(32)}) {
+            if (w > w0 || w < std::min<uint64_t>(E, 32)) continue;
+            for (int K : kClusterSizes) {
+                const uint64_t per = (cols + K - 1) / K * w;
+                if (per <= limit) {
+                    s.w = w; s.K = K; s.per_cta = per; s.item_bytes = cols * w; s.on_chip = true;
+                    return s;
+                }
+            }
         }
     }
     s.w = w0;
+    s.K = 1;
     s.item_bytes = cols * w0;
+    s.per_cta = s.item_bytes;
     s.on_chip = false;
     return s;
 }
 
 Staging plan_col_staging(uint64_t rows, uint64_t E, size_t cap) {
     Staging s;
-    for (uint64_t tb : {uint64_t(128), uint64_t(64), uint64_t(32)}) {
-        uint64_t w, tw;
-        if (E <= tb) { w = E; tw = std::max<uint64_t>(1, tb / E); }
-        else { w = tb; tw = 1; }
-        const uint64_t pitch = slab_pitch(tw, w);
-        if (rows * pitch <= cap) {
-            s.w = w; s.tw = tw; s.pitch = pitch; s.item_bytes = rows * pitch; s.on_chip = true;
-            return s;
+    for (uint64_t limit : {kTargetCtaBytes, static_cast<uint64_t>(cap)}) {
+        for (uint64_t tb : {uint64_t(128), uint64_t(64), uint64_t(32)}) {
+            uint64_t w, tw;
+            if (E <= tb) { w = E; tw = std::max<uint64_t>(1, tb / E); }
+            else { w = tb; tw = 1; }
+            // tw*w contiguous bytes per staged row: a quarter-warp of 16-byte
+            // reads (or a warp of 4-byte reads) covers one row piece, so the
+            // row pitch needs no bank padding
+            const uint64_t pitch = tw * w;
+            for (int K : kClusterSizes) {
+                const uint64_t per = (rows + K - 1) / K * pitch;
+                if (per <= limit) {
+                    s.w = w; s.tw = tw; s.pitch = pitch; s.K = K; s.per_cta = per;
+                    s.item_bytes = rows * pitch; s.on_chip = true;
+                    return s;
+                }
+            }
         }
     }
     // Global staging: 128-byte row pieces.
     s.w = E <= 128 ? E : 128;
     s.tw = E <= 128 ? std::max<uint64_t>(1, 128 / E) : 1;
     s.pitch = s.tw * s.w;
+    s.K = 1;
     s.item_bytes = rows * s.pitch;
+    s.per_cta = s.item_bytes;
     s.on_chip = false;
     return s;
 }

@@ -65,13 +65,17 @@ size_t smem_cap_of(const DeviceCaps& caps);
 
 // How one item of a row or column pass is staged.  A row item is one strip
 // (w bytes of every element) of one row; a column item is one strip of a
-// tile of `tw` adjacent columns over all rows.
+// tile of `tw` adjacent columns over all rows.  An item is split over the K
+// CTAs of a thread-block cluster (K <= 16) and staged in their distributed
+// shared memory; items too large even for that are staged in global scratch.
 struct Staging {
     uint64_t w = 0;        // strip width in bytes
     uint64_t tw = 1;       // columns per item (column passes)
     uint64_t pitch = 0;    // bytes per staged row (column passes)
     uint64_t item_bytes = 0;
-    bool on_chip = false;  // fits one CTA's shared memory
+    int K = 1;             // CTAs of the thread-block cluster sharing one item
+    uint64_t per_cta = 0;  // shared-memory bytes each CTA stages
+    bool on_chip = false;  // the item fits the cluster's distributed shared memory
 };
 
 Staging plan_row_staging(uint64_t cols, uint64_t E, size_t smem_cap);
