@@ -1,5 +1,5 @@
 // Construction of the pass index maps from a Pass, shared by the device
-// executor and host-side tools.  Each FastDiv is sized for the largest
+// executor and host-side tools.  Each divisor is sized for the largest
 // dividend its map can see.
 #pragma once
 
@@ -10,44 +10,68 @@
 
 namespace eithot {
 
-inline FnRowShuffle make_rowshuffle(const Pass& p) {
-    FnRowShuffle f;
-    f.m = static_cast<int64_t>(p.m);
-    f.n = static_cast<int64_t>(p.n);
-    f.c = static_cast<int64_t>(p.c);
-    f.k = p.k;
-    f.b = p.b;
+// The 32-bit flavour of a Catanzaro map is exact when every intermediate
+// value stays below 2^31; the largest is below m*n + m + n.
+inline bool fits32(const Pass& p) {
+    const unsigned __int128 v = static_cast<unsigned __int128>(p.m) * p.n + p.m + p.n;
+    return v < (static_cast<unsigned __int128>(1) << 31);
+}
+
+template <typename I> struct MakeDiv;
+template <> struct MakeDiv<uint32_t> {
+    static FastDiv32 make(uint64_t d, uint64_t) { return FastDiv32::make(d); }
+};
+template <> struct MakeDiv<uint64_t> {
+    static FastDiv make(uint64_t d, uint64_t max_dividend) { return FastDiv::make(d, max_dividend); }
+};
+
+template <typename I>
+inline FnRowShuffleT<I> make_rowshuffle(const Pass& p) {
+    FnRowShuffleT<I> f;
+    f.m = static_cast<I>(p.m);
+    f.n = static_cast<I>(p.n);
+    f.c = static_cast<I>(p.c);
+    f.k = static_cast<I>(p.k);
+    f.b = static_cast<I>(p.b);
     const uint64_t fmax = p.n + p.m * p.n + p.m;
-    f.divc = FastDiv::make(p.c, fmax);
-    const uint64_t bmax = std::max<uint64_t>(fmax / std::max<uint64_t>(p.c, 1) + 1, p.b * p.b);
-    f.divb = FastDiv::make(p.b, bmax);
+    f.divc = MakeDiv<I>::make(p.c, fmax);
+    f.divb = MakeDiv<I>::make(p.b, fmax / std::max<uint64_t>(p.c, 1) + 1);
+    f.divb_mul = FastDiv::make(p.b, p.b * p.b);
     return f;
 }
-inline FnC2RPreRot make_prerot(const Pass& p) {
-    FnC2RPreRot f;
-    f.m = p.m;
-    f.divb = FastDiv::make(p.b, p.n);
+template <typename I>
+inline FnC2RPreRotT<I> make_prerot(const Pass& p) {
+    FnC2RPreRotT<I> f;
+    f.m = static_cast<I>(p.m);
+    f.divb = MakeDiv<I>::make(p.b, p.n);
     return f;
 }
-inline FnR2CPostRot make_postrot(const Pass& p) {
-    FnR2CPostRot f;
-    f.m = p.m;
-    f.divb = FastDiv::make(p.b, p.n);
+template <typename I>
+inline FnR2CPostRotT<I> make_postrot(const Pass& p) {
+    FnR2CPostRotT<I> f;
+    f.m = static_cast<I>(p.m);
+    f.divb = MakeDiv<I>::make(p.b, p.n);
     return f;
 }
-inline FnC2RColShuffle make_c2r_colshuf(const Pass& p) {
-    FnC2RColShuffle f;
-    f.n = p.n;
-    f.c = p.c;
-    f.divm = FastDiv::make(p.m, p.m * p.n + p.n + p.m * p.c);
+template <typename I>
+inline FnC2RColShuffleT<I> make_c2r_colshuf(const Pass& p) {
+    FnC2RColShuffleT<I> f;
+    f.n = static_cast<I>(p.n);
+    f.c = static_cast<I>(p.c);
+    f.divm = MakeDiv<I>::make(p.m, p.m * p.n + p.n + p.m * p.c);
     return f;
 }
-inline FnR2CColShuffle make_r2c_colshuf(const Pass& p) {
-    FnR2CColShuffle f;
-    f.m = p.m; f.a = p.a; f.c = p.c; f.q = p.q;
-    f.divm = FastDiv::make(p.m, p.n + p.m);
-    f.divc = FastDiv::make(p.c, p.c * p.m + p.c + p.m);
-    f.diva = FastDiv::make(p.a, std::max<uint64_t>(p.m + p.c, p.a * p.a));
+template <typename I>
+inline FnR2CColShuffleT<I> make_r2c_colshuf(const Pass& p) {
+    FnR2CColShuffleT<I> f;
+    f.m = static_cast<I>(p.m);
+    f.a = static_cast<I>(p.a);
+    f.c = static_cast<I>(p.c);
+    f.q = static_cast<I>(p.q);
+    f.divm = MakeDiv<I>::make(p.m, p.n + p.m);
+    f.divc = MakeDiv<I>::make(p.c, p.c * p.m + p.c + p.m);
+    f.diva = MakeDiv<I>::make(p.a, p.m + p.c);
+    f.diva_mul = FastDiv::make(p.a, p.a * p.a);
     return f;
 }
 

@@ -1,6 +1,8 @@
 // Index arithmetic shared by the host planner and the sm_103a kernels:
 // division by run-time-invariant divisors and the permutation index maps of
-// the in-place passes.  All maps are pure functions of 64-bit indices.
+// the in-place passes.  Every map exists in a 32-bit flavour (used when the
+// host has checked that all its intermediate values stay below 2^31) and a
+// 64-bit flavour.
 #pragma once
 
 #include <cstdint>
@@ -41,8 +43,6 @@ struct FastDiv {
     uint32_t s = 0;
     uint32_t mode = 0;  // 0: d==1, 1: power of two, 2: 32-bit magic, 3: 64-bit magic
 
-    FastDiv() = default;
-
     // max_dividend: an upper bound (inclusive) on every x passed to div().
     static FastDiv make(uint64_t divisor, uint64_t max_dividend) {
         FastDiv f;
@@ -76,7 +76,35 @@ struct FastDiv {
     EI_HD void divmod(uint64_t x, uint64_t& q, uint64_t& r) const { q = div(x); r = x - q * d; }
 };
 
-// (a * b) mod n for a, b < n.
+// 32-bit-only variant: divisor and every dividend below 2^31.
+struct FastDiv32 {
+    uint32_t d = 1;
+    uint32_t m = 0;
+    uint32_t s = 0;
+    uint32_t mode = 0;  // 0: d==1, 1: power of two, 2: magic
+
+    static FastDiv32 make(uint64_t divisor) {
+        const FastDiv f = FastDiv::make(divisor, 0);
+        FastDiv32 g;
+        g.d = static_cast<uint32_t>(f.d);
+        g.m = static_cast<uint32_t>(f.m);
+        g.s = f.s;
+        g.mode = f.mode;
+        return g;
+    }
+    EI_HD uint32_t div(uint32_t x) const {
+        return mode == 2 ? (mulhi32(x, m) >> s) : (mode == 1 ? (x >> s) : x);
+    }
+    EI_HD uint32_t mod(uint32_t x) const { return x - div(x) * d; }
+    EI_HD void divmod(uint32_t x, uint32_t& q, uint32_t& r) const { q = div(x); r = x - q * d; }
+};
+
+template <typename I> struct DivOf;
+template <> struct DivOf<uint32_t> { using T = FastDiv32; };
+template <> struct DivOf<uint64_t> { using T = FastDiv; };
+
+// (a * b) mod n for a, b < n; n built with max_dividend >= (n-1)^2 when
+// n <= 2^31.
 EI_HD uint64_t mulmod(uint64_t a, uint64_t b, const FastDiv& n) {
     if (n.d <= (uint64_t(1) << 31)) return n.mod(a * b);  // a*b < 2^62
     unsigned __int128 p = static_cast<unsigned __int128>(a) * b;
@@ -89,33 +117,20 @@ EI_HD uint64_t mulmod(uint64_t a, uint64_t b, const FastDiv& n) {
 //   row gather : out[i][j] = in[i][f(i,j)]
 //   row scatter: out[i][f(i,j)] = in[i][j]
 //   col gather : out[i][j] = in[g(i,j)][j]
-// ---------------------------------------------------------------------------
-
-// Transpose of an R x C matrix flattened into one row of R*C elements
-// (the single-pass "linearisation" of EITHOT's 213 row_shuffle,
-// ITNT/src/equations.h:285-311, generalised to any element width):
-// output o = c*R + r takes input r*C + c.
-struct FnTranspose {
-    uint64_t R, C;
-    FastDiv divR;
-    EI_HD uint64_t operator()(uint64_t, uint64_t o) const {
-        uint64_t c, r;
-        divR.divmod(o, c, r);
-        return r * C + c;
-    }
-};
-
 // Catanzaro, Keller & Garland, "A decomposition for in-place matrix
-// transposition" (PPoPP 2014), as parameterised by EITHOT
+// transposition" (PPoPP 2014), parameterised as in EITHOT
 // (ITNT/src/equations.h:319-534, ITNT/src/2dtranspose.cpp:130-181).
 // View: m rows x n cols; c = gcd(m, n); b = n / c; k = (m/c)^-1 mod (n/c).
+// ---------------------------------------------------------------------------
 
 // c2r pre-rotation (col gather): row i of column j takes row (i + j/b) mod m.
-struct FnC2RPreRot {
-    uint64_t m;
-    FastDiv divb;
-    EI_HD uint64_t operator()(uint64_t i, uint64_t j) const {
-        uint64_t x = i + divb.div(j);
+template <typename I>
+struct FnC2RPreRotT {
+    using index_type = I;
+    I m;
+    typename DivOf<I>::T divb;
+    EI_HD I operator()(I i, I j) const {
+        const I x = i + divb.div(j);
         return x >= m ? x - m : x;
     }
 };
@@ -123,52 +138,67 @@ struct FnC2RPreRot {
 // Row shuffle used as a gather by c2r and as a scatter by r2c: with
 // f = j + i(n-1) (+ m when i - (j mod c) > m - c),
 // index = (k * (f / c) mod b) + (f mod c) * b.
-struct FnRowShuffle {
-    int64_t m, n, c;
-    uint64_t k, b;
-    FastDiv divc, divb;
-    EI_HD uint64_t operator()(uint64_t i, uint64_t j) const {
-        uint64_t f = j + i * static_cast<uint64_t>(n - 1);
-        const uint64_t jc = divc.mod(j);
-        if (static_cast<int64_t>(i) - static_cast<int64_t>(jc) > m - c) f += static_cast<uint64_t>(m);
-        uint64_t fq, fr;
+template <typename I>
+struct FnRowShuffleT {
+    using index_type = I;
+    I m, n, c, k, b;
+    typename DivOf<I>::T divc, divb;
+    FastDiv divb_mul;  // b, for the product k * x < b^2
+    EI_HD I operator()(I i, I j) const {
+        I f = j + i * (n - 1);
+        const I jc = divc.mod(j);
+        if (static_cast<int64_t>(i) - static_cast<int64_t>(jc) > static_cast<int64_t>(m) - static_cast<int64_t>(c))
+            f += m;
+        I fq, fr;
         divc.divmod(f, fq, fr);
-        return mulmod(k, divb.mod(fq), divb) + fr * b;
+        return static_cast<I>(mulmod(k, divb.mod(fq), divb_mul)) + fr * b;
     }
 };
 
 // c2r column shuffle (col gather): row i of column j takes
 // (i*n - floor(i*c/m) + j) mod m.
-struct FnC2RColShuffle {
-    uint64_t n, c;
-    FastDiv divm;
-    EI_HD uint64_t operator()(uint64_t i, uint64_t j) const {
-        return divm.mod(i * n - divm.div(i * c) + j);
-    }
+template <typename I>
+struct FnC2RColShuffleT {
+    using index_type = I;
+    I n, c;
+    typename DivOf<I>::T divm;
+    EI_HD I operator()(I i, I j) const { return divm.mod(i * n - divm.div(i * c) + j); }
 };
 
 // r2c column shuffle (col gather): row i of column j takes
-// p((i + m - (j mod m)) mod m), p(x) = a*((c-1)x mod c) + ((ceil-ish(x/c))*q mod a).
-struct FnR2CColShuffle {
-    uint64_t m, a, c, q;
-    FastDiv divm, divc, diva;
-    EI_HD uint64_t operator()(uint64_t i, uint64_t j) const {
-        uint64_t x = i + m - divm.mod(j);
+// p((i + m - (j mod m)) mod m) with
+// p(x) = a*((c-1)x mod c) + (floor((c-1+x)/c) * q mod a).
+template <typename I>
+struct FnR2CColShuffleT {
+    using index_type = I;
+    I m, a, c, q;
+    typename DivOf<I>::T divm, divc, diva;
+    FastDiv diva_mul;  // a, for the product (.) * q < a^2
+    EI_HD I operator()(I i, I j) const {
+        I x = i + m - divm.mod(j);
         if (x >= m) x -= m;
-        const uint64_t t1 = a * divc.mod((c - 1) * x);
-        const uint64_t t2 = mulmod(diva.mod(divc.div(c - 1 + x)), q, diva);
+        const I t1 = a * divc.mod((c - 1) * x);
+        const I t2 = static_cast<I>(mulmod(diva.mod(divc.div(c - 1 + x)), q, diva_mul));
         return t1 + t2;
     }
 };
 
 // r2c post-rotation (col gather): row i of column j takes (i + m - j/b) mod m.
-struct FnR2CPostRot {
-    uint64_t m;
-    FastDiv divb;
-    EI_HD uint64_t operator()(uint64_t i, uint64_t j) const {
-        uint64_t x = i + m - divb.div(j);
+template <typename I>
+struct FnR2CPostRotT {
+    using index_type = I;
+    I m;
+    typename DivOf<I>::T divb;
+    EI_HD I operator()(I i, I j) const {
+        const I x = i + m - divb.div(j);
         return x >= m ? x - m : x;
     }
 };
+
+using FnC2RPreRot = FnC2RPreRotT<uint64_t>;
+using FnRowShuffle = FnRowShuffleT<uint64_t>;
+using FnC2RColShuffle = FnC2RColShuffleT<uint64_t>;
+using FnR2CColShuffle = FnR2CColShuffleT<uint64_t>;
+using FnR2CPostRot = FnR2CPostRotT<uint64_t>;
 
 }  // namespace eithot

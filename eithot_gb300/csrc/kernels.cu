@@ -78,48 +78,79 @@ struct StripGeom {
     FastDiv div_upw, div_strips;
 };
 
+// Cluster barriers.  The middle barrier of an item publishes the staged
+// shared-memory data (release/acquire); the end-of-item barrier only has to
+// keep a CTA from restaging before its peers finished reading it, and every
+// such read has returned its value before the reader arrives, so it is
+// relaxed and does not wait for the item's global stores to drain.
+__device__ __forceinline__ void cluster_sync_publish() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+    asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+__device__ __forceinline__ void cluster_sync_reuse() {
+    asm volatile("barrier.cluster.arrive.relaxed.aligned;\n" ::: "memory");
+    asm volatile("barrier.cluster.wait.aligned;\n" ::: "memory");
+}
+
+// Generic addresses of every peer CTA's dynamic shared memory (K <= 16).
+__device__ __forceinline__ void load_peers(uint8_t** peers, uint8_t* smem, unsigned K) {
+    cg::cluster_group cl = cg::this_cluster();
+    if (threadIdx.x < K) peers[threadIdx.x] = static_cast<uint8_t*>(cl.map_shared_rank(static_cast<void*>(smem), threadIdx.x));
+    __syncthreads();
+}
+
 // ---------------------------------------------------------------------------
 // Slab transpose: B matrices of R x C elements, one strip of one matrix per
 // work item, staged with a padded pitch so the transposed reads are
-// conflict-free.
+// conflict-free.  All intra-item indices are 32-bit (an item is at most the
+// 227 KB of one CTA's shared memory).
 // ---------------------------------------------------------------------------
 struct SlabArgs {
     uint8_t* base;
-    uint64_t B, R, C, pitch, items;
-    StripGeom g;
-    FastDiv div_C, div_R;
+    uint64_t items, E, mat_bytes;
+    uint32_t R, C, pitch, w, upw, last_upw, rowunits;  // rowunits = C*upw (flat loads)
+    bool flat;                                          // whole elements: rows contiguous
+    FastDiv div_strips;
+    FastDiv32 div_C, div_R, div_upw, div_rowunits;
+    uint32_t nstrips;
 };
 
 template <int US>
 __global__ void __launch_bounds__(kThreads) k_slab(SlabArgs a) {
     using U = typename UnitOf<US>::T;
     extern __shared__ __align__(16) uint8_t smem[];
-    const uint64_t pieces = a.R * a.C;
-    const uint64_t units = pieces * a.g.upw;
-    const uint64_t mat_bytes = pieces * a.g.E;
+    const uint32_t units = a.R * a.C * a.upw;
     for (uint64_t it = blockIdx.x; it < a.items; it += gridDim.x) {
         uint64_t b, s;
-        a.g.div_strips.divmod(it, b, s);
-        const uint64_t lim = (s + 1 == a.g.nstrips) ? a.g.last_upw : a.g.upw;
-        uint8_t* mat = a.base + b * mat_bytes + s * a.g.w;
-        for (uint64_t x = threadIdx.x; x < units; x += blockDim.x) {
-            uint64_t p, u;
-            a.g.div_upw.divmod(x, p, u);
-            if (u >= lim) continue;
-            uint64_t r, c;
-            a.div_C.divmod(p, r, c);
-            copy_in<US, U>(smem + r * a.pitch + c * a.g.w + u * US, mat + p * a.g.E + u * US);
+        a.div_strips.divmod(it, b, s);
+        const uint32_t lim = (s + 1 == a.nstrips) ? a.last_upw : a.upw;
+        uint8_t* mat = a.base + b * a.mat_bytes + s * a.w;
+        if (a.flat) {
+            // the slab is R*C*E contiguous bytes: row r of the staging holds
+            // bytes [r*C*E, (r+1)*C*E)
+            for (uint32_t x = threadIdx.x; x < units; x += blockDim.x) {
+                uint32_t r, rem;
+                a.div_rowunits.divmod(x, r, rem);
+                copy_in<US, U>(smem + r * a.pitch + rem * US, mat + static_cast<uint64_t>(x) * US);
+            }
+        } else {
+            for (uint32_t x = threadIdx.x; x < units; x += blockDim.x) {
+                uint32_t p, u, r, c;
+                a.div_upw.divmod(x, p, u);
+                if (u >= lim) continue;
+                a.div_C.divmod(p, r, c);
+                copy_in<US, U>(smem + r * a.pitch + c * a.w + u * US, mat + p * a.E + u * US);
+            }
         }
         copy_in_wait<US>();
         __syncthreads();
-        for (uint64_t x = threadIdx.x; x < units; x += blockDim.x) {
-            uint64_t o, u;
-            a.g.div_upw.divmod(x, o, u);
+        for (uint32_t x = threadIdx.x; x < units; x += blockDim.x) {
+            uint32_t o, u, c, r;
+            a.div_upw.divmod(x, o, u);
             if (u >= lim) continue;
-            uint64_t c, r;  // output o = c*R + r holds input (r, c)
-            a.div_R.divmod(o, c, r);
-            const U v = *reinterpret_cast<const U*>(smem + r * a.pitch + c * a.g.w + u * US);
-            *reinterpret_cast<U*>(mat + o * a.g.E + u * US) = v;
+            a.div_R.divmod(o, c, r);  // output o = c*R + r holds input (r, c)
+            const U v = *reinterpret_cast<const U*>(smem + r * a.pitch + c * a.w + u * US);
+            *reinterpret_cast<U*>(mat + o * a.E + u * US) = v;
         }
         __syncthreads();
     }
@@ -135,127 +166,175 @@ __global__ void __launch_bounds__(kThreads) k_slab(SlabArgs a) {
 // ---------------------------------------------------------------------------
 struct RowArgs {
     uint8_t* base;
-    uint64_t rows, cols, items, P;
-    StripGeom g;
-    FastDiv div_rows, div_P;
+    uint64_t items, E, row_bytes;
+    uint32_t rows, cols, P, w, upw, last_upw, nstrips;
+    bool flat;  // w == E: a CTA's pieces are contiguous bytes
+    FastDiv div_strips, div_rows;
+    FastDiv32 div_upw, div_P;
 };
 
 template <int US, typename Fn, bool kScatter>
 __global__ void __launch_bounds__(kThreads) k_row_cluster(RowArgs a, Fn fn) {
     using U = typename UnitOf<US>::T;
+    using I = typename Fn::index_type;
     extern __shared__ __align__(16) uint8_t smem[];
+    __shared__ uint8_t* peers[16];
     cg::cluster_group cl = cg::this_cluster();
     const unsigned K = cl.num_blocks();
     const unsigned kr = cl.block_rank();
+    load_peers(peers, smem, K);
     const uint64_t cid = blockIdx.x / K, ncl = gridDim.x / K;
-    const uint64_t j0 = kr * a.P;
-    const uint64_t jn = min(a.cols, j0 + a.P);
-    const uint64_t my_units = (jn > j0 ? jn - j0 : 0) * a.g.upw;
-    const uint64_t row_bytes = a.cols * a.g.E;
+    const uint32_t j0 = kr * a.P;
+    const uint32_t jn = min(a.cols, j0 + a.P);
+    const uint32_t my_units = (jn > j0 ? jn - j0 : 0) * a.upw;
     for (uint64_t it = cid; it < a.items; it += ncl) {
         uint64_t bi, s;
-        a.g.div_strips.divmod(it, bi, s);
-        const uint64_t i = a.div_rows.mod(bi);
-        const uint64_t lim = (s + 1 == a.g.nstrips) ? a.g.last_upw : a.g.upw;
-        uint8_t* row = a.base + bi * row_bytes + s * a.g.w;
-        for (uint64_t x = threadIdx.x; x < my_units; x += blockDim.x) {
-            uint64_t jj, u;
-            a.g.div_upw.divmod(x, jj, u);
-            if (u >= lim) continue;
-            const uint64_t j = j0 + jj;
-            if constexpr (kScatter) {
-                const U v = *reinterpret_cast<const U*>(row + j * a.g.E + u * US);
-                const uint64_t dst = fn(i, j);
+        a.div_strips.divmod(it, bi, s);
+        const I i = static_cast<I>(a.div_rows.mod(bi));
+        const uint32_t lim = (s + 1 == a.nstrips) ? a.last_upw : a.upw;
+        uint8_t* row = a.base + bi * a.row_bytes + s * a.w;
+        if constexpr (kScatter) {
+            for (uint32_t x = threadIdx.x; x < my_units; x += blockDim.x) {
+                uint32_t jj, u;
+                a.div_upw.divmod(x, jj, u);
+                if (u >= lim) continue;
+                const uint32_t j = j0 + jj;
+                const U v = *reinterpret_cast<const U*>(row + static_cast<uint64_t>(j) * a.E + u * US);
+                const I dst = fn(i, static_cast<I>(j));
                 if (!in_range(dst, a.cols)) continue;
-                uint64_t owner, off;
-                a.div_P.divmod(dst, owner, off);
-                *cl.map_shared_rank(reinterpret_cast<U*>(smem + off * a.g.w + u * US), static_cast<unsigned>(owner)) = v;
-            } else {
-                copy_in<US, U>(smem + jj * a.g.w + u * US, row + j * a.g.E + u * US);
+                uint32_t owner, off;
+                a.div_P.divmod(static_cast<uint32_t>(dst), owner, off);
+                *reinterpret_cast<U*>(peers[owner] + off * a.w + u * US) = v;
             }
+        } else if (a.flat) {
+            const uint8_t* src = row + static_cast<uint64_t>(j0) * a.E;
+            for (uint32_t x = threadIdx.x; x < my_units; x += blockDim.x)
+                copy_in<US, U>(smem + x * US, src + static_cast<uint64_t>(x) * US);
+            copy_in_wait<US>();
+        } else {
+            for (uint32_t x = threadIdx.x; x < my_units; x += blockDim.x) {
+                uint32_t jj, u;
+                a.div_upw.divmod(x, jj, u);
+                if (u >= lim) continue;
+                copy_in<US, U>(smem + jj * a.w + u * US, row + static_cast<uint64_t>(j0 + jj) * a.E + u * US);
+            }
+            copy_in_wait<US>();
         }
-        if constexpr (!kScatter) copy_in_wait<US>();
-        cl.sync();
-        for (uint64_t x = threadIdx.x; x < my_units; x += blockDim.x) {
-            uint64_t jj, u;
-            a.g.div_upw.divmod(x, jj, u);
+        cluster_sync_publish();
+        for (uint32_t x = threadIdx.x; x < my_units; x += blockDim.x) {
+            uint32_t jj, u;
+            a.div_upw.divmod(x, jj, u);
             if (u >= lim) continue;
-            const uint64_t j = j0 + jj;
+            const uint32_t j = j0 + jj;
             U v;
             if constexpr (kScatter) {
-                v = *reinterpret_cast<const U*>(smem + jj * a.g.w + u * US);
+                v = *reinterpret_cast<const U*>(smem + jj * a.w + u * US);
             } else {
-                const uint64_t src = fn(i, j);
+                const I src = fn(i, static_cast<I>(j));
                 if (!in_range(src, a.cols)) continue;
-                uint64_t owner, off;
-                a.div_P.divmod(src, owner, off);
-                v = *cl.map_shared_rank(reinterpret_cast<const U*>(smem + off * a.g.w + u * US),
-                                        static_cast<unsigned>(owner));
+                uint32_t owner, off;
+                a.div_P.divmod(static_cast<uint32_t>(src), owner, off);
+                v = *reinterpret_cast<const U*>(peers[owner] + off * a.w + u * US);
             }
-            *reinterpret_cast<U*>(row + j * a.g.E + u * US) = v;
+            *reinterpret_cast<U*>(row + static_cast<uint64_t>(j) * a.E + u * US) = v;
         }
-        cl.sync();
+        cluster_sync_reuse();
     }
 }
 
 // ---------------------------------------------------------------------------
 // Column pass staged in a K-CTA cluster: item = one strip of a tile of tw
-// adjacent columns over all rows; CTA k owns rows [k*Q, (k+1)*Q).
+// adjacent columns over all rows; CTA k owns rows [k*Q, (k+1)*Q).  When the
+// tw*upw units of a staged row divide the block, every thread keeps one
+// fixed unit of the row and walks the rows with a pointer stride.
 // ---------------------------------------------------------------------------
 struct ColArgs {
     uint8_t* base;
-    uint64_t rows, cols, tw, ntiles, pitch, items, Q;
-    StripGeom g;
-    FastDiv div_tiles, div_rowunits, div_Q;  // rowunits = tw * upw
+    uint64_t items, E, row_bytes, mat_bytes;
+    uint32_t rows, cols, tw, ntiles, pitch, Q, w, upw, last_upw, nstrips, RU;  // RU = tw*upw
+    FastDiv div_strips, div_tiles;
+    FastDiv32 div_RU, div_upw, div_Q;
 };
 
-template <int US, typename Fn>
+template <int US, typename Fn, bool kLanes>
 __global__ void __launch_bounds__(kThreads) k_col_cluster(ColArgs a, Fn fn) {
     using U = typename UnitOf<US>::T;
+    using I = typename Fn::index_type;
     extern __shared__ __align__(16) uint8_t smem[];
+    __shared__ uint8_t* peers[16];
     cg::cluster_group cl = cg::this_cluster();
     const unsigned K = cl.num_blocks();
     const unsigned kr = cl.block_rank();
+    load_peers(peers, smem, K);
     const uint64_t cid = blockIdx.x / K, ncl = gridDim.x / K;
-    const uint64_t r0 = kr * a.Q;
-    const uint64_t rn = min(a.rows, r0 + a.Q);
-    const uint64_t rowunits = a.tw * a.g.upw;
-    const uint64_t my_units = (rn > r0 ? rn - r0 : 0) * rowunits;
-    const uint64_t row_bytes = a.cols * a.g.E;
-    const uint64_t mat_bytes = a.rows * row_bytes;
+    const uint32_t r0 = kr * a.Q;
+    const uint32_t rn = min(a.rows, r0 + a.Q);
+    const uint32_t myrows = rn > r0 ? rn - r0 : 0;
+    // fixed lane (kLanes): unit (c, u) of every staged row, rows ii0, ii0+step, ...
+    uint32_t lc = 0, lu = 0, ii0 = 0, step = 1;
+    if constexpr (kLanes) {
+        uint32_t lr;
+        a.div_RU.divmod(threadIdx.x, ii0, lr);
+        a.div_upw.divmod(lr, lc, lu);
+        step = blockDim.x / a.RU;
+    }
     for (uint64_t it = cid; it < a.items; it += ncl) {
         uint64_t bt, s, b, t;
-        a.g.div_strips.divmod(it, bt, s);
+        a.div_strips.divmod(it, bt, s);
         a.div_tiles.divmod(bt, b, t);
-        const uint64_t col0 = t * a.tw;
-        const uint64_t tcols = min(a.tw, a.cols - col0);
-        const uint64_t lim = (s + 1 == a.g.nstrips) ? a.g.last_upw : a.g.upw;
-        uint8_t* mat = a.base + b * mat_bytes + col0 * a.g.E + s * a.g.w;
-        for (uint64_t x = threadIdx.x; x < my_units; x += blockDim.x) {
-            uint64_t ii, r, c, u;
-            a.div_rowunits.divmod(x, ii, r);
-            a.g.div_upw.divmod(r, c, u);
-            if (c >= tcols || u >= lim) continue;
-            copy_in<US, U>(smem + ii * a.pitch + c * a.g.w + u * US,
-                           mat + (r0 + ii) * row_bytes + c * a.g.E + u * US);
+        const uint32_t col0 = static_cast<uint32_t>(t) * a.tw;
+        const uint32_t tcols = min(a.tw, a.cols - col0);
+        const uint32_t lim = (s + 1 == a.nstrips) ? a.last_upw : a.upw;
+        uint8_t* mat = a.base + b * a.mat_bytes + static_cast<uint64_t>(col0) * a.E + s * a.w;
+        if constexpr (kLanes) {
+            const bool active = lc < tcols && lu < lim;
+            const uint64_t gstep = static_cast<uint64_t>(step) * a.row_bytes;
+            const uint64_t lane_off = static_cast<uint64_t>(lc) * a.E + lu * US;
+            if (active) {
+                const uint8_t* g = mat + static_cast<uint64_t>(r0 + ii0) * a.row_bytes + lane_off;
+                uint8_t* sm = smem + ii0 * a.pitch + lc * a.w + lu * US;
+                for (uint32_t ii = ii0; ii < myrows; ii += step, g += gstep, sm += step * a.pitch)
+                    copy_in<US, U>(sm, g);
+            }
+            copy_in_wait<US>();
+            cluster_sync_publish();
+            if (active) {
+                uint8_t* g = mat + static_cast<uint64_t>(r0 + ii0) * a.row_bytes + lane_off;
+                const uint32_t soff = lc * a.w + lu * US;
+                for (uint32_t ii = ii0; ii < myrows; ii += step, g += gstep) {
+                    const I src = fn(static_cast<I>(r0 + ii), static_cast<I>(col0 + lc));
+                    if (!in_range(src, a.rows)) continue;
+                    uint32_t owner, off;
+                    a.div_Q.divmod(static_cast<uint32_t>(src), owner, off);
+                    *reinterpret_cast<U*>(g) = *reinterpret_cast<const U*>(peers[owner] + off * a.pitch + soff);
+                }
+            }
+        } else {
+            const uint32_t my_units = myrows * a.RU;
+            for (uint32_t x = threadIdx.x; x < my_units; x += blockDim.x) {
+                uint32_t ii, r, c, u;
+                a.div_RU.divmod(x, ii, r);
+                a.div_upw.divmod(r, c, u);
+                if (c >= tcols || u >= lim) continue;
+                copy_in<US, U>(smem + ii * a.pitch + c * a.w + u * US,
+                               mat + static_cast<uint64_t>(r0 + ii) * a.row_bytes + static_cast<uint64_t>(c) * a.E + u * US);
+            }
+            copy_in_wait<US>();
+            cluster_sync_publish();
+            for (uint32_t x = threadIdx.x; x < my_units; x += blockDim.x) {
+                uint32_t ii, r, c, u;
+                a.div_RU.divmod(x, ii, r);
+                a.div_upw.divmod(r, c, u);
+                if (c >= tcols || u >= lim) continue;
+                const I src = fn(static_cast<I>(r0 + ii), static_cast<I>(col0 + c));
+                if (!in_range(src, a.rows)) continue;
+                uint32_t owner, off;
+                a.div_Q.divmod(static_cast<uint32_t>(src), owner, off);
+                *reinterpret_cast<U*>(mat + static_cast<uint64_t>(r0 + ii) * a.row_bytes + static_cast<uint64_t>(c) * a.E + u * US) =
+                    *reinterpret_cast<const U*>(peers[owner] + off * a.pitch + c * a.w + u * US);
+            }
         }
-        copy_in_wait<US>();
-        cl.sync();
-        for (uint64_t x = threadIdx.x; x < my_units; x += blockDim.x) {
-            uint64_t ii, r, c, u;
-            a.div_rowunits.divmod(x, ii, r);
-            a.g.div_upw.divmod(r, c, u);
-            if (c >= tcols || u >= lim) continue;
-            const uint64_t i = r0 + ii;
-            const uint64_t src = fn(i, col0 + c);
-            if (!in_range(src, a.rows)) continue;
-            uint64_t owner, off;
-            a.div_Q.divmod(src, owner, off);
-            const U v = *cl.map_shared_rank(reinterpret_cast<const U*>(smem + off * a.pitch + c * a.g.w + u * US),
-                                            static_cast<unsigned>(owner));
-            *reinterpret_cast<U*>(mat + i * row_bytes + c * a.g.E + u * US) = v;
-        }
-        cl.sync();
+        cluster_sync_reuse();
     }
 }
 
@@ -472,13 +551,23 @@ template <int US>
 int launch_slab(uint8_t* data, const Pass& p, ExecContext& ctx) {
     SlabArgs a;
     a.base = data + p.offset;
-    a.B = p.batches; a.R = p.rows; a.C = p.cols;
-    a.pitch = slab_pitch(p.cols, p.strip);
-    const uint64_t upw = p.strip / US;
-    a.g = make_strips(p.elem, p.strip, US, p.batches, p.rows * p.cols * upw);
-    a.items = p.batches * a.g.nstrips;
-    a.div_C = FastDiv::make(p.cols, p.rows * p.cols);
-    a.div_R = FastDiv::make(p.rows, p.rows * p.cols);
+    a.E = p.elem;
+    a.mat_bytes = p.rows * p.cols * p.elem;
+    a.R = static_cast<uint32_t>(p.rows);
+    a.C = static_cast<uint32_t>(p.cols);
+    a.w = static_cast<uint32_t>(p.strip);
+    a.pitch = static_cast<uint32_t>(slab_pitch(p.cols, p.strip));
+    a.upw = a.w / US;
+    a.nstrips = static_cast<uint32_t>((p.elem + p.strip - 1) / p.strip);
+    a.last_upw = static_cast<uint32_t>((p.elem - (a.nstrips - 1) * p.strip) / US);
+    a.flat = (p.strip == p.elem);
+    a.rowunits = a.C * a.upw;
+    a.items = p.batches * a.nstrips;
+    a.div_strips = FastDiv::make(a.nstrips, a.items);
+    a.div_C = FastDiv32::make(a.C);
+    a.div_R = FastDiv32::make(a.R);
+    a.div_upw = FastDiv32::make(a.upw);
+    a.div_rowunits = FastDiv32::make(a.rowunits);
     const size_t smem = slab_smem_bytes(p.rows, p.cols, p.strip);
     const void* k = reinterpret_cast<const void*>(&k_slab<US>);
     EI_CHECK(prep_smem(k, smem));
@@ -491,26 +580,42 @@ int launch_slab(uint8_t* data, const Pass& p, ExecContext& ctx) {
 
 // ---- rows ------------------------------------------------------------------
 template <int US, typename Fn, bool kScatter>
-int launch_row(uint8_t* data, const Pass& p, const Fn& fn, ExecContext& ctx) {
+int launch_row_staged(uint8_t* data, const Pass& p, const Staging& st, ExecContext& ctx, const Fn& fn);
+
+template <int US, typename FnOnChip, typename Fn64, bool kScatter>
+int launch_row(uint8_t* data, const Pass& p, const FnOnChip& fn, const Fn64& fn64, ExecContext& ctx) {
     const size_t cap = smem_cap_of(ctx.caps);
     const Staging st = plan_row_staging(p.cols, p.elem, cap);
+    if (!st.on_chip) return launch_row_staged<US, Fn64, kScatter>(data, p, st, ctx, fn64);
+    RowArgs a;
+    a.base = data + p.offset;
+    a.E = p.elem;
+    a.row_bytes = p.cols * p.elem;
+    a.rows = static_cast<uint32_t>(p.rows);
+    a.cols = static_cast<uint32_t>(p.cols);
+    a.w = static_cast<uint32_t>(st.w);
+    a.upw = a.w / US;
+    a.nstrips = static_cast<uint32_t>((p.elem + st.w - 1) / st.w);
+    a.last_upw = static_cast<uint32_t>((p.elem - (a.nstrips - 1) * st.w) / US);
+    a.flat = (st.w == p.elem);
+    a.P = static_cast<uint32_t>((p.cols + st.K - 1) / st.K);
+    a.items = p.batches * p.rows * a.nstrips;
+    a.div_strips = FastDiv::make(a.nstrips, a.items);
+    a.div_rows = FastDiv::make(p.rows, p.batches * p.rows);
+    a.div_upw = FastDiv32::make(a.upw);
+    a.div_P = FastDiv32::make(a.P);
+    const size_t smem = static_cast<size_t>(a.P) * st.w;
+    EI_CHECK(launch_clusters(k_row_cluster<US, FnOnChip, kScatter>, st.K, smem, a.items, ctx, a, fn));
+    EI_CHECK(cudaGetLastError());
+    ctx.launches++;
+    return 0;
+}
+
+template <int US, typename Fn, bool kScatter>
+int launch_row_staged(uint8_t* data, const Pass& p, const Staging& st, ExecContext& ctx, const Fn& fn) {
     const uint64_t upw = st.w / US;
     const StripGeom g = make_strips(p.elem, st.w, US, p.batches * p.rows, p.cols * upw);
     const uint64_t items = p.batches * p.rows * g.nstrips;
-    if (st.on_chip) {
-        RowArgs a;
-        a.base = data + p.offset;
-        a.rows = p.rows; a.cols = p.cols; a.items = items;
-        a.P = (p.cols + st.K - 1) / st.K;
-        a.g = g;
-        a.div_rows = FastDiv::make(p.rows, p.batches * p.rows);
-        a.div_P = FastDiv::make(a.P, p.cols);
-        const size_t smem = a.P * st.w;
-        EI_CHECK(launch_clusters(k_row_cluster<US, Fn, kScatter>, st.K, smem, items, ctx, a, fn));
-        EI_CHECK(cudaGetLastError());
-        ctx.launches++;
-        return 0;
-    }
     const uint64_t item_bytes = p.cols * st.w;
     if (ctx.scratch_bytes < item_bytes || ctx.scratch == nullptr) {
         ctx.err = "workspace too small for a staged row pass";
@@ -538,29 +643,11 @@ int launch_row(uint8_t* data, const Pass& p, const Fn& fn, ExecContext& ctx) {
 
 // ---- columns ---------------------------------------------------------------
 template <int US, typename Fn>
-int launch_col(uint8_t* data, const Pass& p, const Fn& fn, ExecContext& ctx) {
-    const size_t cap = smem_cap_of(ctx.caps);
-    const Staging st = plan_col_staging(p.rows, p.elem, cap);
+int launch_col_staged(uint8_t* data, const Pass& p, const Staging& st, ExecContext& ctx, const Fn& fn) {
     const uint64_t upw = st.w / US;
     const uint64_t ntiles = (p.cols + st.tw - 1) / st.tw;
     const StripGeom g = make_strips(p.elem, st.w, US, p.batches * ntiles, p.rows * st.tw * upw);
     const uint64_t items = p.batches * ntiles * g.nstrips;
-    if (st.on_chip) {
-        ColArgs a;
-        a.base = data + p.offset;
-        a.rows = p.rows; a.cols = p.cols; a.tw = st.tw; a.ntiles = ntiles; a.pitch = st.pitch;
-        a.items = items;
-        a.Q = (p.rows + st.K - 1) / st.K;
-        a.g = g;
-        a.div_tiles = FastDiv::make(ntiles, p.batches * ntiles);
-        a.div_rowunits = FastDiv::make(st.tw * upw, p.rows * st.tw * upw);
-        a.div_Q = FastDiv::make(a.Q, p.rows);
-        const size_t smem = a.Q * st.pitch;
-        EI_CHECK(launch_clusters(k_col_cluster<US, Fn>, st.K, smem, items, ctx, a, fn));
-        EI_CHECK(cudaGetLastError());
-        ctx.launches++;
-        return 0;
-    }
     const uint64_t item_bytes = p.rows * st.tw * st.w;
     if (ctx.scratch_bytes < item_bytes || ctx.scratch == nullptr) {
         ctx.err = "workspace too small for a staged column pass";
@@ -585,6 +672,43 @@ int launch_col(uint8_t* data, const Pass& p, const Fn& fn, ExecContext& ctx) {
         EI_CHECK(cudaGetLastError());
         ctx.launches += 2;
     }
+    return 0;
+}
+
+template <int US, typename FnOnChip, typename Fn64>
+int launch_col(uint8_t* data, const Pass& p, const FnOnChip& fn, const Fn64& fn64, ExecContext& ctx) {
+    const size_t cap = smem_cap_of(ctx.caps);
+    const Staging st = plan_col_staging(p.rows, p.elem, cap);
+    if (!st.on_chip) return launch_col_staged<US, Fn64>(data, p, st, ctx, fn64);
+    ColArgs a;
+    a.base = data + p.offset;
+    a.E = p.elem;
+    a.row_bytes = p.cols * p.elem;
+    a.mat_bytes = p.rows * a.row_bytes;
+    a.rows = static_cast<uint32_t>(p.rows);
+    a.cols = static_cast<uint32_t>(p.cols);
+    a.tw = static_cast<uint32_t>(st.tw);
+    a.ntiles = static_cast<uint32_t>((p.cols + st.tw - 1) / st.tw);
+    a.pitch = static_cast<uint32_t>(st.pitch);
+    a.w = static_cast<uint32_t>(st.w);
+    a.upw = a.w / US;
+    a.nstrips = static_cast<uint32_t>((p.elem + st.w - 1) / st.w);
+    a.last_upw = static_cast<uint32_t>((p.elem - (a.nstrips - 1) * st.w) / US);
+    a.RU = a.tw * a.upw;
+    a.Q = static_cast<uint32_t>((p.rows + st.K - 1) / st.K);
+    a.items = p.batches * a.ntiles * a.nstrips;
+    a.div_strips = FastDiv::make(a.nstrips, a.items);
+    a.div_tiles = FastDiv::make(a.ntiles, p.batches * a.ntiles);
+    a.div_RU = FastDiv32::make(a.RU);
+    a.div_upw = FastDiv32::make(a.upw);
+    a.div_Q = FastDiv32::make(a.Q);
+    const size_t smem = static_cast<size_t>(a.Q) * st.pitch;
+    if (kThreads % a.RU == 0)
+        EI_CHECK(launch_clusters(k_col_cluster<US, FnOnChip, true>, st.K, smem, a.items, ctx, a, fn));
+    else
+        EI_CHECK(launch_clusters(k_col_cluster<US, FnOnChip, false>, st.K, smem, a.items, ctx, a, fn));
+    EI_CHECK(cudaGetLastError());
+    ctx.launches++;
     return 0;
 }
 
@@ -655,20 +779,39 @@ int block_move(uint8_t* data, const Pass& p, ExecContext& ctx) {
 }
 
 // ---- dispatch ------------------------------------------------------------------
+template <int US, template <typename> class FnT, typename Make32, typename Make64>
+int run_col(uint8_t* data, const Pass& p, ExecContext& ctx, Make32 m32, Make64 m64) {
+    const FnT<uint64_t> f64 = m64(p);
+    if (fits32(p)) return launch_col<US>(data, p, m32(p), f64, ctx);
+    return launch_col<US>(data, p, f64, f64, ctx);
+}
+
 template <int US>
 int run_pass_u(uint8_t* data, const Pass& p, ExecContext& ctx) {
     switch (p.type) {
         case kSlabTranspose: return launch_slab<US>(data, p, ctx);
         case kRowGather:
-            return launch_row<US, FnRowShuffle, false>(data, p, make_rowshuffle(p), ctx);
-        case kRowScatter:
-            return launch_row<US, FnRowShuffle, true>(data, p, make_rowshuffle(p), ctx);
+        case kRowScatter: {
+            const FnRowShuffleT<uint64_t> f64 = make_rowshuffle<uint64_t>(p);
+            const bool sc = p.type == kRowScatter;
+            if (fits32(p)) {
+                const FnRowShuffleT<uint32_t> f32 = make_rowshuffle<uint32_t>(p);
+                return sc ? launch_row<US, FnRowShuffleT<uint32_t>, FnRowShuffleT<uint64_t>, true>(data, p, f32, f64, ctx)
+                          : launch_row<US, FnRowShuffleT<uint32_t>, FnRowShuffleT<uint64_t>, false>(data, p, f32, f64, ctx);
+            }
+            return sc ? launch_row<US, FnRowShuffleT<uint64_t>, FnRowShuffleT<uint64_t>, true>(data, p, f64, f64, ctx)
+                      : launch_row<US, FnRowShuffleT<uint64_t>, FnRowShuffleT<uint64_t>, false>(data, p, f64, f64, ctx);
+        }
         case kColGather:
             switch (p.fn) {
-                case kFnC2RPreRot: return launch_col<US, FnC2RPreRot>(data, p, make_prerot(p), ctx);
-                case kFnC2RColShuffle: return launch_col<US, FnC2RColShuffle>(data, p, make_c2r_colshuf(p), ctx);
-                case kFnR2CColShuffle: return launch_col<US, FnR2CColShuffle>(data, p, make_r2c_colshuf(p), ctx);
-                case kFnR2CPostRot: return launch_col<US, FnR2CPostRot>(data, p, make_postrot(p), ctx);
+                case kFnC2RPreRot:
+                    return run_col<US, FnC2RPreRotT>(data, p, ctx, make_prerot<uint32_t>, make_prerot<uint64_t>);
+                case kFnC2RColShuffle:
+                    return run_col<US, FnC2RColShuffleT>(data, p, ctx, make_c2r_colshuf<uint32_t>, make_c2r_colshuf<uint64_t>);
+                case kFnR2CColShuffle:
+                    return run_col<US, FnR2CColShuffleT>(data, p, ctx, make_r2c_colshuf<uint32_t>, make_r2c_colshuf<uint64_t>);
+                case kFnR2CPostRot:
+                    return run_col<US, FnR2CPostRotT>(data, p, ctx, make_postrot<uint32_t>, make_postrot<uint64_t>);
                 default: break;
             }
             break;

@@ -50,7 +50,7 @@ void apply(uint8_t* data, const Pass& p) {
         }
         case kRowGather:
         case kRowScatter: {
-            const FnRowShuffle fn = make_rowshuffle(p);
+            const FnRowShuffle fn = make_rowshuffle<uint64_t>(p);
             std::vector<uint8_t> tmp(p.cols * E);
             for (uint64_t bi = 0; bi < p.batches * p.rows; ++bi) {
                 const uint64_t i = bi % p.rows;
@@ -65,10 +65,10 @@ void apply(uint8_t* data, const Pass& p) {
         }
         case kColGather:
             switch (p.fn) {
-                case kFnC2RPreRot: col_gather(base, p, make_prerot(p)); break;
-                case kFnC2RColShuffle: col_gather(base, p, make_c2r_colshuf(p)); break;
-                case kFnR2CColShuffle: col_gather(base, p, make_r2c_colshuf(p)); break;
-                case kFnR2CPostRot: col_gather(base, p, make_postrot(p)); break;
+                case kFnC2RPreRot: col_gather(base, p, make_prerot<uint64_t>(p)); break;
+                case kFnC2RColShuffle: col_gather(base, p, make_c2r_colshuf<uint64_t>(p)); break;
+                case kFnR2CColShuffle: col_gather(base, p, make_r2c_colshuf<uint64_t>(p)); break;
+                case kFnR2CPostRot: col_gather(base, p, make_postrot<uint64_t>(p)); break;
             }
             break;
         case kBlockMove:
@@ -118,6 +118,38 @@ int hs_describe(char* buf, size_t len, int rank, const int64_t* dims, const int*
     std::strncpy(buf, s.c_str(), len);
     if (len) buf[len - 1] = 0;
     return static_cast<int>(passes.size());
+}
+
+// Compares the 32-bit flavour of every Catanzaro map the plan uses with the
+// 64-bit flavour over all (i, j) when m*n <= max_full, else a strided
+// sample.  Returns the number of disagreements (or -1 on error).
+long hs_check_fn32(int rank, const int64_t* dims, const int* perm, size_t elem, int nb, double alpha,
+                   int order, long max_full) {
+    NdPlan plan;
+    if (!make_nd_plan(rank, dims, perm, nb, alpha, order, &plan, &g_err)) return -1;
+    std::vector<Pass> passes;
+    DeviceCaps caps;
+    if (!lower_plan(plan, elem, caps, &passes, &g_err)) return -1;
+    long bad = 0;
+    for (const Pass& p : passes) {
+        if (p.type != kRowGather && p.type != kRowScatter && p.type != kColGather) continue;
+        if (!fits32(p)) continue;
+        const uint64_t total = p.m * p.n;
+        const uint64_t stride = total <= static_cast<uint64_t>(max_full) ? 1 : total / max_full + 1;
+        for (uint64_t x = 0; x < total; x += stride) {
+            const uint64_t i = x / p.n, j = x % p.n;
+            uint64_t a = 0, b = 0;
+            switch (p.type == kColGather ? p.fn : -1) {
+                case -1: a = make_rowshuffle<uint64_t>(p)(i, j); b = make_rowshuffle<uint32_t>(p)(i, j); break;
+                case kFnC2RPreRot: a = make_prerot<uint64_t>(p)(i, j); b = make_prerot<uint32_t>(p)(i, j); break;
+                case kFnC2RColShuffle: a = make_c2r_colshuf<uint64_t>(p)(i, j); b = make_c2r_colshuf<uint32_t>(p)(i, j); break;
+                case kFnR2CColShuffle: a = make_r2c_colshuf<uint64_t>(p)(i, j); b = make_r2c_colshuf<uint32_t>(p)(i, j); break;
+                case kFnR2CPostRot: a = make_postrot<uint64_t>(p)(i, j); b = make_postrot<uint32_t>(p)(i, j); break;
+            }
+            if (a != b) ++bad;
+        }
+    }
+    return bad;
 }
 
 }  // extern "C"

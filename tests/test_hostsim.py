@@ -55,3 +55,20 @@ def test_large_elements(hostsim):
     assert run(hostsim, [700, 3, 600], [1, 3, 2], 2)
     assert run(hostsim, [64, 6, 5, 70], [1, 3, 2, 4], 4)
     assert run(hostsim, [1500, 2, 300], [1, 3, 2], 4)
+
+
+@pytest.mark.parametrize("dims,perm,elem", [
+    ([4, 20011, 8192, 2], [1, 3, 2, 4], 4), ([3001, 4096], [2, 1], 4), ([2048, 1536], [2, 1], 4),
+    ([9973, 1024], [2, 1], 8), ([16, 3001, 1024, 25, 4], [5, 3, 1, 4, 2], 2), ([1000, 999], [2, 1], 2),
+    ([60000, 300], [2, 1], 4), ([17, 30011, 37], [1, 3, 2], 4)])
+def test_32bit_maps_agree_with_64bit(hostsim, dims, perm, elem):
+    """The kernels use the 32-bit flavour of a map whenever every
+    intermediate stays below 2^31; it must equal the 64-bit flavour."""
+    import ctypes
+    r = len(dims)
+    hostsim.hs_check_fn32.restype = ctypes.c_long
+    hostsim.hs_check_fn32.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int),
+                                      ctypes.c_size_t, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_long]
+    bad = hostsim.hs_check_fn32(r, (ctypes.c_int64 * r)(*dims), (ctypes.c_int * r)(*perm), elem, 1, 0.01, 0,
+                                2000000)
+    assert bad == 0
