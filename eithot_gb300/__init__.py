@@ -72,6 +72,8 @@ def _load():
     lib.eithot_profile_get.argtypes = [ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t,
                                        ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
     lib.eithot_last_stats.argtypes = [ctypes.POINTER(_Stats)]
+    lib.eithot_tune_set.argtypes = [ctypes.c_char_p, ctypes.c_double]
+    lib.eithot_tune_get.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double)]
     return lib
 
 
@@ -215,4 +217,15 @@ def index_faults() -> int:
     (kernels skip them); synchronises the device."""
     v = ctypes.c_uint()
     _check(lib.eithot_index_faults(ctypes.byref(v)))
+    return v.value
+
+
+def tune_set(key: str, value: float) -> None:
+    """Process-wide lowering knob ("cta_bytes", "max_cluster", "variant")."""
+    _check(lib.eithot_tune_set(key.encode(), float(value)))
+
+
+def tune_get(key: str) -> float:
+    v = ctypes.c_double()
+    _check(lib.eithot_tune_get(key.encode(), ctypes.byref(v)))
     return v.value

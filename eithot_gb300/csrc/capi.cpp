@@ -79,6 +79,38 @@ const char* eithot_last_error(void) { return g_err.c_str(); }
 
 int eithot_version(void) { return 100; }
 
+int eithot_tune_set(const char* key, double value) {
+    if (!key) return fail(EITHOT_EINVAL, "null key");
+    eithot::Tuning& t = eithot::tuning();
+    const std::string k(key);
+    if (k == "cta_bytes") {
+        if (value < 1024 || value > 232448) return fail(EITHOT_EINVAL, "cta_bytes out of range");
+        t.cta_bytes = static_cast<uint64_t>(value);
+    } else if (k == "max_cluster") {
+        const int v = static_cast<int>(value);
+        if (v != 1 && v != 2 && v != 4 && v != 8 && v != 16) return fail(EITHOT_EINVAL, "max_cluster must be 1, 2, 4, 8 or 16");
+        t.max_cluster = v;
+    } else if (k == "variant") {
+        const int v = static_cast<int>(value);
+        if (v < 0 || v > 2) return fail(EITHOT_EINVAL, "variant must be 0, 1 or 2");
+        t.variant = v;
+    } else {
+        return fail(EITHOT_EINVAL, "unknown tuning key " + k);
+    }
+    return EITHOT_OK;
+}
+
+int eithot_tune_get(const char* key, double* value) {
+    if (!key || !value) return fail(EITHOT_EINVAL, "null argument");
+    const eithot::Tuning& t = eithot::tuning();
+    const std::string k(key);
+    if (k == "cta_bytes") *value = static_cast<double>(t.cta_bytes);
+    else if (k == "max_cluster") *value = t.max_cluster;
+    else if (k == "variant") *value = t.variant;
+    else return fail(EITHOT_EINVAL, "unknown tuning key " + k);
+    return EITHOT_OK;
+}
+
 int eithot_set_profiling(int enable) {
     g_profile = enable != 0;
     return EITHOT_OK;

@@ -163,15 +163,57 @@ __global__ void __launch_bounds__(kThreads) k_slab(SlabArgs a) {
 // CTA writes its pieces reading f(i,j) from whichever CTA holds it.
 // Scatter: each CTA loads its pieces and stores piece j into the CTA that
 // owns f(i,j); after the cluster barrier each CTA writes its own range.
+// Items are double-buffered: the loads of the next item are issued before
+// the write-back of the current one, so HBM reads overlap the gathers.
 // ---------------------------------------------------------------------------
 struct RowArgs {
     uint8_t* base;
     uint64_t items, E, row_bytes;
-    uint32_t rows, cols, P, w, upw, last_upw, nstrips;
+    uint32_t rows, cols, P, w, upw, last_upw, nstrips, buf_bytes;
     bool flat;  // w == E: a CTA's pieces are contiguous bytes
     FastDiv div_strips, div_rows;
     FastDiv32 div_upw, div_P;
 };
+
+constexpr int kBatch = 4;  // remote shared-memory loads in flight per thread
+
+template <int US, typename Fn, bool kScatter>
+__device__ __forceinline__ void row_stage_in(const RowArgs& a, const Fn& fn, uint8_t* const* peers, uint8_t* buf,
+                                             uint32_t boff, uint64_t it, uint32_t j0, uint32_t my_units) {
+    using U = typename UnitOf<US>::T;
+    using I = typename Fn::index_type;
+    uint64_t bi, s;
+    a.div_strips.divmod(it, bi, s);
+    const uint32_t lim = (s + 1 == a.nstrips) ? a.last_upw : a.upw;
+    const uint8_t* row = a.base + bi * a.row_bytes + s * a.w;
+    if constexpr (kScatter) {
+        const I i = static_cast<I>(a.div_rows.mod(bi));
+        for (uint32_t x = threadIdx.x; x < my_units; x += blockDim.x) {
+            uint32_t jj, u;
+            a.div_upw.divmod(x, jj, u);
+            if (u >= lim) continue;
+            const uint32_t j = j0 + jj;
+            const U v = *reinterpret_cast<const U*>(row + static_cast<uint64_t>(j) * a.E + u * US);
+            const I dst = fn(i, static_cast<I>(j));
+            if (!in_range(dst, a.cols)) continue;
+            uint32_t owner, off;
+            a.div_P.divmod(static_cast<uint32_t>(dst), owner, off);
+            *reinterpret_cast<U*>(peers[owner] + boff + off * a.w + u * US) = v;
+        }
+    } else if (a.flat) {
+        const uint8_t* src = row + static_cast<uint64_t>(j0) * a.E;
+        for (uint32_t x = threadIdx.x; x < my_units; x += blockDim.x)
+            copy_in<US, U>(buf + x * US, src + static_cast<uint64_t>(x) * US);
+    } else {
+        for (uint32_t x = threadIdx.x; x < my_units; x += blockDim.x) {
+            uint32_t jj, u;
+            a.div_upw.divmod(x, jj, u);
+            if (u >= lim) continue;
+            copy_in<US, U>(buf + jj * a.w + u * US, row + static_cast<uint64_t>(j0 + jj) * a.E + u * US);
+        }
+    }
+    if constexpr (US >= 4 && !kScatter) asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
 
 template <int US, typename Fn, bool kScatter>
 __global__ void __launch_bounds__(kThreads) k_row_cluster(RowArgs a, Fn fn) {
@@ -187,56 +229,47 @@ __global__ void __launch_bounds__(kThreads) k_row_cluster(RowArgs a, Fn fn) {
     const uint32_t j0 = kr * a.P;
     const uint32_t jn = min(a.cols, j0 + a.P);
     const uint32_t my_units = (jn > j0 ? jn - j0 : 0) * a.upw;
-    for (uint64_t it = cid; it < a.items; it += ncl) {
+    cluster_sync_reuse();  // every CTA of the cluster is running before any DSMEM access
+    if (cid < a.items) row_stage_in<US, Fn, kScatter>(a, fn, peers, smem, 0, cid, j0, my_units);
+    uint32_t k = 0;
+    for (uint64_t it = cid; it < a.items; it += ncl, ++k) {
+        const uint32_t boff = (k & 1) * a.buf_bytes;
+        if constexpr (US >= 4 && !kScatter) asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        cluster_sync_publish();
+        const uint64_t nxt = it + ncl;
+        if (nxt < a.items)
+            row_stage_in<US, Fn, kScatter>(a, fn, peers, smem + (boff ^ a.buf_bytes), boff ^ a.buf_bytes, nxt, j0, my_units);
         uint64_t bi, s;
         a.div_strips.divmod(it, bi, s);
         const I i = static_cast<I>(a.div_rows.mod(bi));
         const uint32_t lim = (s + 1 == a.nstrips) ? a.last_upw : a.upw;
         uint8_t* row = a.base + bi * a.row_bytes + s * a.w;
-        if constexpr (kScatter) {
-            for (uint32_t x = threadIdx.x; x < my_units; x += blockDim.x) {
+        for (uint32_t x0 = threadIdx.x; x0 < my_units; x0 += kBatch * blockDim.x) {
+            U v[kBatch];
+            uint8_t* dst[kBatch];
+#pragma unroll
+            for (int q = 0; q < kBatch; ++q) {
+                dst[q] = nullptr;
+                const uint32_t x = x0 + q * blockDim.x;
+                if (x >= my_units) continue;
                 uint32_t jj, u;
                 a.div_upw.divmod(x, jj, u);
                 if (u >= lim) continue;
                 const uint32_t j = j0 + jj;
-                const U v = *reinterpret_cast<const U*>(row + static_cast<uint64_t>(j) * a.E + u * US);
-                const I dst = fn(i, static_cast<I>(j));
-                if (!in_range(dst, a.cols)) continue;
-                uint32_t owner, off;
-                a.div_P.divmod(static_cast<uint32_t>(dst), owner, off);
-                *reinterpret_cast<U*>(peers[owner] + off * a.w + u * US) = v;
+                if constexpr (kScatter) {
+                    v[q] = *reinterpret_cast<const U*>(smem + boff + jj * a.w + u * US);
+                } else {
+                    const I src = fn(i, static_cast<I>(j));
+                    if (!in_range(src, a.cols)) continue;
+                    uint32_t owner, off;
+                    a.div_P.divmod(static_cast<uint32_t>(src), owner, off);
+                    v[q] = *reinterpret_cast<const U*>(peers[owner] + boff + off * a.w + u * US);
+                }
+                dst[q] = row + static_cast<uint64_t>(j) * a.E + u * US;
             }
-        } else if (a.flat) {
-            const uint8_t* src = row + static_cast<uint64_t>(j0) * a.E;
-            for (uint32_t x = threadIdx.x; x < my_units; x += blockDim.x)
-                copy_in<US, U>(smem + x * US, src + static_cast<uint64_t>(x) * US);
-            copy_in_wait<US>();
-        } else {
-            for (uint32_t x = threadIdx.x; x < my_units; x += blockDim.x) {
-                uint32_t jj, u;
-                a.div_upw.divmod(x, jj, u);
-                if (u >= lim) continue;
-                copy_in<US, U>(smem + jj * a.w + u * US, row + static_cast<uint64_t>(j0 + jj) * a.E + u * US);
-            }
-            copy_in_wait<US>();
-        }
-        cluster_sync_publish();
-        for (uint32_t x = threadIdx.x; x < my_units; x += blockDim.x) {
-            uint32_t jj, u;
-            a.div_upw.divmod(x, jj, u);
-            if (u >= lim) continue;
-            const uint32_t j = j0 + jj;
-            U v;
-            if constexpr (kScatter) {
-                v = *reinterpret_cast<const U*>(smem + jj * a.w + u * US);
-            } else {
-                const I src = fn(i, static_cast<I>(j));
-                if (!in_range(src, a.cols)) continue;
-                uint32_t owner, off;
-                a.div_P.divmod(static_cast<uint32_t>(src), owner, off);
-                v = *reinterpret_cast<const U*>(peers[owner] + off * a.w + u * US);
-            }
-            *reinterpret_cast<U*>(row + static_cast<uint64_t>(j) * a.E + u * US) = v;
+#pragma unroll
+            for (int q = 0; q < kBatch; ++q)
+                if (dst[q]) *reinterpret_cast<U*>(dst[q]) = v[q];
         }
         cluster_sync_reuse();
     }
@@ -246,15 +279,60 @@ __global__ void __launch_bounds__(kThreads) k_row_cluster(RowArgs a, Fn fn) {
 // Column pass staged in a K-CTA cluster: item = one strip of a tile of tw
 // adjacent columns over all rows; CTA k owns rows [k*Q, (k+1)*Q).  When the
 // tw*upw units of a staged row divide the block, every thread keeps one
-// fixed unit of the row and walks the rows with a pointer stride.
+// fixed unit of the row and walks the rows with a pointer stride.  Items are
+// double-buffered like the row pass.
 // ---------------------------------------------------------------------------
 struct ColArgs {
     uint8_t* base;
     uint64_t items, E, row_bytes, mat_bytes;
-    uint32_t rows, cols, tw, ntiles, pitch, Q, w, upw, last_upw, nstrips, RU;  // RU = tw*upw
+    uint32_t rows, cols, tw, ntiles, pitch, Q, w, upw, last_upw, nstrips, RU, buf_bytes;  // RU = tw*upw
     FastDiv div_strips, div_tiles;
     FastDiv32 div_RU, div_upw, div_Q;
 };
+
+struct ColItem {
+    uint8_t* mat;
+    uint32_t col0, tcols, lim;
+};
+
+__device__ __forceinline__ ColItem col_item(const ColArgs& a, uint64_t it) {
+    uint64_t bt, s, b, t;
+    a.div_strips.divmod(it, bt, s);
+    a.div_tiles.divmod(bt, b, t);
+    ColItem c;
+    c.col0 = static_cast<uint32_t>(t) * a.tw;
+    c.tcols = min(a.tw, a.cols - c.col0);
+    c.lim = (s + 1 == a.nstrips) ? a.last_upw : a.upw;
+    c.mat = a.base + b * a.mat_bytes + static_cast<uint64_t>(c.col0) * a.E + s * a.w;
+    return c;
+}
+
+template <int US, bool kLanes>
+__device__ __forceinline__ void col_stage_in(const ColArgs& a, uint8_t* buf, uint64_t it, uint32_t r0,
+                                             uint32_t myrows, uint32_t lc, uint32_t lu, uint32_t ii0,
+                                             uint32_t step) {
+    using U = typename UnitOf<US>::T;
+    const ColItem ci = col_item(a, it);
+    if constexpr (kLanes) {
+        if (lc < ci.tcols && lu < ci.lim) {
+            const uint64_t gstep = static_cast<uint64_t>(step) * a.row_bytes;
+            const uint8_t* g = ci.mat + static_cast<uint64_t>(r0 + ii0) * a.row_bytes + static_cast<uint64_t>(lc) * a.E + lu * US;
+            uint8_t* sm = buf + ii0 * a.pitch + lc * a.w + lu * US;
+            for (uint32_t ii = ii0; ii < myrows; ii += step, g += gstep, sm += step * a.pitch) copy_in<US, U>(sm, g);
+        }
+    } else {
+        const uint32_t my_units = myrows * a.RU;
+        for (uint32_t x = threadIdx.x; x < my_units; x += blockDim.x) {
+            uint32_t ii, r, c, u;
+            a.div_RU.divmod(x, ii, r);
+            a.div_upw.divmod(r, c, u);
+            if (c >= ci.tcols || u >= ci.lim) continue;
+            copy_in<US, U>(buf + ii * a.pitch + c * a.w + u * US,
+                           ci.mat + static_cast<uint64_t>(r0 + ii) * a.row_bytes + static_cast<uint64_t>(c) * a.E + u * US);
+        }
+    }
+    if constexpr (US >= 4) asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
 
 template <int US, typename Fn, bool kLanes>
 __global__ void __launch_bounds__(kThreads) k_col_cluster(ColArgs a, Fn fn) {
@@ -270,7 +348,6 @@ __global__ void __launch_bounds__(kThreads) k_col_cluster(ColArgs a, Fn fn) {
     const uint32_t r0 = kr * a.Q;
     const uint32_t rn = min(a.rows, r0 + a.Q);
     const uint32_t myrows = rn > r0 ? rn - r0 : 0;
-    // fixed lane (kLanes): unit (c, u) of every staged row, rows ii0, ii0+step, ...
     uint32_t lc = 0, lu = 0, ii0 = 0, step = 1;
     if constexpr (kLanes) {
         uint32_t lr;
@@ -278,35 +355,40 @@ __global__ void __launch_bounds__(kThreads) k_col_cluster(ColArgs a, Fn fn) {
         a.div_upw.divmod(lr, lc, lu);
         step = blockDim.x / a.RU;
     }
-    for (uint64_t it = cid; it < a.items; it += ncl) {
-        uint64_t bt, s, b, t;
-        a.div_strips.divmod(it, bt, s);
-        a.div_tiles.divmod(bt, b, t);
-        const uint32_t col0 = static_cast<uint32_t>(t) * a.tw;
-        const uint32_t tcols = min(a.tw, a.cols - col0);
-        const uint32_t lim = (s + 1 == a.nstrips) ? a.last_upw : a.upw;
-        uint8_t* mat = a.base + b * a.mat_bytes + static_cast<uint64_t>(col0) * a.E + s * a.w;
+    cluster_sync_reuse();  // every CTA of the cluster is running before any DSMEM access
+    if (cid < a.items) col_stage_in<US, kLanes>(a, smem, cid, r0, myrows, lc, lu, ii0, step);
+    uint32_t k = 0;
+    for (uint64_t it = cid; it < a.items; it += ncl, ++k) {
+        const uint32_t boff = (k & 1) * a.buf_bytes;
+        if constexpr (US >= 4) asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        cluster_sync_publish();
+        const uint64_t nxt = it + ncl;
+        if (nxt < a.items) col_stage_in<US, kLanes>(a, smem + (boff ^ a.buf_bytes), nxt, r0, myrows, lc, lu, ii0, step);
+        const ColItem ci = col_item(a, it);
         if constexpr (kLanes) {
-            const bool active = lc < tcols && lu < lim;
-            const uint64_t gstep = static_cast<uint64_t>(step) * a.row_bytes;
-            const uint64_t lane_off = static_cast<uint64_t>(lc) * a.E + lu * US;
-            if (active) {
-                const uint8_t* g = mat + static_cast<uint64_t>(r0 + ii0) * a.row_bytes + lane_off;
-                uint8_t* sm = smem + ii0 * a.pitch + lc * a.w + lu * US;
-                for (uint32_t ii = ii0; ii < myrows; ii += step, g += gstep, sm += step * a.pitch)
-                    copy_in<US, U>(sm, g);
-            }
-            copy_in_wait<US>();
-            cluster_sync_publish();
-            if (active) {
-                uint8_t* g = mat + static_cast<uint64_t>(r0 + ii0) * a.row_bytes + lane_off;
-                const uint32_t soff = lc * a.w + lu * US;
-                for (uint32_t ii = ii0; ii < myrows; ii += step, g += gstep) {
-                    const I src = fn(static_cast<I>(r0 + ii), static_cast<I>(col0 + lc));
-                    if (!in_range(src, a.rows)) continue;
-                    uint32_t owner, off;
-                    a.div_Q.divmod(static_cast<uint32_t>(src), owner, off);
-                    *reinterpret_cast<U*>(g) = *reinterpret_cast<const U*>(peers[owner] + off * a.pitch + soff);
+            if (lc < ci.tcols && lu < ci.lim) {
+                const uint64_t gstep = static_cast<uint64_t>(step) * a.row_bytes;
+                uint8_t* g = ci.mat + static_cast<uint64_t>(r0 + ii0) * a.row_bytes + static_cast<uint64_t>(lc) * a.E + lu * US;
+                const uint32_t soff = boff + lc * a.w + lu * US;
+                const I col = static_cast<I>(ci.col0 + lc);
+                for (uint32_t ii = ii0; ii < myrows; ii += kBatch * step, g += kBatch * gstep) {
+                    U v[kBatch];
+                    bool ok[kBatch];
+#pragma unroll
+                    for (int q = 0; q < kBatch; ++q) {
+                        const uint32_t iq = ii + q * step;
+                        ok[q] = false;
+                        if (iq >= myrows) continue;
+                        const I src = fn(static_cast<I>(r0 + iq), col);
+                        if (!in_range(src, a.rows)) continue;
+                        uint32_t owner, off;
+                        a.div_Q.divmod(static_cast<uint32_t>(src), owner, off);
+                        v[q] = *reinterpret_cast<const U*>(peers[owner] + off * a.pitch + soff);
+                        ok[q] = true;
+                    }
+#pragma unroll
+                    for (int q = 0; q < kBatch; ++q)
+                        if (ok[q]) *reinterpret_cast<U*>(g + q * gstep) = v[q];
                 }
             }
         } else {
@@ -315,23 +397,13 @@ __global__ void __launch_bounds__(kThreads) k_col_cluster(ColArgs a, Fn fn) {
                 uint32_t ii, r, c, u;
                 a.div_RU.divmod(x, ii, r);
                 a.div_upw.divmod(r, c, u);
-                if (c >= tcols || u >= lim) continue;
-                copy_in<US, U>(smem + ii * a.pitch + c * a.w + u * US,
-                               mat + static_cast<uint64_t>(r0 + ii) * a.row_bytes + static_cast<uint64_t>(c) * a.E + u * US);
-            }
-            copy_in_wait<US>();
-            cluster_sync_publish();
-            for (uint32_t x = threadIdx.x; x < my_units; x += blockDim.x) {
-                uint32_t ii, r, c, u;
-                a.div_RU.divmod(x, ii, r);
-                a.div_upw.divmod(r, c, u);
-                if (c >= tcols || u >= lim) continue;
-                const I src = fn(static_cast<I>(r0 + ii), static_cast<I>(col0 + c));
+                if (c >= ci.tcols || u >= ci.lim) continue;
+                const I src = fn(static_cast<I>(r0 + ii), static_cast<I>(ci.col0 + c));
                 if (!in_range(src, a.rows)) continue;
                 uint32_t owner, off;
                 a.div_Q.divmod(static_cast<uint32_t>(src), owner, off);
-                *reinterpret_cast<U*>(mat + static_cast<uint64_t>(r0 + ii) * a.row_bytes + static_cast<uint64_t>(c) * a.E + u * US) =
-                    *reinterpret_cast<const U*>(peers[owner] + off * a.pitch + c * a.w + u * US);
+                *reinterpret_cast<U*>(ci.mat + static_cast<uint64_t>(r0 + ii) * a.row_bytes + static_cast<uint64_t>(c) * a.E + u * US) =
+                    *reinterpret_cast<const U*>(peers[owner] + boff + off * a.pitch + c * a.w + u * US);
             }
         }
         cluster_sync_reuse();
@@ -604,7 +676,8 @@ int launch_row(uint8_t* data, const Pass& p, const FnOnChip& fn, const Fn64& fn6
     a.div_rows = FastDiv::make(p.rows, p.batches * p.rows);
     a.div_upw = FastDiv32::make(a.upw);
     a.div_P = FastDiv32::make(a.P);
-    const size_t smem = static_cast<size_t>(a.P) * st.w;
+    a.buf_bytes = static_cast<uint32_t>((static_cast<uint64_t>(a.P) * st.w + 127) / 128 * 128);
+    const size_t smem = 2 * static_cast<size_t>(a.buf_bytes);
     EI_CHECK(launch_clusters(k_row_cluster<US, FnOnChip, kScatter>, st.K, smem, a.items, ctx, a, fn));
     EI_CHECK(cudaGetLastError());
     ctx.launches++;
@@ -702,7 +775,8 @@ int launch_col(uint8_t* data, const Pass& p, const FnOnChip& fn, const Fn64& fn6
     a.div_RU = FastDiv32::make(a.RU);
     a.div_upw = FastDiv32::make(a.upw);
     a.div_Q = FastDiv32::make(a.Q);
-    const size_t smem = static_cast<size_t>(a.Q) * st.pitch;
+    a.buf_bytes = static_cast<uint32_t>((static_cast<uint64_t>(a.Q) * st.pitch + 127) / 128 * 128);
+    const size_t smem = 2 * static_cast<size_t>(a.buf_bytes);
     if (kThreads % a.RU == 0)
         EI_CHECK(launch_clusters(k_col_cluster<US, FnOnChip, true>, st.K, smem, a.items, ctx, a, fn));
     else

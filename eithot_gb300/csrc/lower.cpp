@@ -50,19 +50,24 @@ uint64_t slab_pitch(uint64_t C, uint64_t w) {
 size_t slab_smem_bytes(uint64_t R, uint64_t C, uint64_t w) { return R * slab_pitch(C, w); }
 
 namespace {
-// Per-CTA staging target: three CTAs' worth fit one SM, so the load phase of
-// one cluster overlaps the write-back phase of another on the same SM.
-constexpr uint64_t kTargetCtaBytes = 72 * 1024;
 constexpr int kClusterSizes[] = {1, 2, 4, 8, 16};
 }  // namespace
+
+Tuning& tuning() {
+    static Tuning t;
+    return t;
+}
 
 Staging plan_row_staging(uint64_t cols, uint64_t E, size_t cap) {
     Staging s;
     const uint64_t w0 = strip_width(E);
-    for (uint64_t limit : {kTargetCtaBytes, static_cast<uint64_t>(cap)}) {
+    // Per-CTA staging target (one of the two item buffers); by default three
+    // CTAs with double buffers fit one SM.
+    for (uint64_t limit : {tuning().cta_bytes, static_cast<uint64_t>(cap / 2)}) {
         for (uint64_t w : {w0, uint64_t(64), uint64_t(32)}) {
             if (w > w0 || w < std::min<uint64_t>(E, 32)) continue;
             for (int K : kClusterSizes) {
+                if (K > tuning().max_cluster) break;
                 const uint64_t per = (cols + K - 1) / K * w;
                 if (per <= limit) {
                     s.w = w; s.K = K; s.per_cta = per; s.item_bytes = cols * w; s.on_chip = true;
@@ -81,7 +86,7 @@ Staging plan_row_staging(uint64_t cols, uint64_t E, size_t cap) {
 
 Staging plan_col_staging(uint64_t rows, uint64_t E, size_t cap) {
     Staging s;
-    for (uint64_t limit : {kTargetCtaBytes, static_cast<uint64_t>(cap)}) {
+    for (uint64_t limit : {tuning().cta_bytes, static_cast<uint64_t>(cap / 2)}) {
         for (uint64_t tb : {uint64_t(128), uint64_t(64), uint64_t(32)}) {
             uint64_t w, tw;
             if (E <= tb) { w = E; tw = std::max<uint64_t>(1, tb / E); }
@@ -91,6 +96,7 @@ Staging plan_col_staging(uint64_t rows, uint64_t E, size_t cap) {
             // row pitch needs no bank padding
             const uint64_t pitch = tw * w;
             for (int K : kClusterSizes) {
+                if (K > tuning().max_cluster) break;
                 const uint64_t per = (rows + K - 1) / K * pitch;
                 if (per <= limit) {
                     s.w = w; s.tw = tw; s.pitch = pitch; s.K = K; s.per_cta = per;
@@ -166,7 +172,9 @@ void lower_xpose(const Xpose& x, const DeviceCaps& caps, std::vector<Pass>* pass
     gcd_inverse(x.R, x.C, &g, &inv);
     const double c2r = (g > 1 ? col_cost(x.R, x.E, cap) : 0.0) + row_cost(x.C, x.E, cap) + col_cost(x.R, x.E, cap);
     const double r2c = col_cost(x.C, x.E, cap) + row_cost(x.R, x.E, cap) + (g > 1 ? col_cost(x.C, x.E, cap) : 0.0);
-    const bool use_c2r = (c2r < r2c) || (c2r == r2c && x.C >= x.R);
+    bool use_c2r = (c2r < r2c) || (c2r == r2c && x.C >= x.R);
+    if (tuning().variant == 1) use_c2r = true;
+    if (tuning().variant == 2) use_c2r = false;
     Pass base;
     base.offset = x.offset;
     base.batches = x.B;

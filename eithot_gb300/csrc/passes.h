@@ -63,6 +63,15 @@ struct DeviceCaps {
 // Shared memory the single-CTA kernels may use per block.
 size_t smem_cap_of(const DeviceCaps& caps);
 
+// Process-wide tuning of the lowering (set through eithot_tune_set; the
+// autotuner fills these per shape).
+struct Tuning {
+    uint64_t cta_bytes = 36 * 1024;  // target bytes one CTA stages per item buffer
+    int max_cluster = 16;            // largest thread-block cluster used
+    int variant = 0;                 // 0: cost model, 1: force c2r, 2: force r2c
+};
+Tuning& tuning();
+
 // How one item of a row or column pass is staged.  A row item is one strip
 // (w bytes of every element) of one row; a column item is one strip of a
 // tile of `tw` adjacent columns over all rows.  An item is split over the K

@@ -142,6 +142,15 @@ int eithot_estimate(int rank, const int64_t* dims, const int* perm_1based,
                     size_t smem_per_block, int padding_blocks,
                     int* nb_out, double* alpha_out, size_t* extra_bytes_out);
 
+/* ---- tuning ----------------------------------------------------------------
+ * No reference counterpart (the reference fixes its kernel choices at
+ * compile time).  Process-wide knobs of the lowering, used by the autotuner:
+ *   "cta_bytes"   bytes one CTA stages per item buffer (1024 .. 232448)
+ *   "max_cluster" largest thread-block cluster (1, 2, 4, 8, 16)
+ *   "variant"     0 cost model, 1 force c2r, 2 force r2c for 2D transposes */
+int eithot_tune_set(const char* key, double value);
+int eithot_tune_get(const char* key, double* value);
+
 /* ---- per-pass profiling -------------------------------------------------
  * No reference counterpart (the reference times only whole calls,
  * ITNT/src/test_inplace.cpp:43-69).  When enabled for the calling thread,
