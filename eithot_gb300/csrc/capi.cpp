@@ -83,9 +83,8 @@ int eithot_tune_set(const char* key, double value) {
     if (!key) return fail(EITHOT_EINVAL, "null key");
     eithot::Tuning& t = eithot::tuning();
     const std::string k(key);
-    if (k == "cta_bytes") {
-        if (value < 1024 || value > 232448) return fail(EITHOT_EINVAL, "cta_bytes out of range");
-        t.cta_bytes = static_cast<uint64_t>(value);
+    if (k == "dbuf") {
+        t.dbuf = value != 0.0 ? 1 : 0;
     } else if (k == "max_cluster") {
         const int v = static_cast<int>(value);
         if (v != 1 && v != 2 && v != 4 && v != 8 && v != 16) return fail(EITHOT_EINVAL, "max_cluster must be 1, 2, 4, 8 or 16");
@@ -104,7 +103,7 @@ int eithot_tune_get(const char* key, double* value) {
     if (!key || !value) return fail(EITHOT_EINVAL, "null argument");
     const eithot::Tuning& t = eithot::tuning();
     const std::string k(key);
-    if (k == "cta_bytes") *value = static_cast<double>(t.cta_bytes);
+    if (k == "dbuf") *value = t.dbuf;
     else if (k == "max_cluster") *value = t.max_cluster;
     else if (k == "variant") *value = t.variant;
     else return fail(EITHOT_EINVAL, "unknown tuning key " + k);

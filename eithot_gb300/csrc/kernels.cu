@@ -171,6 +171,7 @@ struct RowArgs {
     uint64_t items, E, row_bytes;
     uint32_t rows, cols, P, w, upw, last_upw, nstrips, buf_bytes;
     bool flat;  // w == E: a CTA's pieces are contiguous bytes
+    bool dbuf;  // two item buffers: the next item's loads overlap this item's write-back
     FastDiv div_strips, div_rows;
     FastDiv32 div_upw, div_P;
 };
@@ -230,14 +231,15 @@ __global__ void __launch_bounds__(kThreads) k_row_cluster(RowArgs a, Fn fn) {
     const uint32_t jn = min(a.cols, j0 + a.P);
     const uint32_t my_units = (jn > j0 ? jn - j0 : 0) * a.upw;
     cluster_sync_reuse();  // every CTA of the cluster is running before any DSMEM access
-    if (cid < a.items) row_stage_in<US, Fn, kScatter>(a, fn, peers, smem, 0, cid, j0, my_units);
+    if (a.dbuf && cid < a.items) row_stage_in<US, Fn, kScatter>(a, fn, peers, smem, 0, cid, j0, my_units);
     uint32_t k = 0;
     for (uint64_t it = cid; it < a.items; it += ncl, ++k) {
-        const uint32_t boff = (k & 1) * a.buf_bytes;
+        const uint32_t boff = a.dbuf ? (k & 1) * a.buf_bytes : 0;
+        if (!a.dbuf) row_stage_in<US, Fn, kScatter>(a, fn, peers, smem, 0, it, j0, my_units);
         if constexpr (US >= 4 && !kScatter) asm volatile("cp.async.wait_group 0;\n" ::: "memory");
         cluster_sync_publish();
         const uint64_t nxt = it + ncl;
-        if (nxt < a.items)
+        if (a.dbuf && nxt < a.items)
             row_stage_in<US, Fn, kScatter>(a, fn, peers, smem + (boff ^ a.buf_bytes), boff ^ a.buf_bytes, nxt, j0, my_units);
         uint64_t bi, s;
         a.div_strips.divmod(it, bi, s);
@@ -286,6 +288,7 @@ struct ColArgs {
     uint8_t* base;
     uint64_t items, E, row_bytes, mat_bytes;
     uint32_t rows, cols, tw, ntiles, pitch, Q, w, upw, last_upw, nstrips, RU, buf_bytes;  // RU = tw*upw
+    bool dbuf;
     FastDiv div_strips, div_tiles;
     FastDiv32 div_RU, div_upw, div_Q;
 };
@@ -356,14 +359,15 @@ __global__ void __launch_bounds__(kThreads) k_col_cluster(ColArgs a, Fn fn) {
         step = blockDim.x / a.RU;
     }
     cluster_sync_reuse();  // every CTA of the cluster is running before any DSMEM access
-    if (cid < a.items) col_stage_in<US, kLanes>(a, smem, cid, r0, myrows, lc, lu, ii0, step);
+    if (a.dbuf && cid < a.items) col_stage_in<US, kLanes>(a, smem, cid, r0, myrows, lc, lu, ii0, step);
     uint32_t k = 0;
     for (uint64_t it = cid; it < a.items; it += ncl, ++k) {
-        const uint32_t boff = (k & 1) * a.buf_bytes;
+        const uint32_t boff = a.dbuf ? (k & 1) * a.buf_bytes : 0;
+        if (!a.dbuf) col_stage_in<US, kLanes>(a, smem, it, r0, myrows, lc, lu, ii0, step);
         if constexpr (US >= 4) asm volatile("cp.async.wait_group 0;\n" ::: "memory");
         cluster_sync_publish();
         const uint64_t nxt = it + ncl;
-        if (nxt < a.items) col_stage_in<US, kLanes>(a, smem + (boff ^ a.buf_bytes), nxt, r0, myrows, lc, lu, ii0, step);
+        if (a.dbuf && nxt < a.items) col_stage_in<US, kLanes>(a, smem + (boff ^ a.buf_bytes), nxt, r0, myrows, lc, lu, ii0, step);
         const ColItem ci = col_item(a, it);
         if constexpr (kLanes) {
             if (lc < ci.tcols && lu < ci.lim) {
@@ -657,7 +661,7 @@ int launch_row_staged(uint8_t* data, const Pass& p, const Staging& st, ExecConte
 template <int US, typename FnOnChip, typename Fn64, bool kScatter>
 int launch_row(uint8_t* data, const Pass& p, const FnOnChip& fn, const Fn64& fn64, ExecContext& ctx) {
     const size_t cap = smem_cap_of(ctx.caps);
-    const Staging st = plan_row_staging(p.cols, p.elem, cap);
+    const Staging st = plan_row_staging(p.cols, p.elem, cap, kScatter);
     if (!st.on_chip) return launch_row_staged<US, Fn64, kScatter>(data, p, st, ctx, fn64);
     RowArgs a;
     a.base = data + p.offset;
@@ -677,7 +681,8 @@ int launch_row(uint8_t* data, const Pass& p, const FnOnChip& fn, const Fn64& fn6
     a.div_upw = FastDiv32::make(a.upw);
     a.div_P = FastDiv32::make(a.P);
     a.buf_bytes = static_cast<uint32_t>((static_cast<uint64_t>(a.P) * st.w + 127) / 128 * 128);
-    const size_t smem = 2 * static_cast<size_t>(a.buf_bytes);
+    a.dbuf = st.dbuf;
+    const size_t smem = (st.dbuf ? 2 : 1) * static_cast<size_t>(a.buf_bytes);
     EI_CHECK(launch_clusters(k_row_cluster<US, FnOnChip, kScatter>, st.K, smem, a.items, ctx, a, fn));
     EI_CHECK(cudaGetLastError());
     ctx.launches++;
@@ -776,7 +781,8 @@ int launch_col(uint8_t* data, const Pass& p, const FnOnChip& fn, const Fn64& fn6
     a.div_upw = FastDiv32::make(a.upw);
     a.div_Q = FastDiv32::make(a.Q);
     a.buf_bytes = static_cast<uint32_t>((static_cast<uint64_t>(a.Q) * st.pitch + 127) / 128 * 128);
-    const size_t smem = 2 * static_cast<size_t>(a.buf_bytes);
+    a.dbuf = st.dbuf;
+    const size_t smem = (st.dbuf ? 2 : 1) * static_cast<size_t>(a.buf_bytes);
     if (kThreads % a.RU == 0)
         EI_CHECK(launch_clusters(k_col_cluster<US, FnOnChip, true>, st.K, smem, a.items, ctx, a, fn));
     else
@@ -903,7 +909,7 @@ uint64_t pass_unit(const uint8_t* data, const Pass& p, size_t smem_cap) {
             return unit_for({addr, p.elem, p.strip, p.elem % p.strip == 0 ? p.strip : p.elem % p.strip});
         case kRowGather:
         case kRowScatter: {
-            const Staging st = plan_row_staging(p.cols, p.elem, smem_cap);
+            const Staging st = plan_row_staging(p.cols, p.elem, smem_cap, p.type == kRowScatter);
             return unit_for({addr, p.elem, st.w, p.elem % st.w == 0 ? st.w : p.elem % st.w});
         }
         case kColGather: {
@@ -924,7 +930,7 @@ size_t pass_workspace_bytes(const Pass& p, const DeviceCaps& caps) {
     switch (p.type) {
         case kRowGather:
         case kRowScatter: {
-            const Staging st = plan_row_staging(p.cols, p.elem, cap);
+            const Staging st = plan_row_staging(p.cols, p.elem, cap, p.type == kRowScatter);
             return st.on_chip ? 0 : p.cols * st.w;
         }
         case kColGather: {
@@ -948,7 +954,7 @@ size_t pass_workspace_ideal(const Pass& p, const DeviceCaps& caps) {
     switch (p.type) {
         case kRowGather:
         case kRowScatter: {
-            const Staging st = plan_row_staging(p.cols, p.elem, cap);
+            const Staging st = plan_row_staging(p.cols, p.elem, cap, p.type == kRowScatter);
             if (st.on_chip) return 0;
             const uint64_t ns = (p.elem + st.w - 1) / st.w;
             return p.batches * p.rows * ns * p.cols * st.w;

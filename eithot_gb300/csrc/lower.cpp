@@ -51,6 +51,23 @@ size_t slab_smem_bytes(uint64_t R, uint64_t C, uint64_t w) { return R * slab_pit
 
 namespace {
 constexpr int kClusterSizes[] = {1, 2, 4, 8, 16};
+
+int log2i(int K) {
+    int l = 0;
+    while ((1 << l) < K) ++l;
+    return l;
+}
+
+// Modelled slowdown of staging an item over K CTAs, per doubling of K, for
+// items moved in granules of g bytes through distributed shared memory
+// (measured on GB300: 128-byte pulls lose ~10-15% per doubling, 16-byte
+// pulls 40-70%, 16-byte pushes ~30%).
+double dsmem_penalty(uint64_t g, bool push) {
+    if (g >= 128) return 0.12;
+    if (g >= 64) return 0.2;
+    if (g >= 32) return 0.3;
+    return push ? 0.35 : 0.7;
+}
 }  // namespace
 
 Tuning& tuning() {
@@ -58,19 +75,31 @@ Tuning& tuning() {
     return t;
 }
 
-Staging plan_row_staging(uint64_t cols, uint64_t E, size_t cap) {
+Staging plan_row_staging(uint64_t cols, uint64_t E, size_t cap, bool scatter) {
     Staging s;
     const uint64_t w0 = strip_width(E);
-    // Per-CTA staging target (one of the two item buffers); by default three
-    // CTAs with double buffers fit one SM.
-    for (uint64_t limit : {tuning().cta_bytes, static_cast<uint64_t>(cap / 2)}) {
+    for (uint64_t w : {w0, uint64_t(64), uint64_t(32)}) {
+        if (w > w0 || w < std::min<uint64_t>(E, 32)) continue;
+        // a whole row strip in one CTA
+        if (cols * w <= cap) {
+            s.w = w; s.K = 1; s.per_cta = cols * w; s.item_bytes = cols * w;
+            s.on_chip = true; s.dbuf = false;
+            s.cost = 1.0 + (w < E ? 0.05 : 0.0);
+            return s;
+        }
+    }
+    for (bool db : {true, false}) {
+        if (db && !tuning().dbuf) continue;
+        const uint64_t limit = db ? cap / 2 : cap;
         for (uint64_t w : {w0, uint64_t(64), uint64_t(32)}) {
             if (w > w0 || w < std::min<uint64_t>(E, 32)) continue;
             for (int K : kClusterSizes) {
                 if (K > tuning().max_cluster) break;
                 const uint64_t per = (cols + K - 1) / K * w;
                 if (per <= limit) {
-                    s.w = w; s.K = K; s.per_cta = per; s.item_bytes = cols * w; s.on_chip = true;
+                    s.w = w; s.K = K; s.per_cta = per; s.item_bytes = cols * w;
+                    s.on_chip = true; s.dbuf = db;
+                    s.cost = 1.0 + dsmem_penalty(w, scatter) * log2i(K);
                     return s;
                 }
             }
@@ -81,26 +110,30 @@ Staging plan_row_staging(uint64_t cols, uint64_t E, size_t cap) {
     s.item_bytes = cols * w0;
     s.per_cta = s.item_bytes;
     s.on_chip = false;
+    s.cost = 2.5;
     return s;
 }
 
 Staging plan_col_staging(uint64_t rows, uint64_t E, size_t cap) {
     Staging s;
-    for (uint64_t limit : {tuning().cta_bytes, static_cast<uint64_t>(cap / 2)}) {
-        for (uint64_t tb : {uint64_t(128), uint64_t(64), uint64_t(32)}) {
-            uint64_t w, tw;
-            if (E <= tb) { w = E; tw = std::max<uint64_t>(1, tb / E); }
-            else { w = tb; tw = 1; }
-            // tw*w contiguous bytes per staged row: a quarter-warp of 16-byte
-            // reads (or a warp of 4-byte reads) covers one row piece, so the
-            // row pitch needs no bank padding
-            const uint64_t pitch = tw * w;
+    for (uint64_t tb : {uint64_t(128), uint64_t(64), uint64_t(32)}) {
+        uint64_t w, tw;
+        if (E <= tb) { w = E; tw = std::max<uint64_t>(1, tb / E); }
+        else { w = tb; tw = 1; }
+        // tw*w contiguous bytes per staged row: a quarter-warp of 16-byte
+        // reads (or a warp of 4-byte reads) covers one row piece, so the row
+        // pitch needs no bank padding
+        const uint64_t pitch = tw * w;
+        for (bool db : {true, false}) {
+            if (db && !tuning().dbuf) continue;
+            const uint64_t limit = db ? cap / 2 : cap;
             for (int K : kClusterSizes) {
                 if (K > tuning().max_cluster) break;
                 const uint64_t per = (rows + K - 1) / K * pitch;
                 if (per <= limit) {
                     s.w = w; s.tw = tw; s.pitch = pitch; s.K = K; s.per_cta = per;
-                    s.item_bytes = rows * pitch; s.on_chip = true;
+                    s.item_bytes = rows * pitch; s.on_chip = true; s.dbuf = db && K > 1;
+                    s.cost = 1.0 + dsmem_penalty(pitch, false) * log2i(K) + (tb < 128 ? 0.1 : 0.0);
                     return s;
                 }
             }
@@ -114,6 +147,7 @@ Staging plan_col_staging(uint64_t rows, uint64_t E, size_t cap) {
     s.item_bytes = rows * s.pitch;
     s.per_cta = s.item_bytes;
     s.on_chip = false;
+    s.cost = 2.5;
     return s;
 }
 
@@ -135,11 +169,11 @@ Xpose xpose_of(const LowOp& op, uint64_t elem, uint64_t n_sub, uint64_t base_off
 
 namespace {
 
-double row_cost(uint64_t cols, uint64_t E, size_t cap) {
-    return plan_row_staging(cols, E, cap).on_chip ? 1.0 : 2.0;
+double row_cost(uint64_t cols, uint64_t E, size_t cap, bool scatter) {
+    return plan_row_staging(cols, E, cap, scatter).cost;
 }
 double col_cost(uint64_t rows, uint64_t E, size_t cap) {
-    return plan_col_staging(rows, E, cap).on_chip ? 1.0 : 2.0;
+    return plan_col_staging(rows, E, cap).cost;
 }
 
 std::string geom(const char* name, uint64_t B, uint64_t r, uint64_t c, uint64_t E) {
@@ -170,8 +204,8 @@ void lower_xpose(const Xpose& x, const DeviceCaps& caps, std::vector<Pass>* pass
     // Catanzaro: c2r on the R x C view, or r2c on the C x R view.
     uint64_t g, inv;
     gcd_inverse(x.R, x.C, &g, &inv);
-    const double c2r = (g > 1 ? col_cost(x.R, x.E, cap) : 0.0) + row_cost(x.C, x.E, cap) + col_cost(x.R, x.E, cap);
-    const double r2c = col_cost(x.C, x.E, cap) + row_cost(x.R, x.E, cap) + (g > 1 ? col_cost(x.C, x.E, cap) : 0.0);
+    const double c2r = (g > 1 ? col_cost(x.R, x.E, cap) : 0.0) + row_cost(x.C, x.E, cap, false) + col_cost(x.R, x.E, cap);
+    const double r2c = col_cost(x.C, x.E, cap) + row_cost(x.R, x.E, cap, true) + (g > 1 ? col_cost(x.C, x.E, cap) : 0.0);
     bool use_c2r = (c2r < r2c) || (c2r == r2c && x.C >= x.R);
     if (tuning().variant == 1) use_c2r = true;
     if (tuning().variant == 2) use_c2r = false;

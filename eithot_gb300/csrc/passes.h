@@ -66,9 +66,9 @@ size_t smem_cap_of(const DeviceCaps& caps);
 // Process-wide tuning of the lowering (set through eithot_tune_set; the
 // autotuner fills these per shape).
 struct Tuning {
-    uint64_t cta_bytes = 36 * 1024;  // target bytes one CTA stages per item buffer
-    int max_cluster = 16;            // largest thread-block cluster used
-    int variant = 0;                 // 0: cost model, 1: force c2r, 2: force r2c
+    int max_cluster = 16;  // largest thread-block cluster used
+    int variant = 0;       // 0: cost model, 1: force c2r, 2: force r2c
+    int dbuf = 1;          // allow double-buffered cluster items
 };
 Tuning& tuning();
 
@@ -83,11 +83,15 @@ struct Staging {
     uint64_t pitch = 0;    // bytes per staged row (column passes)
     uint64_t item_bytes = 0;
     int K = 1;             // CTAs of the thread-block cluster sharing one item
-    uint64_t per_cta = 0;  // shared-memory bytes each CTA stages
+    uint64_t per_cta = 0;  // shared-memory bytes each CTA stages per item
+    bool dbuf = false;     // two item buffers per CTA (next item's loads overlap)
     bool on_chip = false;  // the item fits the cluster's distributed shared memory
+    double cost = 0;       // modelled time in units of one streaming pass
 };
 
-Staging plan_row_staging(uint64_t cols, uint64_t E, size_t smem_cap);
+// scatter: the row pass pushes elements to their destinations (r2c);
+// otherwise it pulls them (c2r).
+Staging plan_row_staging(uint64_t cols, uint64_t E, size_t smem_cap, bool scatter = false);
 Staging plan_col_staging(uint64_t rows, uint64_t E, size_t smem_cap);
 
 // Lowers every step of `plan` for element size `elem` into passes.

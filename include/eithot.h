@@ -145,7 +145,7 @@ int eithot_estimate(int rank, const int64_t* dims, const int* perm_1based,
 /* ---- tuning ----------------------------------------------------------------
  * No reference counterpart (the reference fixes its kernel choices at
  * compile time).  Process-wide knobs of the lowering, used by the autotuner:
- *   "cta_bytes"   bytes one CTA stages per item buffer (1024 .. 232448)
+ *   "dbuf"        1 allow double-buffered cluster items, 0 single buffer
  *   "max_cluster" largest thread-block cluster (1, 2, 4, 8, 16)
  *   "variant"     0 cost model, 1 force c2r, 2 force r2c for 2D transposes */
 int eithot_tune_set(const char* key, double value);
