@@ -188,18 +188,33 @@ __device__ __forceinline__ void row_stage_in(const RowArgs& a, const Fn& fn, uin
     const uint32_t lim = (s + 1 == a.nstrips) ? a.last_upw : a.upw;
     const uint8_t* row = a.base + bi * a.row_bytes + s * a.w;
     if constexpr (kScatter) {
+        // kLoadBatch global loads in flight per thread before the pushes
+        constexpr int kLoadBatch = US >= 8 ? 4 : 8;
         const I i = static_cast<I>(a.div_rows.mod(bi));
-        for (uint32_t x = threadIdx.x; x < my_units; x += blockDim.x) {
-            uint32_t jj, u;
-            a.div_upw.divmod(x, jj, u);
-            if (u >= lim) continue;
-            const uint32_t j = j0 + jj;
-            const U v = *reinterpret_cast<const U*>(row + static_cast<uint64_t>(j) * a.E + u * US);
-            const I dst = fn(i, static_cast<I>(j));
-            if (!in_range(dst, a.cols)) continue;
-            uint32_t owner, off;
-            a.div_P.divmod(static_cast<uint32_t>(dst), owner, off);
-            *reinterpret_cast<U*>(peers[owner] + boff + off * a.w + u * US) = v;
+        for (uint32_t x0 = threadIdx.x; x0 < my_units; x0 += kLoadBatch * blockDim.x) {
+            U v[kLoadBatch];
+            uint32_t jq[kLoadBatch], uq[kLoadBatch];
+            bool ok[kLoadBatch];
+#pragma unroll
+            for (int q = 0; q < kLoadBatch; ++q) {
+                const uint32_t x = x0 + q * blockDim.x;
+                ok[q] = false;
+                if (x >= my_units) continue;
+                a.div_upw.divmod(x, jq[q], uq[q]);
+                if (uq[q] >= lim) continue;
+                jq[q] += j0;
+                v[q] = *reinterpret_cast<const U*>(row + static_cast<uint64_t>(jq[q]) * a.E + uq[q] * US);
+                ok[q] = true;
+            }
+#pragma unroll
+            for (int q = 0; q < kLoadBatch; ++q) {
+                if (!ok[q]) continue;
+                const I dst = fn(i, static_cast<I>(jq[q]));
+                if (!in_range(dst, a.cols)) continue;
+                uint32_t owner, off;
+                a.div_P.divmod(static_cast<uint32_t>(dst), owner, off);
+                *reinterpret_cast<U*>(peers[owner] + boff + off * a.w + uq[q] * US) = v[q];
+            }
         }
     } else if (a.flat) {
         const uint8_t* src = row + static_cast<uint64_t>(j0) * a.E;
