@@ -40,6 +40,17 @@ inline FnRowShuffleT<I> make_rowshuffle(const Pass& p) {
     return f;
 }
 template <typename I>
+inline FnRowShuffleInvT<I> make_rowshuffle_inv(const Pass& p) {
+    FnRowShuffleInvT<I> f;
+    f.m = static_cast<I>(p.m);
+    f.n = static_cast<I>(p.n);
+    f.divb = MakeDiv<I>::make(p.b, p.n);
+    f.divm = MakeDiv<I>::make(p.m, p.n / std::max<uint64_t>(p.b, 1) + p.m);
+    f.divn = MakeDiv<I>::make(p.n, p.m + p.n * p.m);
+    return f;
+}
+
+template <typename I>
 inline FnC2RPreRotT<I> make_prerot(const Pass& p) {
     FnC2RPreRotT<I> f;
     f.m = static_cast<I>(p.m);

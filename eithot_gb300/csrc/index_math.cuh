@@ -155,6 +155,22 @@ struct FnRowShuffleT {
     }
 };
 
+// Inverse of the row shuffle (EITHOT's otherwise unused r2c::row_shuffle,
+// ITNT/src/equations.h:440-464): j -> ((j/b + i) mod m + j*m) mod n.  A
+// gather with this map equals a scatter with FnRowShuffleT and vice versa,
+// so either row pass can be run in whichever direction stages better.
+template <typename I>
+struct FnRowShuffleInvT {
+    using index_type = I;
+    I m, n;
+    typename DivOf<I>::T divb, divm, divn;
+    EI_HD I operator()(I i, I j) const {
+        I r = divb.div(j) + i;
+        if (r >= m) r = divm.mod(r);
+        return divn.mod(r + j * m);
+    }
+};
+
 // c2r column shuffle (col gather): row i of column j takes
 // (i*n - floor(i*c/m) + j) mod m.
 template <typename I>

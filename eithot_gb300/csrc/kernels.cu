@@ -887,15 +887,37 @@ int run_pass_u(uint8_t* data, const Pass& p, ExecContext& ctx) {
         case kSlabTranspose: return launch_slab<US>(data, p, ctx);
         case kRowGather:
         case kRowScatter: {
+            // A row pass is run as a gather when one CTA holds the whole row
+            // (cp.async loads, local gathers) or when it moves wide granules;
+            // otherwise as a scatter (remote pushes beat remote pulls for
+            // 16-32 byte granules).  The inverse map turns one into the other.
+            const Staging st = plan_row_staging(p.cols, p.elem, smem_cap_of(ctx.caps), p.type == kRowScatter);
+            const bool gather = !st.on_chip || st.K == 1 || st.w >= 64;
+            const bool use_inverse = gather == (p.type == kRowScatter);
+            if (!st.on_chip) {  // staged: keep the pass's own direction
+                const FnRowShuffleT<uint64_t> f64 = make_rowshuffle<uint64_t>(p);
+                return p.type == kRowScatter
+                           ? launch_row<US, FnRowShuffleT<uint64_t>, FnRowShuffleT<uint64_t>, true>(data, p, f64, f64, ctx)
+                           : launch_row<US, FnRowShuffleT<uint64_t>, FnRowShuffleT<uint64_t>, false>(data, p, f64, f64, ctx);
+            }
+            if (use_inverse) {
+                const FnRowShuffleInvT<uint64_t> h64 = make_rowshuffle_inv<uint64_t>(p);
+                if (fits32(p)) {
+                    const FnRowShuffleInvT<uint32_t> h32 = make_rowshuffle_inv<uint32_t>(p);
+                    return gather ? launch_row<US, FnRowShuffleInvT<uint32_t>, FnRowShuffleInvT<uint64_t>, false>(data, p, h32, h64, ctx)
+                                  : launch_row<US, FnRowShuffleInvT<uint32_t>, FnRowShuffleInvT<uint64_t>, true>(data, p, h32, h64, ctx);
+                }
+                return gather ? launch_row<US, FnRowShuffleInvT<uint64_t>, FnRowShuffleInvT<uint64_t>, false>(data, p, h64, h64, ctx)
+                              : launch_row<US, FnRowShuffleInvT<uint64_t>, FnRowShuffleInvT<uint64_t>, true>(data, p, h64, h64, ctx);
+            }
             const FnRowShuffleT<uint64_t> f64 = make_rowshuffle<uint64_t>(p);
-            const bool sc = p.type == kRowScatter;
             if (fits32(p)) {
                 const FnRowShuffleT<uint32_t> f32 = make_rowshuffle<uint32_t>(p);
-                return sc ? launch_row<US, FnRowShuffleT<uint32_t>, FnRowShuffleT<uint64_t>, true>(data, p, f32, f64, ctx)
-                          : launch_row<US, FnRowShuffleT<uint32_t>, FnRowShuffleT<uint64_t>, false>(data, p, f32, f64, ctx);
+                return gather ? launch_row<US, FnRowShuffleT<uint32_t>, FnRowShuffleT<uint64_t>, false>(data, p, f32, f64, ctx)
+                              : launch_row<US, FnRowShuffleT<uint32_t>, FnRowShuffleT<uint64_t>, true>(data, p, f32, f64, ctx);
             }
-            return sc ? launch_row<US, FnRowShuffleT<uint64_t>, FnRowShuffleT<uint64_t>, true>(data, p, f64, f64, ctx)
-                      : launch_row<US, FnRowShuffleT<uint64_t>, FnRowShuffleT<uint64_t>, false>(data, p, f64, f64, ctx);
+            return gather ? launch_row<US, FnRowShuffleT<uint64_t>, FnRowShuffleT<uint64_t>, false>(data, p, f64, f64, ctx)
+                          : launch_row<US, FnRowShuffleT<uint64_t>, FnRowShuffleT<uint64_t>, true>(data, p, f64, f64, ctx);
         }
         case kColGather:
             switch (p.fn) {

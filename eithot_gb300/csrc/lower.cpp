@@ -75,7 +75,16 @@ Tuning& tuning() {
     return t;
 }
 
+namespace {
+// A CTA footprint at most this large lets two CTAs share an SM (GB300:
+// 228 KB of shared memory per SM); clusters of CTAs that each fill an SM
+// leave SMs unused when whole clusters no longer fit a GPC.
+constexpr uint64_t kTwoPerSm = 110 * 1024;
+constexpr double kOnePerSmPenalty = 0.25;
+}  // namespace
+
 Staging plan_row_staging(uint64_t cols, uint64_t E, size_t cap, bool scatter) {
+    (void)scatter;
     Staging s;
     const uint64_t w0 = strip_width(E);
     for (uint64_t w : {w0, uint64_t(64), uint64_t(32)}) {
@@ -88,18 +97,22 @@ Staging plan_row_staging(uint64_t cols, uint64_t E, size_t cap, bool scatter) {
             return s;
         }
     }
-    for (bool db : {true, false}) {
-        if (db && !tuning().dbuf) continue;
-        const uint64_t limit = db ? cap / 2 : cap;
+    for (uint64_t occ_limit : {kTwoPerSm, static_cast<uint64_t>(cap)}) {
         for (uint64_t w : {w0, uint64_t(64), uint64_t(32)}) {
             if (w > w0 || w < std::min<uint64_t>(E, 32)) continue;
             for (int K : kClusterSizes) {
                 if (K > tuning().max_cluster) break;
                 const uint64_t per = (cols + K - 1) / K * w;
-                if (per <= limit) {
+                for (bool db : {true, false}) {
+                    if (db && !tuning().dbuf) continue;
+                    const uint64_t foot = per * (db ? 2 : 1);
+                    if (foot > cap || foot > occ_limit) continue;
                     s.w = w; s.K = K; s.per_cta = per; s.item_bytes = cols * w;
                     s.on_chip = true; s.dbuf = db;
-                    s.cost = 1.0 + dsmem_penalty(w, scatter) * log2i(K);
+                    // 16-32 byte granules are pushed whatever the pass's own
+                    // direction (the inverse map turns a gather into a scatter)
+                    s.cost = 1.0 + dsmem_penalty(w, true) * log2i(K) + (db ? 0.0 : 0.1) +
+                             (foot > kTwoPerSm ? kOnePerSmPenalty : 0.0);
                     return s;
                 }
             }
@@ -116,24 +129,26 @@ Staging plan_row_staging(uint64_t cols, uint64_t E, size_t cap, bool scatter) {
 
 Staging plan_col_staging(uint64_t rows, uint64_t E, size_t cap) {
     Staging s;
-    for (uint64_t tb : {uint64_t(128), uint64_t(64), uint64_t(32)}) {
-        uint64_t w, tw;
-        if (E <= tb) { w = E; tw = std::max<uint64_t>(1, tb / E); }
-        else { w = tb; tw = 1; }
-        // tw*w contiguous bytes per staged row: a quarter-warp of 16-byte
-        // reads (or a warp of 4-byte reads) covers one row piece, so the row
-        // pitch needs no bank padding
-        const uint64_t pitch = tw * w;
-        for (bool db : {true, false}) {
-            if (db && !tuning().dbuf) continue;
-            const uint64_t limit = db ? cap / 2 : cap;
+    for (uint64_t occ_limit : {kTwoPerSm, static_cast<uint64_t>(cap)}) {
+        for (uint64_t tb : {uint64_t(128), uint64_t(64), uint64_t(32)}) {
+            uint64_t w, tw;
+            if (E <= tb) { w = E; tw = std::max<uint64_t>(1, tb / E); }
+            else { w = tb; tw = 1; }
+            // tw*w contiguous bytes per staged row: a quarter-warp of 16-byte
+            // reads (or a warp of 4-byte reads) covers one row piece, so the
+            // row pitch needs no bank padding
+            const uint64_t pitch = tw * w;
             for (int K : kClusterSizes) {
                 if (K > tuning().max_cluster) break;
                 const uint64_t per = (rows + K - 1) / K * pitch;
-                if (per <= limit) {
+                for (bool db : {true, false}) {
+                    if (db && (!tuning().dbuf || K == 1)) continue;
+                    const uint64_t foot = per * (db ? 2 : 1);
+                    if (foot > cap || foot > occ_limit) continue;
                     s.w = w; s.tw = tw; s.pitch = pitch; s.K = K; s.per_cta = per;
-                    s.item_bytes = rows * pitch; s.on_chip = true; s.dbuf = db && K > 1;
-                    s.cost = 1.0 + dsmem_penalty(pitch, false) * log2i(K) + (tb < 128 ? 0.1 : 0.0);
+                    s.item_bytes = rows * pitch; s.on_chip = true; s.dbuf = db;
+                    s.cost = 1.0 + dsmem_penalty(pitch, false) * log2i(K) + (tb < 128 ? 0.1 : 0.0) +
+                             (foot > kTwoPerSm ? kOnePerSmPenalty : 0.0);
                     return s;
                 }
             }

@@ -152,4 +152,34 @@ long hs_check_fn32(int rank, const int64_t* dims, const int* perm, size_t elem, 
     return bad;
 }
 
+// For every row pass of the plan, checks that the inverse map undoes the
+// row shuffle (both flavours) on all (i, j) when m*n <= max_full, else a
+// strided sample.  Returns the number of failures (or -1 on error).
+long hs_check_inverse(int rank, const int64_t* dims, const int* perm, size_t elem, int nb, double alpha,
+                      int order, long max_full) {
+    NdPlan plan;
+    if (!make_nd_plan(rank, dims, perm, nb, alpha, order, &plan, &g_err)) return -1;
+    std::vector<Pass> passes;
+    DeviceCaps caps;
+    if (!lower_plan(plan, elem, caps, &passes, &g_err)) return -1;
+    long bad = 0;
+    for (const Pass& p : passes) {
+        if (p.type != kRowGather && p.type != kRowScatter) continue;
+        const auto f = make_rowshuffle<uint64_t>(p);
+        const auto h = make_rowshuffle_inv<uint64_t>(p);
+        const bool f32ok = fits32(p);
+        const uint64_t total = p.m * p.n;
+        const uint64_t stride = total <= static_cast<uint64_t>(max_full) ? 1 : total / max_full + 1;
+        for (uint64_t x = 0; x < total; x += stride) {
+            const uint64_t i = x / p.n, j = x % p.n;
+            if (f(i, h(i, j)) != j || h(i, f(i, j)) != j) ++bad;
+            if (f32ok) {
+                const auto h32 = make_rowshuffle_inv<uint32_t>(p);
+                if (h32(static_cast<uint32_t>(i), static_cast<uint32_t>(j)) != h(i, j)) ++bad;
+            }
+        }
+    }
+    return bad;
+}
+
 }  // extern "C"

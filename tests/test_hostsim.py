@@ -72,3 +72,18 @@ def test_32bit_maps_agree_with_64bit(hostsim, dims, perm, elem):
     bad = hostsim.hs_check_fn32(r, (ctypes.c_int64 * r)(*dims), (ctypes.c_int * r)(*perm), elem, 1, 0.01, 0,
                                 2000000)
     assert bad == 0
+
+
+@pytest.mark.parametrize("dims,perm,elem", [
+    ([4, 20011, 8192, 2], [1, 3, 2, 4], 4), ([3001, 4096], [2, 1], 4), ([2048, 1536], [2, 1], 4),
+    ([1000, 999], [2, 1], 2), ([60000, 300], [2, 1], 4), ([64, 8000], [2, 1], 8), ([6, 4, 3401], [3, 2, 1], 2)])
+def test_row_shuffle_inverse(hostsim, dims, perm, elem):
+    """EITHOT's r2c::row_shuffle map inverts the row shuffle, so the executor
+    may run a row pass as a gather or as a scatter."""
+    import ctypes
+    r = len(dims)
+    hostsim.hs_check_inverse.restype = ctypes.c_long
+    hostsim.hs_check_inverse.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int),
+                                         ctypes.c_size_t, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_long]
+    assert hostsim.hs_check_inverse(r, (ctypes.c_int64 * r)(*dims), (ctypes.c_int * r)(*perm), elem, 1, 0.01, 0,
+                                    2000000) == 0
