@@ -288,6 +288,65 @@ int eithot_transpose_ex(void* d_data, size_t capacity_bytes, int rank, const int
     return EITHOT_OK;
 }
 
+// The no-allocation variant: scratch comes from the library's fixed device
+// array instead of cudaMallocAsync.  For callers that may not allocate
+// device memory during the call: their device memory is owned by another
+// allocator (a framework's caching pool that has reserved the free HBM, so an
+// extra allocation would fail or fragment it), or the call sits on a path
+// that must not pay for an allocation.  The first call on each device looks
+// up the array's device address (cudaGetSymbolAddress); make that first call
+// before any stream capture.  All calls share the array and it keeps the
+// last call's contents; nothing in it needs to start at zero.  Calls whose
+// device work overlaps (other streams, other host threads) race on it.
+int eithot_transpose_noalloc(void* d_data, size_t capacity_bytes, int rank, const int64_t* dims,
+                             const int* perm_1based, size_t elem_size, int num_sub_tensors,
+                             double alpha, void* stream) {
+    std::memset(&g_stats, 0, sizeof(g_stats));
+    if (!d_data) return fail(EITHOT_EINVAL, "null data pointer");
+    eithot::DeviceCaps caps;
+    int rc = device_caps(&caps);
+    if (rc) return rc;
+    {
+        cudaPointerAttributes attr;
+        cudaError_t e = cudaPointerGetAttributes(&attr, d_data);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(EITHOT_EINVAL, std::string("data pointer: ") + cudaGetErrorString(e));
+        }
+        if (attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged)
+            return fail(EITHOT_EINVAL, "data must be device or managed memory");
+    }
+    eithot::NdPlan plan;
+    std::vector<eithot::Pass> passes;
+    rc = build(rank, dims, perm_1based, elem_size, num_sub_tensors, alpha, EITHOT_ORDER_MIXED, caps, &plan,
+               &passes);
+    if (rc) return rc;
+    if (static_cast<double>(plan.padded_volume) * static_cast<double>(elem_size) > static_cast<double>(capacity_bytes))
+        return fail(EITHOT_EINVAL, "buffer capacity is smaller than the (padded) tensor");
+    size_t need = 0;
+    for (const auto& p : passes) need = std::max(need, eithot::pass_workspace_bytes(p, caps));
+    if (need > eithot::kNoAllocScratchBytes)
+        return fail(EITHOT_EINVAL, "this transpose needs " + std::to_string(need) +
+                                       " bytes of scratch, more than the fixed " +
+                                       std::to_string(eithot::kNoAllocScratchBytes) +
+                                       " bytes of eithot_transpose_noalloc; use eithot_transpose_ex");
+    eithot::ExecContext ctx;
+    ctx.caps = caps;
+    ctx.stream = static_cast<cudaStream_t>(stream);
+    if (need > 0) {
+        std::string err;
+        if ((rc = eithot::noalloc_scratch(&ctx.scratch, &err))) return fail(rc, err);
+        ctx.scratch_bytes = eithot::kNoAllocScratchBytes;
+    }
+    g_stats.algorithmic_bytes = 2.0 * static_cast<double>(plan.volume) * static_cast<double>(elem_size);
+    g_stats.workspace_bytes = ctx.scratch_bytes;
+    rc = eithot::run_passes(static_cast<uint8_t*>(d_data), passes, ctx);
+    g_stats.n_passes = ctx.passes;
+    g_stats.n_launches = ctx.launches;
+    if (rc) return fail(rc, ctx.err);
+    return EITHOT_OK;
+}
+
 int eithot_transpose(void* d_data, size_t capacity_bytes, int rank, const int64_t* dims,
                      const int* perm_1based, size_t elem_size, int num_sub_tensors, double alpha,
                      void* stream) {

@@ -51,6 +51,13 @@ int run_passes(uint8_t* data, const std::vector<Pass>& passes, ExecContext& ctx)
 
 bool query_caps(int device, DeviceCaps* caps, std::string* err);
 
+// Size of the fixed device scratch behind eithot_transpose_noalloc.
+constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;
+
+// Device address of that scratch on the current device (looked up on the
+// first call per device).
+int noalloc_scratch(uint8_t** ptr, std::string* err);
+
 // Count of index-map results that fell outside their row/column since the
 // last read (the kernels skip such accesses).  Synchronises the device.
 int read_index_faults(unsigned int* out);

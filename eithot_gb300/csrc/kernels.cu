@@ -1054,6 +1054,40 @@ int run_passes(uint8_t* data, const std::vector<Pass>& passes, ExecContext& ctx)
     return 0;
 }
 
+// Fixed scratch for eithot_transpose_noalloc: a file-scope device array, so
+// the entry point never allocates.  Every GPU that loads the library holds
+// these bytes until the process exits; all calls share them.
+static __device__ __align__(256) uint8_t g_noalloc_scratch[kNoAllocScratchBytes];
+
+int noalloc_scratch(uint8_t** ptr, std::string* err) {
+    // In host code g_noalloc_scratch names a host-side stand-in; its device
+    // address is looked up once per device, with that device current.
+    static std::mutex mu;
+    static std::vector<std::pair<int, uint8_t*>> cache;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        *err = std::string("cudaGetDevice: ") + cudaGetErrorString(e);
+        return EITHOT_STATUS_CUDA;
+    }
+    std::lock_guard<std::mutex> lock(mu);
+    for (auto& c : cache) {
+        if (c.first == dev) {
+            *ptr = c.second;
+            return 0;
+        }
+    }
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+        *err = std::string("cudaGetSymbolAddress(fixed scratch): ") + cudaGetErrorString(e);
+        return EITHOT_STATUS_CUDA;
+    }
+    cache.emplace_back(dev, static_cast<uint8_t*>(p));
+    *ptr = static_cast<uint8_t*>(p);
+    return 0;
+}
+
 int read_index_faults(unsigned int* out) {
     unsigned int v = 0, zero = 0;
     cudaError_t e = cudaMemcpyFromSymbol(&v, g_index_faults, sizeof(v));

@@ -121,6 +121,21 @@ int eithot_transpose_ex(void* d_data, size_t capacity_bytes, int rank,
                         int reorder_type, void* d_workspace,
                         size_t workspace_bytes, void* stream);
 
+/* No counterpart in the reference (whose kernels allocate managed temporaries
+ * per pass).  As eithot_transpose, but it allocates nothing: the scratch the
+ * staged passes and the padding moves need comes from a fixed 32 MiB device
+ * array inside the library, which every GPU that loads the library holds
+ * until the process exits.  For callers that may not allocate device memory
+ * during the call, e.g. because another allocator owns the device's memory.
+ * Requests needing more than 32 MiB of scratch fail with EITHOT_EINVAL.  The
+ * first call on a device looks up the array's address; make it before any
+ * stream capture.  Calls share the array: calls whose device work overlaps
+ * race on it. */
+int eithot_transpose_noalloc(void* d_data, size_t capacity_bytes, int rank,
+                             const int64_t* dims, const int* perm_1based,
+                             size_t elem_size, int num_sub_tensors, double alpha,
+                             void* stream);
+
 /* Device scratch bytes eithot_transpose_ex needs for this request. */
 int eithot_workspace_size(int rank, const int64_t* dims, const int* perm_1based,
                           size_t elem_size, int num_sub_tensors, double alpha,
