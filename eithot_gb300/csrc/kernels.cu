@@ -352,7 +352,7 @@ __device__ __forceinline__ void col_stage_in(const ColArgs& a, uint8_t* buf, uin
     if constexpr (US >= 4) asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
 
-template <int US, typename Fn, bool kLanes>
+template <int US, typename Fn, bool kLanes, int kB>
 __global__ void __launch_bounds__(kThreads) k_col_cluster(ColArgs a, Fn fn) {
     using U = typename UnitOf<US>::T;
     using I = typename Fn::index_type;
@@ -390,11 +390,11 @@ __global__ void __launch_bounds__(kThreads) k_col_cluster(ColArgs a, Fn fn) {
                 uint8_t* g = ci.mat + static_cast<uint64_t>(r0 + ii0) * a.row_bytes + static_cast<uint64_t>(lc) * a.E + lu * US;
                 const uint32_t soff = boff + lc * a.w + lu * US;
                 const I col = static_cast<I>(ci.col0 + lc);
-                for (uint32_t ii = ii0; ii < myrows; ii += kBatch * step, g += kBatch * gstep) {
-                    U v[kBatch];
-                    bool ok[kBatch];
+                for (uint32_t ii = ii0; ii < myrows; ii += kB * step, g += kB * gstep) {
+                    U v[kB];
+                    bool ok[kB];
 #pragma unroll
-                    for (int q = 0; q < kBatch; ++q) {
+                    for (int q = 0; q < kB; ++q) {
                         const uint32_t iq = ii + q * step;
                         ok[q] = false;
                         if (iq >= myrows) continue;
@@ -406,7 +406,7 @@ __global__ void __launch_bounds__(kThreads) k_col_cluster(ColArgs a, Fn fn) {
                         ok[q] = true;
                     }
 #pragma unroll
-                    for (int q = 0; q < kBatch; ++q)
+                    for (int q = 0; q < kB; ++q)
                         if (ok[q]) *reinterpret_cast<U*>(g + q * gstep) = v[q];
                 }
             }
@@ -798,10 +798,12 @@ int launch_col(uint8_t* data, const Pass& p, const FnOnChip& fn, const Fn64& fn6
     a.buf_bytes = static_cast<uint32_t>((static_cast<uint64_t>(a.Q) * st.pitch + 127) / 128 * 128);
     a.dbuf = st.dbuf;
     const size_t smem = (st.dbuf ? 2 : 1) * static_cast<size_t>(a.buf_bytes);
-    if (kThreads % a.RU == 0)
-        EI_CHECK(launch_clusters(k_col_cluster<US, FnOnChip, true>, st.K, smem, a.items, ctx, a, fn));
+    if (kThreads % a.RU != 0)
+        EI_CHECK(launch_clusters(k_col_cluster<US, FnOnChip, false, 4>, st.K, smem, a.items, ctx, a, fn));
+    else if (tuning().col_batch >= 8)
+        EI_CHECK(launch_clusters(k_col_cluster<US, FnOnChip, true, 8>, st.K, smem, a.items, ctx, a, fn));
     else
-        EI_CHECK(launch_clusters(k_col_cluster<US, FnOnChip, false>, st.K, smem, a.items, ctx, a, fn));
+        EI_CHECK(launch_clusters(k_col_cluster<US, FnOnChip, true, 4>, st.K, smem, a.items, ctx, a, fn));
     EI_CHECK(cudaGetLastError());
     ctx.launches++;
     return 0;

@@ -131,6 +131,7 @@ Staging plan_col_staging(uint64_t rows, uint64_t E, size_t cap) {
     Staging s;
     for (uint64_t occ_limit : {kTwoPerSm, static_cast<uint64_t>(cap)}) {
         for (uint64_t tb : {uint64_t(128), uint64_t(64), uint64_t(32)}) {
+            if (tuning().col_chunk && tb != static_cast<uint64_t>(tuning().col_chunk)) continue;
             uint64_t w, tw;
             if (E <= tb) { w = E; tw = std::max<uint64_t>(1, tb / E); }
             else { w = tb; tw = 1; }

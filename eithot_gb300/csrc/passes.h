@@ -69,6 +69,8 @@ struct Tuning {
     int max_cluster = 16;  // largest thread-block cluster used
     int variant = 0;       // 0: cost model, 1: force c2r, 2: force r2c
     int dbuf = 1;          // allow double-buffered cluster items
+    int col_batch = 4;     // remote loads in flight per thread in column passes (4 or 8)
+    int col_chunk = 0;     // 0: cost model; 32/64/128: bytes per staged row piece of column passes
 };
 Tuning& tuning();
 

@@ -162,7 +162,9 @@ int eithot_estimate(int rank, const int64_t* dims, const int* perm_1based,
  * compile time).  Process-wide knobs of the lowering, used by the autotuner:
  *   "dbuf"        1 allow double-buffered cluster items, 0 single buffer
  *   "max_cluster" largest thread-block cluster (1, 2, 4, 8, 16)
- *   "variant"     0 cost model, 1 force c2r, 2 force r2c for 2D transposes */
+ *   "variant"     0 cost model, 1 force c2r, 2 force r2c for 2D transposes
+ *   "col_batch"   remote loads in flight per thread in column passes (4, 8)
+ *   "col_chunk"   0 cost model, or 32/64/128 bytes per staged column-row piece */
 int eithot_tune_set(const char* key, double value);
 int eithot_tune_get(const char* key, double* value);
 
