@@ -221,7 +221,8 @@ def index_faults() -> int:
 
 
 def tune_set(key: str, value: float) -> None:
-    """Process-wide lowering knob ("dbuf", "max_cluster", "variant", "col_batch", "col_chunk")."""
+    """Process-wide lowering knob ("dbuf", "max_cluster", "variant", "col_batch", "col_chunk",
+    "col_owner")."""
     _check(lib.eithot_tune_set(key.encode(), float(value)))
 
 

@@ -87,6 +87,8 @@ int eithot_tune_set(const char* key, double value) {
         t.dbuf = value != 0.0 ? 1 : 0;
     } else if (k == "col_batch") {
         t.col_batch = value >= 8 ? 8 : 4;
+    } else if (k == "col_owner") {
+        t.col_owner = value != 0.0 ? 1 : 0;
     } else if (k == "col_chunk") {
         const int v = static_cast<int>(value);
         if (v != 0 && v != 32 && v != 64 && v != 128) return fail(EITHOT_EINVAL, "col_chunk must be 0, 32, 64 or 128");
@@ -111,6 +113,7 @@ int eithot_tune_get(const char* key, double* value) {
     const std::string k(key);
     if (k == "dbuf") *value = t.dbuf;
     else if (k == "col_batch") *value = t.col_batch;
+    else if (k == "col_owner") *value = t.col_owner;
     else if (k == "col_chunk") *value = t.col_chunk;
     else if (k == "max_cluster") *value = t.max_cluster;
     else if (k == "variant") *value = t.variant;

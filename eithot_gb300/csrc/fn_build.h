@@ -86,4 +86,30 @@ inline FnR2CColShuffleT<I> make_r2c_colshuf(const Pass& p) {
     return f;
 }
 
+// Owner maps of the column passes that have one (see index_math.cuh).
+template <typename I>
+inline OwnerColShuffleT<I> make_owner_colshuf(const Pass& p) {
+    OwnerColShuffleT<I> o;
+    o.inv = make_r2c_colshuf<I>(p);
+    return o;
+}
+template <typename I>
+inline OwnerPreRotT<I> make_owner_prerot(const Pass& p) {
+    OwnerPreRotT<I> o;
+    o.inv = make_postrot<I>(p);
+    return o;
+}
+template <typename I>
+inline OwnerPostRotT<I> make_owner_postrot(const Pass& p) {
+    OwnerPostRotT<I> o;
+    o.inv = make_prerot<I>(p);
+    return o;
+}
+template <typename I>
+inline OwnerR2CColShuffleT<I> make_owner_r2c_colshuf(const Pass& p) {
+    OwnerR2CColShuffleT<I> o;
+    o.fn = make_r2c_colshuf<I>(p);
+    return o;
+}
+
 }  // namespace eithot

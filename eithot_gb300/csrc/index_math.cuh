@@ -211,6 +211,52 @@ struct FnR2CPostRotT {
     }
 };
 
+// ---------------------------------------------------------------------------
+// Owner maps.  Every column gather above reads, for output row i of column
+// j, source row sigma((T(i) + delta(j)) mod m) with T and sigma bijections.
+// A CTA that stages "slots" t (slot t holds source row sigma(t)) can then
+// write the whole row piece of output row T^-1((t - delta(j0)) mod m) of a
+// tile starting at column j0, element j0+c coming from slot
+// t + delta(j0+c) - delta(j0):
+//   c2r column shuffle: sigma = id, delta = j;    output row = r2c column shuffle at (t, j0)
+//   c2r pre-rotation:   sigma = id, delta = j/b;  output row = r2c post-rotation at (t, j0)
+//   r2c post-rotation:  sigma = id, delta = -j/b; output row = c2r pre-rotation at (t, j0)
+//   r2c column shuffle: sigma = p(., 0), T = id, delta = -j; output row = (t + j0) mod m
+// (the r2c column shuffle is p((i - j) mod m), p(x) its value at column 0).
+// ---------------------------------------------------------------------------
+template <typename I>
+struct OwnerColShuffleT {
+    using index_type = I;
+    FnR2CColShuffleT<I> inv;
+    EI_HD I stage_of(I t) const { return t; }
+    EI_HD I row_of(I t, I j0) const { return inv(t, j0); }
+    EI_HD int64_t delta(I j) const { return static_cast<int64_t>(j); }
+};
+template <typename I>
+struct OwnerPreRotT {
+    using index_type = I;
+    FnR2CPostRotT<I> inv;
+    EI_HD I stage_of(I t) const { return t; }
+    EI_HD I row_of(I t, I j0) const { return inv(t, j0); }
+    EI_HD int64_t delta(I j) const { return static_cast<int64_t>(inv.divb.div(j)); }
+};
+template <typename I>
+struct OwnerPostRotT {
+    using index_type = I;
+    FnC2RPreRotT<I> inv;
+    EI_HD I stage_of(I t) const { return t; }
+    EI_HD I row_of(I t, I j0) const { return inv(t, j0); }
+    EI_HD int64_t delta(I j) const { return -static_cast<int64_t>(inv.divb.div(j)); }
+};
+template <typename I>
+struct OwnerR2CColShuffleT {
+    using index_type = I;
+    FnR2CColShuffleT<I> fn;
+    EI_HD I stage_of(I t) const { return fn(t, 0); }
+    EI_HD I row_of(I t, I j0) const { return fn.divm.mod(t + j0); }
+    EI_HD int64_t delta(I j) const { return -static_cast<int64_t>(j); }
+};
+
 using FnC2RPreRot = FnC2RPreRotT<uint64_t>;
 using FnRowShuffle = FnRowShuffleT<uint64_t>;
 using FnC2RColShuffle = FnC2RColShuffleT<uint64_t>;

@@ -430,6 +430,142 @@ __global__ void __launch_bounds__(kThreads) k_col_cluster(ColArgs a, Fn fn) {
 }
 
 // ---------------------------------------------------------------------------
+// Owner-computed column pass (c2r column shuffle, c2r pre-rotation, r2c
+// post-rotation; see the owner maps in index_math.cuh).  CTA k of the
+// cluster stages source rows [k*Q - Hlo, (k+1)*Q + Hhi) (mod m) of the tile;
+// after the cluster barrier it writes, for every owned source row x, the
+// whole row piece of output row row_of(x, j0), reading only its own shared
+// memory.  The barrier only orders every CTA's loads of the tile before any
+// CTA's writes to it, so it is relaxed: a load that has returned its value
+// cannot be affected by a later write.
+// ---------------------------------------------------------------------------
+struct ColOwnArgs {
+    uint8_t* base;
+    uint64_t items, E, row_bytes, mat_bytes;
+    uint32_t rows, cols, tw, ntiles, pitch, Q, Hlo, Hhi, w, upw, last_upw, nstrips, RU, buf_bytes;
+    uint32_t hbase;  // (-Hlo) mod m: slot x0 - Hlo is slot (x0 + hbase) mod m, also when Hlo > m
+    bool dbuf;
+    FastDiv div_strips, div_tiles;
+    FastDiv32 div_RU, div_upw, div_m;
+};
+
+struct OwnItem {
+    uint8_t* mat;
+    uint32_t col0, tcols, lim;
+};
+
+__device__ __forceinline__ OwnItem own_item(const ColOwnArgs& a, uint64_t it) {
+    uint64_t bt, s, b, t;
+    a.div_strips.divmod(it, bt, s);
+    a.div_tiles.divmod(bt, b, t);
+    OwnItem c;
+    c.col0 = static_cast<uint32_t>(t) * a.tw;
+    c.tcols = min(a.tw, a.cols - c.col0);
+    c.lim = (s + 1 == a.nstrips) ? a.last_upw : a.upw;
+    c.mat = a.base + b * a.mat_bytes + static_cast<uint64_t>(c.col0) * a.E + s * a.w;
+    return c;
+}
+
+// Stages slots x0 - Hlo .. x0 - Hlo + nstage - 1 (modulo m); slot t holds
+// source row own.stage_of(t).
+template <int US, typename Own, bool kLanes>
+__device__ __forceinline__ void own_stage_in(const ColOwnArgs& a, const Own& own, uint8_t* buf, uint64_t it,
+                                             uint32_t x0, uint32_t nstage, uint32_t lc, uint32_t lu,
+                                             uint32_t ii0, uint32_t step) {
+    using U = typename UnitOf<US>::T;
+    using I = typename Own::index_type;
+    const OwnItem ci = own_item(a, it);
+    const uint32_t tbase = x0 + a.hbase;  // reduced modulo m per slot
+    if constexpr (kLanes) {
+        if (lc < ci.tcols && lu < ci.lim) {
+            const uint64_t lane_off = static_cast<uint64_t>(lc) * a.E + lu * US;
+            for (uint32_t ii = ii0; ii < nstage; ii += step) {
+                const I gr = own.stage_of(static_cast<I>(a.div_m.mod(tbase + ii)));
+                if (!in_range(gr, a.rows)) continue;
+                copy_in<US, U>(buf + ii * a.pitch + lc * a.w + lu * US,
+                               ci.mat + static_cast<uint64_t>(gr) * a.row_bytes + lane_off);
+            }
+        }
+    } else {
+        const uint32_t units = nstage * a.RU;
+        for (uint32_t x = threadIdx.x; x < units; x += blockDim.x) {
+            uint32_t ii, r, c, u;
+            a.div_RU.divmod(x, ii, r);
+            a.div_upw.divmod(r, c, u);
+            if (c >= ci.tcols || u >= ci.lim) continue;
+            const I gr = own.stage_of(static_cast<I>(a.div_m.mod(tbase + ii)));
+            if (!in_range(gr, a.rows)) continue;
+            copy_in<US, U>(buf + ii * a.pitch + c * a.w + u * US,
+                           ci.mat + static_cast<uint64_t>(gr) * a.row_bytes + static_cast<uint64_t>(c) * a.E + u * US);
+        }
+    }
+    if constexpr (US >= 4) asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+template <int US, typename Own, bool kLanes>
+__global__ void __launch_bounds__(kThreads) k_col_owner(ColOwnArgs a, Own own) {
+    using U = typename UnitOf<US>::T;
+    using I = typename Own::index_type;
+    extern __shared__ __align__(16) uint8_t smem[];
+    cg::cluster_group cl = cg::this_cluster();
+    const unsigned K = cl.num_blocks();
+    const unsigned kr = cl.block_rank();
+    const uint64_t cid = blockIdx.x / K, ncl = gridDim.x / K;
+    const uint32_t x0 = kr * a.Q;
+    const uint32_t myrows = x0 < a.rows ? min(a.Q, a.rows - x0) : 0;
+    const uint32_t nstage = myrows ? myrows + a.Hlo + a.Hhi : 0;
+    uint32_t lc = 0, lu = 0, ii0 = 0, step = 1;
+    if constexpr (kLanes) {
+        uint32_t lr;
+        a.div_RU.divmod(threadIdx.x, ii0, lr);
+        a.div_upw.divmod(lr, lc, lu);
+        step = blockDim.x / a.RU;
+    }
+    if (a.dbuf && cid < a.items) own_stage_in<US, Own, kLanes>(a, own, smem, cid, x0, nstage, lc, lu, ii0, step);
+    uint32_t k = 0;
+    for (uint64_t it = cid; it < a.items; it += ncl, ++k) {
+        const uint32_t boff = a.dbuf ? (k & 1) * a.buf_bytes : 0;
+        if (!a.dbuf) own_stage_in<US, Own, kLanes>(a, own, smem, it, x0, nstage, lc, lu, ii0, step);
+        if constexpr (US >= 4) asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        cluster_sync_reuse();  // every CTA holds its rows of this tile: writes may start
+        const uint64_t nxt = it + ncl;
+        if (a.dbuf && nxt < a.items)
+            own_stage_in<US, Own, kLanes>(a, own, smem + (boff ^ a.buf_bytes), nxt, x0, nstage, lc, lu, ii0, step);
+        const OwnItem ci = own_item(a, it);
+        const uint8_t* buf = smem + boff;
+        if constexpr (kLanes) {
+            if (lc < ci.tcols && lu < ci.lim) {
+                const int64_t d = own.delta(static_cast<I>(ci.col0 + lc)) - own.delta(static_cast<I>(ci.col0));
+                const uint32_t soff = lc * a.w + lu * US;
+                const uint64_t lane_off = static_cast<uint64_t>(lc) * a.E + lu * US;
+                for (uint32_t ii = ii0; ii < myrows; ii += step) {
+                    const I i = own.row_of(static_cast<I>(x0 + ii), static_cast<I>(ci.col0));
+                    const int64_t local = static_cast<int64_t>(ii + a.Hlo) + d;
+                    if (!in_range(i, a.rows) || !in_range(static_cast<uint64_t>(local), nstage)) continue;
+                    *reinterpret_cast<U*>(ci.mat + static_cast<uint64_t>(i) * a.row_bytes + lane_off) =
+                        *reinterpret_cast<const U*>(buf + static_cast<uint32_t>(local) * a.pitch + soff);
+                }
+            }
+        } else {
+            const uint32_t units = myrows * a.RU;
+            for (uint32_t x = threadIdx.x; x < units; x += blockDim.x) {
+                uint32_t ii, r, c, u;
+                a.div_RU.divmod(x, ii, r);
+                a.div_upw.divmod(r, c, u);
+                if (c >= ci.tcols || u >= ci.lim) continue;
+                const int64_t d = own.delta(static_cast<I>(ci.col0 + c)) - own.delta(static_cast<I>(ci.col0));
+                const I i = own.row_of(static_cast<I>(x0 + ii), static_cast<I>(ci.col0));
+                const int64_t local = static_cast<int64_t>(ii + a.Hlo) + d;
+                if (!in_range(i, a.rows) || !in_range(static_cast<uint64_t>(local), nstage)) continue;
+                *reinterpret_cast<U*>(ci.mat + static_cast<uint64_t>(i) * a.row_bytes + static_cast<uint64_t>(c) * a.E + u * US) =
+                    *reinterpret_cast<const U*>(buf + static_cast<uint32_t>(local) * a.pitch + c * a.w + u * US);
+            }
+        }
+        __syncthreads();  // this CTA's threads are done with the buffer before it is restaged
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Grid-staged row / column passes for items larger than shared memory.
 // Items [it0, it0 + n) are copied to scratch (item-major, natural layout
 // for gathers, permuted layout for scatters) by k_*_stage_in, then written
@@ -809,6 +945,46 @@ int launch_col(uint8_t* data, const Pass& p, const FnOnChip& fn, const Fn64& fn6
     return 0;
 }
 
+template <int US, typename Own>
+int launch_col_owner(uint8_t* data, const Pass& p, const Staging& st, const Own& own, ExecContext& ctx) {
+    ColOwnArgs a;
+    a.base = data + p.offset;
+    a.E = p.elem;
+    a.row_bytes = p.cols * p.elem;
+    a.mat_bytes = p.rows * a.row_bytes;
+    a.rows = static_cast<uint32_t>(p.rows);
+    a.cols = static_cast<uint32_t>(p.cols);
+    a.tw = static_cast<uint32_t>(st.tw);
+    a.ntiles = static_cast<uint32_t>((p.cols + st.tw - 1) / st.tw);
+    a.pitch = static_cast<uint32_t>(st.pitch);
+    a.w = static_cast<uint32_t>(st.w);
+    a.upw = a.w / US;
+    a.nstrips = static_cast<uint32_t>((p.elem + st.w - 1) / st.w);
+    a.last_upw = static_cast<uint32_t>((p.elem - (a.nstrips - 1) * st.w) / US);
+    a.RU = a.tw * a.upw;
+    a.Q = static_cast<uint32_t>((p.rows + st.K - 1) / st.K);
+    a.Hlo = static_cast<uint32_t>(st.hlo);
+    a.Hhi = static_cast<uint32_t>(st.hhi);
+    a.hbase = static_cast<uint32_t>((p.rows - st.hlo % p.rows) % p.rows);
+    a.items = p.batches * a.ntiles * a.nstrips;
+    a.div_strips = FastDiv::make(a.nstrips, a.items);
+    a.div_tiles = FastDiv::make(a.ntiles, p.batches * a.ntiles);
+    a.div_RU = FastDiv32::make(a.RU);
+    a.div_upw = FastDiv32::make(a.upw);
+    a.div_m = FastDiv32::make(p.rows);
+    const uint64_t slots = static_cast<uint64_t>(a.Q) + a.Hlo + a.Hhi;
+    a.buf_bytes = static_cast<uint32_t>((slots * st.pitch + 127) / 128 * 128);
+    a.dbuf = st.dbuf;
+    const size_t smem = (st.dbuf ? 2 : 1) * static_cast<size_t>(a.buf_bytes);
+    if (kThreads % a.RU != 0)
+        EI_CHECK(launch_clusters(k_col_owner<US, Own, false>, st.K, smem, a.items, ctx, a, own));
+    else
+        EI_CHECK(launch_clusters(k_col_owner<US, Own, true>, st.K, smem, a.items, ctx, a, own));
+    EI_CHECK(cudaGetLastError());
+    ctx.launches++;
+    return 0;
+}
+
 // ---- block moves -------------------------------------------------------------
 template <int US>
 int copy_blocks(const uint8_t* src, uint8_t* dst, uint64_t blk, uint64_t sp, uint64_t dp,
@@ -876,8 +1052,13 @@ int block_move(uint8_t* data, const Pass& p, ExecContext& ctx) {
 }
 
 // ---- dispatch ------------------------------------------------------------------
-template <int US, template <typename> class FnT, typename Make32, typename Make64>
-int run_col(uint8_t* data, const Pass& p, ExecContext& ctx, Make32 m32, Make64 m64) {
+template <int US, template <typename> class FnT, typename Make32, typename Make64, typename Own32, typename Own64>
+int run_col(uint8_t* data, const Pass& p, ExecContext& ctx, Make32 m32, Make64 m64, Own32 o32, Own64 o64) {
+    const Staging st = plan_col_pass(p, smem_cap_of(ctx.caps));
+    if (st.owner) {
+        if (fits32(p)) return launch_col_owner<US>(data, p, st, o32(p), ctx);
+        return launch_col_owner<US>(data, p, st, o64(p), ctx);
+    }
     const FnT<uint64_t> f64 = m64(p);
     if (fits32(p)) return launch_col<US>(data, p, m32(p), f64, ctx);
     return launch_col<US>(data, p, f64, f64, ctx);
@@ -924,13 +1105,17 @@ int run_pass_u(uint8_t* data, const Pass& p, ExecContext& ctx) {
         case kColGather:
             switch (p.fn) {
                 case kFnC2RPreRot:
-                    return run_col<US, FnC2RPreRotT>(data, p, ctx, make_prerot<uint32_t>, make_prerot<uint64_t>);
+                    return run_col<US, FnC2RPreRotT>(data, p, ctx, make_prerot<uint32_t>, make_prerot<uint64_t>,
+                                                     make_owner_prerot<uint32_t>, make_owner_prerot<uint64_t>);
                 case kFnC2RColShuffle:
-                    return run_col<US, FnC2RColShuffleT>(data, p, ctx, make_c2r_colshuf<uint32_t>, make_c2r_colshuf<uint64_t>);
+                    return run_col<US, FnC2RColShuffleT>(data, p, ctx, make_c2r_colshuf<uint32_t>, make_c2r_colshuf<uint64_t>,
+                                                         make_owner_colshuf<uint32_t>, make_owner_colshuf<uint64_t>);
                 case kFnR2CColShuffle:
-                    return run_col<US, FnR2CColShuffleT>(data, p, ctx, make_r2c_colshuf<uint32_t>, make_r2c_colshuf<uint64_t>);
+                    return run_col<US, FnR2CColShuffleT>(data, p, ctx, make_r2c_colshuf<uint32_t>, make_r2c_colshuf<uint64_t>,
+                                                         make_owner_r2c_colshuf<uint32_t>, make_owner_r2c_colshuf<uint64_t>);
                 case kFnR2CPostRot:
-                    return run_col<US, FnR2CPostRotT>(data, p, ctx, make_postrot<uint32_t>, make_postrot<uint64_t>);
+                    return run_col<US, FnR2CPostRotT>(data, p, ctx, make_postrot<uint32_t>, make_postrot<uint64_t>,
+                                                      make_owner_postrot<uint32_t>, make_owner_postrot<uint64_t>);
                 default: break;
             }
             break;
@@ -952,7 +1137,7 @@ uint64_t pass_unit(const uint8_t* data, const Pass& p, size_t smem_cap) {
             return unit_for({addr, p.elem, st.w, p.elem % st.w == 0 ? st.w : p.elem % st.w});
         }
         case kColGather: {
-            const Staging st = plan_col_staging(p.rows, p.elem, smem_cap);
+            const Staging st = plan_col_pass(p, smem_cap);
             return unit_for({addr, p.elem, st.w, st.pitch, p.elem % st.w == 0 ? st.w : p.elem % st.w});
         }
         case kBlockMove:
@@ -973,7 +1158,7 @@ size_t pass_workspace_bytes(const Pass& p, const DeviceCaps& caps) {
             return st.on_chip ? 0 : p.cols * st.w;
         }
         case kColGather: {
-            const Staging st = plan_col_staging(p.rows, p.elem, cap);
+            const Staging st = plan_col_pass(p, cap);
             return st.on_chip ? 0 : p.rows * st.tw * st.w;
         }
         case kBlockMove: {
@@ -999,7 +1184,7 @@ size_t pass_workspace_ideal(const Pass& p, const DeviceCaps& caps) {
             return p.batches * p.rows * ns * p.cols * st.w;
         }
         case kColGather: {
-            const Staging st = plan_col_staging(p.rows, p.elem, cap);
+            const Staging st = plan_col_pass(p, cap);
             if (st.on_chip) return 0;
             const uint64_t ns = (p.elem + st.w - 1) / st.w;
             const uint64_t nt = (p.cols + st.tw - 1) / st.tw;

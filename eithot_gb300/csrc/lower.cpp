@@ -167,6 +167,65 @@ Staging plan_col_staging(uint64_t rows, uint64_t E, size_t cap) {
     return s;
 }
 
+void owner_halo(int fn, uint64_t b, uint64_t tw, uint64_t* lo, uint64_t* hi) {
+    *lo = 0;
+    *hi = 0;
+    if (tw <= 1) return;
+    // delta(j0 + c) - delta(j0) over c < tw: c for the shuffles, at most
+    // (tw - 1) / b + 1 steps of j / b for the rotations
+    const bool shuffle = fn == kFnC2RColShuffle || fn == kFnR2CColShuffle;
+    const uint64_t spread = shuffle ? tw - 1 : (tw - 1) / std::max<uint64_t>(b, 1) + 1;
+    if (fn == kFnR2CPostRot || fn == kFnR2CColShuffle) *lo = spread; else *hi = spread;
+}
+
+namespace {
+// Owner-computed column staging: the cluster's CTAs split the tile's rows,
+// each staging its share plus halo; writes read only the CTA's own shared
+// memory, so the cluster size costs only its barrier.
+Staging plan_col_owner(uint64_t rows, uint64_t E, int fn, uint64_t b, size_t cap) {
+    Staging s;
+    for (uint64_t occ_limit : {kTwoPerSm, static_cast<uint64_t>(cap)}) {
+        for (uint64_t tb : {uint64_t(128), uint64_t(64), uint64_t(32)}) {
+            if (tuning().col_chunk && tb != static_cast<uint64_t>(tuning().col_chunk)) continue;
+            uint64_t w, tw;
+            if (E <= tb) { w = E; tw = std::max<uint64_t>(1, tb / E); }
+            else { w = tb; tw = 1; }
+            const uint64_t pitch = tw * w;
+            uint64_t lo, hi;
+            owner_halo(fn, b, tw, &lo, &hi);
+            for (int K : kClusterSizes) {
+                if (K > tuning().max_cluster) break;
+                const uint64_t Q = (rows + K - 1) / K;
+                const uint64_t per = (Q + lo + hi) * pitch;
+                for (bool db : {true, false}) {
+                    if (db && !tuning().dbuf) continue;
+                    const uint64_t foot = per * (db ? 2 : 1);
+                    if (foot > cap || foot > occ_limit) continue;
+                    s.w = w; s.tw = tw; s.pitch = pitch; s.K = K; s.per_cta = per;
+                    s.item_bytes = rows * pitch; s.on_chip = true; s.dbuf = db;
+                    s.owner = true; s.hlo = lo; s.hhi = hi;
+                    // halo rows are read twice; a barrier per item per doubling of K
+                    s.cost = 1.0 + 0.5 * static_cast<double>((lo + hi) * K) / static_cast<double>(rows) +
+                             0.03 * log2i(K) + (tb < 128 ? 0.1 : 0.0) + (db ? 0.0 : 0.1) +
+                             (foot > kTwoPerSm ? kOnePerSmPenalty : 0.0);
+                    return s;
+                }
+            }
+        }
+    }
+    s.on_chip = false;
+    return s;
+}
+}  // namespace
+
+Staging plan_col_pass(const Pass& p, size_t cap) {
+    if (tuning().col_owner) {
+        const Staging s = plan_col_owner(p.rows, p.elem, p.fn, p.b, cap);
+        if (s.on_chip) return s;
+    }
+    return plan_col_staging(p.rows, p.elem, cap);
+}
+
 Xpose xpose_of(const LowOp& op, uint64_t elem, uint64_t n_sub, uint64_t base_offset) {
     Xpose x;
     x.offset = base_offset;
@@ -188,8 +247,10 @@ namespace {
 double row_cost(uint64_t cols, uint64_t E, size_t cap, bool scatter) {
     return plan_row_staging(cols, E, cap, scatter).cost;
 }
-double col_cost(uint64_t rows, uint64_t E, size_t cap) {
-    return plan_col_staging(rows, E, cap).cost;
+double col_cost(uint64_t rows, uint64_t E, int fn, uint64_t b, size_t cap) {
+    Pass p;
+    p.rows = rows; p.elem = E; p.fn = fn; p.b = b;
+    return plan_col_pass(p, cap).cost;
 }
 
 std::string geom(const char* name, uint64_t B, uint64_t r, uint64_t c, uint64_t E) {
@@ -220,8 +281,10 @@ void lower_xpose(const Xpose& x, const DeviceCaps& caps, std::vector<Pass>* pass
     // Catanzaro: c2r on the R x C view, or r2c on the C x R view.
     uint64_t g, inv;
     gcd_inverse(x.R, x.C, &g, &inv);
-    const double c2r = (g > 1 ? col_cost(x.R, x.E, cap) : 0.0) + row_cost(x.C, x.E, cap, false) + col_cost(x.R, x.E, cap);
-    const double r2c = col_cost(x.C, x.E, cap) + row_cost(x.R, x.E, cap, true) + (g > 1 ? col_cost(x.C, x.E, cap) : 0.0);
+    const double c2r = (g > 1 ? col_cost(x.R, x.E, kFnC2RPreRot, x.C / g, cap) : 0.0) + row_cost(x.C, x.E, cap, false) +
+                       col_cost(x.R, x.E, kFnC2RColShuffle, x.C / g, cap);
+    const double r2c = col_cost(x.C, x.E, kFnR2CColShuffle, x.R / g, cap) + row_cost(x.R, x.E, cap, true) +
+                       (g > 1 ? col_cost(x.C, x.E, kFnR2CPostRot, x.R / g, cap) : 0.0);
     bool use_c2r = (c2r < r2c) || (c2r == r2c && x.C >= x.R);
     if (tuning().variant == 1) use_c2r = true;
     if (tuning().variant == 2) use_c2r = false;
@@ -231,10 +294,11 @@ void lower_xpose(const Xpose& x, const DeviceCaps& caps, std::vector<Pass>* pass
     base.elem = x.E;
     if (use_c2r) {
         const uint64_t m = x.R, n = x.C;
-        uint64_t unused, k;
+        uint64_t unused, k, q;
         gcd_inverse(m / g, n / g, &unused, &k);  // k = (m/g)^-1 mod (n/g)
+        gcd_inverse(n / g, m / g, &unused, &q);  // q = (n/g)^-1 mod (m/g), for the inverse column map
         base.rows = m; base.cols = n;
-        base.m = m; base.n = n; base.c = g; base.k = k; base.a = m / g; base.b = n / g;
+        base.m = m; base.n = n; base.c = g; base.k = k; base.q = q; base.a = m / g; base.b = n / g;
         if (g > 1) {
             Pass p = base; p.type = kColGather; p.fn = kFnC2RPreRot;
             p.what = geom("c2r-prerotate", x.B, m, n, x.E);

@@ -71,6 +71,7 @@ struct Tuning {
     int dbuf = 1;          // allow double-buffered cluster items
     int col_batch = 4;     // remote loads in flight per thread in column passes (4 or 8)
     int col_chunk = 0;     // 0: cost model; 32/64/128: bytes per staged row piece of column passes
+    int col_owner = 1;     // column passes: 1 owner-computed writes, 0 gathers through distributed smem
 };
 Tuning& tuning();
 
@@ -88,6 +89,8 @@ struct Staging {
     uint64_t per_cta = 0;  // shared-memory bytes each CTA stages per item
     bool dbuf = false;     // two item buffers per CTA (next item's loads overlap)
     bool on_chip = false;  // the item fits the cluster's distributed shared memory
+    bool owner = false;    // column pass run owner-computed (each CTA writes from its own rows)
+    uint64_t hlo = 0, hhi = 0;  // owner-computed: halo rows staged below / above the owned ones
     double cost = 0;       // modelled time in units of one streaming pass
 };
 
@@ -95,6 +98,14 @@ struct Staging {
 // otherwise it pulls them (c2r).
 Staging plan_row_staging(uint64_t cols, uint64_t E, size_t smem_cap, bool scatter = false);
 Staging plan_col_staging(uint64_t rows, uint64_t E, size_t smem_cap);
+
+// Rows of halo an owner-computed column tile of tw columns needs below (lo)
+// and above (hi) its owned rows for column map `fn` (b = n / gcd(m, n)).
+void owner_halo(int fn, uint64_t b, uint64_t tw, uint64_t* lo, uint64_t* hi);
+
+// Staging of column pass `p` (fn, rows, elem, b): owner-computed when the
+// tuning allows and the tile fits on chip, else plan_col_staging's.
+Staging plan_col_pass(const Pass& p, size_t smem_cap);
 
 // Lowers every step of `plan` for element size `elem` into passes.
 bool lower_plan(const NdPlan& plan, uint64_t elem, const DeviceCaps& caps,

@@ -164,7 +164,9 @@ int eithot_estimate(int rank, const int64_t* dims, const int* perm_1based,
  *   "max_cluster" largest thread-block cluster (1, 2, 4, 8, 16)
  *   "variant"     0 cost model, 1 force c2r, 2 force r2c for 2D transposes
  *   "col_batch"   remote loads in flight per thread in column passes (4, 8)
- *   "col_chunk"   0 cost model, or 32/64/128 bytes per staged column-row piece */
+ *   "col_chunk"   0 cost model, or 32/64/128 bytes per staged column-row piece
+ *   "col_owner"   1 column passes write from the rows each CTA staged itself,
+ *                 0 gather through distributed shared memory */
 int eithot_tune_set(const char* key, double value);
 int eithot_tune_get(const char* key, double* value);
 

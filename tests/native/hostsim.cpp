@@ -183,3 +183,83 @@ long hs_check_inverse(int rank, const int64_t* dims, const int* perm, size_t ele
 }
 
 }  // extern "C"
+
+namespace {
+// Checks one owner map against the column gather it replaces: for tiles of
+// tw columns starting at j0, slot t's output row i = row_of(t, j0) must take,
+// at column j0 + c, the source row the gather names, held by slot
+// t + delta(j0 + c) - delta(j0), within the planned halo.
+template <typename Own, typename Fn>
+long check_owner(const Pass& p, const Own& own, const Fn& g, uint64_t tw, long max_full) {
+    uint64_t lo, hi;
+    owner_halo(p.fn, p.b, tw, &lo, &hi);
+    long bad = 0;
+    const uint64_t m = p.m, n = p.n;
+    const uint64_t ntiles = (n + tw - 1) / tw;
+    const uint64_t total = m * ntiles;
+    const uint64_t stride = total <= static_cast<uint64_t>(max_full) ? 1 : total / max_full + 1;
+    std::vector<uint8_t> seen;
+    for (uint64_t x = 0; x < total; x += stride) {
+        const uint64_t t = x % m, j0 = (x / m) * tw;
+        using I = typename Own::index_type;
+        const uint64_t i = own.row_of(static_cast<I>(t), static_cast<I>(j0));
+        if (i >= m) { ++bad; continue; }
+        if (stride == 1) {  // row_of(., j0) is a bijection of the m slots
+            if (t == 0) seen.assign(m, 0);
+            if (seen[i]++) ++bad;
+        }
+        for (uint64_t c = 0; c < tw && j0 + c < n; ++c) {
+            const int64_t d = own.delta(static_cast<I>(j0 + c)) - own.delta(static_cast<I>(j0));
+            if (d < -static_cast<int64_t>(lo) || d > static_cast<int64_t>(hi)) { ++bad; continue; }
+            const int64_t sm = static_cast<int64_t>(m);
+            const uint64_t slot = static_cast<uint64_t>(((static_cast<int64_t>(t) + d) % sm + sm) % sm);
+            if (static_cast<uint64_t>(own.stage_of(static_cast<I>(slot))) != static_cast<uint64_t>(g(i, j0 + c))) ++bad;
+        }
+    }
+    return bad;
+}
+
+template <typename I>
+long check_owner_pass(const Pass& p, uint64_t tw, long max_full) {
+    switch (p.fn) {
+        case kFnC2RPreRot: return check_owner(p, make_owner_prerot<I>(p), make_prerot<uint64_t>(p), tw, max_full);
+        case kFnC2RColShuffle: return check_owner(p, make_owner_colshuf<I>(p), make_c2r_colshuf<uint64_t>(p), tw, max_full);
+        case kFnR2CColShuffle: return check_owner(p, make_owner_r2c_colshuf<I>(p), make_r2c_colshuf<uint64_t>(p), tw, max_full);
+        case kFnR2CPostRot: return check_owner(p, make_owner_postrot<I>(p), make_postrot<uint64_t>(p), tw, max_full);
+        default: return 0;
+    }
+}
+}  // namespace
+
+extern "C" {
+
+// Owner-computed column passes of both 2D variants of the plan agree with
+// the column gathers they stand for (tiles of 1..128 columns); returns the
+// number of disagreements, -1 on a planning error.  Counts every column pass
+// visited in *n_checked.
+long hs_check_owner(int rank, const int64_t* dims, const int* perm, size_t elem, int nb, double alpha,
+                    int order, long max_full, long* n_checked) {
+    NdPlan plan;
+    if (!make_nd_plan(rank, dims, perm, nb, alpha, order, &plan, &g_err)) return -1;
+    long bad = 0, visited = 0;
+    const int saved = tuning().variant;
+    for (int variant : {1, 2}) {
+        tuning().variant = variant;
+        std::vector<Pass> passes;
+        DeviceCaps caps;
+        if (!lower_plan(plan, elem, caps, &passes, &g_err)) { tuning().variant = saved; return -1; }
+        for (const Pass& p : passes) {
+            if (p.type != kColGather) continue;
+            ++visited;
+            for (uint64_t tw : {1, 2, 4, 8, 16, 32, 128}) {
+                bad += check_owner_pass<uint64_t>(p, tw, max_full);
+                if (fits32(p)) bad += check_owner_pass<uint32_t>(p, tw, max_full);
+            }
+        }
+    }
+    tuning().variant = saved;
+    if (n_checked) *n_checked = visited;
+    return bad;
+}
+
+}  // extern "C"

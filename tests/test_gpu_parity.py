@@ -83,6 +83,44 @@ def test_catanzaro_2d(E, R, C, elem):
     run_case(E, [C, R], [2, 1], elem)
 
 
+@pytest.fixture
+def tuned(E):
+    keys = ("variant", "col_owner", "col_chunk", "max_cluster", "dbuf")
+    saved = {k: E.tune_get(k) for k in keys}
+
+    def set_(**kw):
+        for k, v in kw.items():
+            E.tune_set(k, v)
+    yield set_
+    for k, v in saved.items():
+        E.tune_set(k, v)
+
+
+@pytest.mark.parametrize("R,C,elem", [(3001, 4096, 4), (6000, 4000, 2), (4000, 6000, 1), (5, 70000, 8),
+                                      (70000, 5, 8), (5000, 60, 16), (40, 2000, 24), (1000, 999, 1),
+                                      (2048, 1536, 32)])
+@pytest.mark.parametrize("variant", [1, 2])
+@pytest.mark.parametrize("owner", [0, 1])
+def test_column_kernels_both_forms(E, tuned, R, C, elem, variant, owner):
+    """c2r and r2c, each with owner-computed column passes and with column
+    gathers through distributed shared memory, on shapes with gcd 1 and
+    gcd > 1 (rotations), rows fewer than a tile's halo and wide elements."""
+    tuned(variant=variant, col_owner=owner)
+    run_case(E, [C, R], [2, 1], elem)
+
+
+@pytest.mark.parametrize("chunk,max_cluster,dbuf", [(32, 16, 1), (64, 8, 1), (128, 4, 0), (64, 2, 1), (32, 1, 0)])
+def test_column_tilings(E, tuned, chunk, max_cluster, dbuf):
+    """Row-piece widths, cluster sizes and single/double buffering of the
+    column passes (the autotuner's search space)."""
+    tuned(col_chunk=chunk, max_cluster=max_cluster, dbuf=dbuf)
+    for variant in (1, 2):
+        E.tune_set("variant", variant)
+        run_case(E, [4096, 3001], [2, 1], 4)
+        run_case(E, [4, 20011, 819, 2], [1, 3, 2, 4], 4)
+        run_case(E, [4000, 6000], [2, 1], 2)
+
+
 @pytest.mark.parametrize("dims,perm", [([60000, 300], [2, 1]), ([300, 60000], [2, 1]),
                                        ([4, 20011, 819, 2], [1, 3, 2, 4]), ([17, 30011, 37], [1, 3, 2]),
                                        ([3, 50000, 41], [3, 2, 1])])

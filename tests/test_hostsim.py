@@ -87,3 +87,24 @@ def test_row_shuffle_inverse(hostsim, dims, perm, elem):
                                          ctypes.c_size_t, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_long]
     assert hostsim.hs_check_inverse(r, (ctypes.c_int64 * r)(*dims), (ctypes.c_int * r)(*perm), elem, 1, 0.01, 0,
                                     2000000) == 0
+
+
+@pytest.mark.parametrize("dims,perm,elem", [
+    ([4, 20011, 8192, 2], [1, 3, 2, 4], 4), ([3001, 4096], [2, 1], 4), ([2048, 1536], [2, 1], 4),
+    ([1000, 999], [2, 1], 2), ([60000, 300], [2, 1], 4), ([6000, 4000], [2, 1], 4), ([4000, 6000], [2, 1], 2),
+    ([5, 70000], [2, 1], 8), ([60, 4, 3401], [3, 2, 1], 2), ([12, 9000, 900], [1, 3, 2], 4)])
+def test_owner_maps_match_column_gathers(hostsim, dims, perm, elem):
+    """Owner-computed column passes (each CTA writes whole output row pieces
+    from the source rows it staged itself, plus a halo) write exactly what
+    the column gathers of both the c2r and the r2c variant write."""
+    import ctypes
+    r = len(dims)
+    hostsim.hs_check_owner.restype = ctypes.c_long
+    hostsim.hs_check_owner.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int),
+                                       ctypes.c_size_t, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_long,
+                                       ctypes.POINTER(ctypes.c_long)]
+    visited = ctypes.c_long()
+    bad = hostsim.hs_check_owner(r, (ctypes.c_int64 * r)(*dims), (ctypes.c_int * r)(*perm), elem, 1, 0.01, 0,
+                                 300000, ctypes.byref(visited))
+    assert bad == 0
+    assert visited.value >= 1
