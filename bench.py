@@ -74,11 +74,18 @@ def load_peaks():
 
 
 def load_traffic():
-    path = os.path.join(ROOT, "profiles", "traffic.json")
+    """DRAM bytes per launch of each pass kind at this workload, as measured
+    by ncu (dram__bytes_read.sum + dram__bytes_write.sum): lines
+    `<pass kind> <bytes>` in profiles/traffic.txt, '#' starts a comment."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    out = {}
     if os.path.exists(path):
         with open(path) as f:
-            return json.load(f)
-    return {}
+            for line in f:
+                line = line.split("#", 1)[0].split()
+                if len(line) == 2:
+                    out[line[0]] = float(line[1])
+    return out
 
 
 class ClockSampler:

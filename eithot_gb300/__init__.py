@@ -220,9 +220,25 @@ def index_faults() -> int:
     return v.value
 
 
+def sync_timeouts() -> int:
+    """Bounded group-barrier waits that gave up since the last call (their
+    transposes' outputs are invalid); synchronises the device."""
+    v = ctypes.c_uint()
+    _check(lib.eithot_sync_timeouts(ctypes.byref(v)))
+    return v.value
+
+
+def selftest_wait() -> int:
+    """Runs one bounded wait that nothing releases; returns the timeouts it
+    counted (1 when the bound holds)."""
+    v = ctypes.c_uint()
+    _check(lib.eithot_selftest_wait(ctypes.byref(v)))
+    return v.value
+
+
 def tune_set(key: str, value: float) -> None:
     """Process-wide lowering knob ("dbuf", "max_cluster", "variant", "col_batch", "col_chunk",
-    "col_owner")."""
+    "col_owner", "col_form")."""
     _check(lib.eithot_tune_set(key.encode(), float(value)))
 
 

@@ -89,9 +89,14 @@ int eithot_tune_set(const char* key, double value) {
         t.col_batch = value >= 8 ? 8 : 4;
     } else if (k == "col_owner") {
         t.col_owner = value != 0.0 ? 1 : 0;
+    } else if (k == "col_form") {
+        const int v = static_cast<int>(value);
+        if (v < 0 || v > 2) return fail(EITHOT_EINVAL, "col_form must be 0, 1 or 2");
+        t.col_form = v;
     } else if (k == "col_chunk") {
         const int v = static_cast<int>(value);
-        if (v != 0 && v != 32 && v != 64 && v != 128) return fail(EITHOT_EINVAL, "col_chunk must be 0, 32, 64 or 128");
+        if (v != 0 && v != 32 && v != 64 && v != 128 && v != 256 && v != 512)
+            return fail(EITHOT_EINVAL, "col_chunk must be 0, 32, 64, 128, 256 or 512");
         t.col_chunk = v;
     } else if (k == "max_cluster") {
         const int v = static_cast<int>(value);
@@ -114,6 +119,7 @@ int eithot_tune_get(const char* key, double* value) {
     if (k == "dbuf") *value = t.dbuf;
     else if (k == "col_batch") *value = t.col_batch;
     else if (k == "col_owner") *value = t.col_owner;
+    else if (k == "col_form") *value = t.col_form;
     else if (k == "col_chunk") *value = t.col_chunk;
     else if (k == "max_cluster") *value = t.max_cluster;
     else if (k == "variant") *value = t.variant;
@@ -156,6 +162,19 @@ int eithot_profile_get(int i, char* name, size_t name_len, double* ms, double* b
 int eithot_index_faults(unsigned int* count) {
     if (!count) return fail(EITHOT_EINVAL, "null count");
     if (eithot::read_index_faults(count)) return fail(EITHOT_ECUDA, "reading the index-fault counter failed");
+    return EITHOT_OK;
+}
+
+int eithot_sync_timeouts(unsigned int* count) {
+    if (!count) return fail(EITHOT_EINVAL, "null count");
+    if (eithot::read_sync_timeouts(count)) return fail(EITHOT_ECUDA, "reading the sync-timeout counter failed");
+    return EITHOT_OK;
+}
+
+int eithot_selftest_wait(unsigned int* timeouts) {
+    if (!timeouts) return fail(EITHOT_EINVAL, "null count");
+    std::string err;
+    if (eithot::run_wait_selftest(timeouts, &err)) return fail(EITHOT_ECUDA, err);
     return EITHOT_OK;
 }
 
@@ -420,6 +439,10 @@ void transpose(void* data, int source, int rank, void* dim, void* permutation, s
             std::fprintf(stderr, "inplace::transpose: %s\n", cudaGetErrorString(e));
             return;
         }
+        unsigned int timeouts = 0;
+        if (eithot_sync_timeouts(&timeouts) == EITHOT_OK && timeouts)
+            std::fprintf(stderr, "inplace::transpose: %u bounded device waits gave up; the output is invalid\n",
+                         timeouts);
     } else {
         std::fprintf(stderr, "inplace::transpose: %s\n", eithot_last_error());
     }

@@ -62,4 +62,13 @@ int noalloc_scratch(uint8_t** ptr, std::string* err);
 // last read (the kernels skip such accesses).  Synchronises the device.
 int read_index_faults(unsigned int* out);
 
+// Returns and clears the number of bounded group-barrier waits that gave up
+// (their launch aborted its writes); synchronises the device.
+int read_sync_timeouts(unsigned int* out);
+
+// Launches one CTA that waits on a counter nothing increments; it must give
+// up after its spin limit.  *timeouts = timeouts counted (1 when the bound
+// holds).  Synchronises the device.
+int run_wait_selftest(unsigned int* timeouts, std::string* err);
+
 }  // namespace eithot

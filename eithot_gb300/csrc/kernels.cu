@@ -566,6 +566,125 @@ __global__ void __launch_bounds__(kThreads) k_col_owner(ColOwnArgs a, Own own) {
 }
 
 // ---------------------------------------------------------------------------
+// Owner-computed column pass over groups of G co-resident CTAs (a
+// cooperative launch guarantees co-residency), for tiles larger than a
+// cluster's shared memory.  Group g takes items g, g + nG, ...; its CTA r
+// owns slots [r*Q, (r+1)*Q).  The barrier between the group's loads and its
+// writes is a monotonic arrival counter per group in global memory (zeroed
+// before the launch): after its loads of the group's k-th item have landed
+// in shared memory a CTA adds 1 with release semantics, and it writes once
+// the counter has reached (k+1)*G (acquire).  Every wait is bounded: a CTA
+// that gives up (or sees another give up) counts a sync timeout, raises the
+// launch's abort flag and returns after its own copies have landed.
+// ---------------------------------------------------------------------------
+struct GroupSync {
+    unsigned* counters;  // nG arrival counters, then the abort flag
+    unsigned G, nG;
+};
+
+__device__ unsigned g_sync_timeouts;
+
+constexpr uint32_t kSpinLimit = 1u << 20;  // ~0.5 s of polling at ~0.5 us per poll
+
+__device__ __forceinline__ void group_arrive(unsigned* ctr) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;\n" ::"l"(ctr) : "memory");
+}
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Thread 0 waits until *ctr >= target; false when it gave up or the launch
+// was aborted.  Called by thread 0 only.
+__device__ bool group_wait(const unsigned* ctr, unsigned target, unsigned* abort_flag) {
+    for (uint32_t it = 0; it < kSpinLimit; ++it) {
+        if (ld_acquire(ctr) >= target) return true;
+        if ((it & 31) == 31 && ld_acquire(abort_flag) != 0) return false;
+        __nanosleep(256);
+    }
+    atomicAdd(&g_sync_timeouts, 1u);
+    atomicExch(abort_flag, 1u);
+    return false;
+}
+
+template <int US, typename Own, bool kLanes>
+__global__ void __launch_bounds__(kThreads) k_col_group(ColOwnArgs a, Own own, GroupSync gs) {
+    using U = typename UnitOf<US>::T;
+    using I = typename Own::index_type;
+    extern __shared__ __align__(16) uint8_t smem[];
+    __shared__ int s_ok;
+    const unsigned grp = blockIdx.x / gs.G, r = blockIdx.x - grp * gs.G;
+    if (grp >= gs.nG) return;  // never launched: the grid is nG * G CTAs
+    unsigned* ctr = gs.counters + grp;
+    unsigned* abort_flag = gs.counters + gs.nG;
+    const uint32_t x0 = r * a.Q;
+    const uint32_t myrows = x0 < a.rows ? min(a.Q, a.rows - x0) : 0;
+    const uint32_t nstage = myrows ? myrows + a.Hlo + a.Hhi : 0;
+    uint32_t lc = 0, lu = 0, ii0 = 0, step = 1;
+    if constexpr (kLanes) {
+        uint32_t lr;
+        a.div_RU.divmod(threadIdx.x, ii0, lr);
+        a.div_upw.divmod(lr, lc, lu);
+        step = blockDim.x / a.RU;
+    }
+    if (a.dbuf && grp < a.items) own_stage_in<US, Own, kLanes>(a, own, smem, grp, x0, nstage, lc, lu, ii0, step);
+    uint32_t k = 0;
+    for (uint64_t it = grp; it < a.items; it += gs.nG, ++k) {
+        const uint32_t boff = a.dbuf ? (k & 1) * a.buf_bytes : 0;
+        if (!a.dbuf) own_stage_in<US, Own, kLanes>(a, own, smem, it, x0, nstage, lc, lu, ii0, step);
+        if constexpr (US >= 4) asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        __syncthreads();  // this CTA's slots of the item are in shared memory
+        if (threadIdx.x == 0 && gs.G > 1) group_arrive(ctr);
+        const uint64_t nxt = it + gs.nG;
+        if (a.dbuf && nxt < a.items)
+            own_stage_in<US, Own, kLanes>(a, own, smem + (boff ^ a.buf_bytes), nxt, x0, nstage, lc, lu, ii0, step);
+        if (threadIdx.x == 0) s_ok = gs.G <= 1 || group_wait(ctr, (k + 1) * gs.G, abort_flag);
+        __syncthreads();  // every CTA of the group holds its slots: writes may start
+        if (!s_ok) break;
+        const OwnItem ci = own_item(a, it);
+        const uint8_t* buf = smem + boff;
+        if constexpr (kLanes) {
+            if (lc < ci.tcols && lu < ci.lim) {
+                const int64_t d = own.delta(static_cast<I>(ci.col0 + lc)) - own.delta(static_cast<I>(ci.col0));
+                const uint32_t soff = lc * a.w + lu * US;
+                const uint64_t lane_off = static_cast<uint64_t>(lc) * a.E + lu * US;
+                for (uint32_t ii = ii0; ii < myrows; ii += step) {
+                    const I i = own.row_of(static_cast<I>(x0 + ii), static_cast<I>(ci.col0));
+                    const int64_t local = static_cast<int64_t>(ii + a.Hlo) + d;
+                    if (!in_range(i, a.rows) || !in_range(static_cast<uint64_t>(local), nstage)) continue;
+                    *reinterpret_cast<U*>(ci.mat + static_cast<uint64_t>(i) * a.row_bytes + lane_off) =
+                        *reinterpret_cast<const U*>(buf + static_cast<uint32_t>(local) * a.pitch + soff);
+                }
+            }
+        } else {
+            const uint32_t units = myrows * a.RU;
+            for (uint32_t x = threadIdx.x; x < units; x += blockDim.x) {
+                uint32_t ii, rr, c, u;
+                a.div_RU.divmod(x, ii, rr);
+                a.div_upw.divmod(rr, c, u);
+                if (c >= ci.tcols || u >= ci.lim) continue;
+                const int64_t d = own.delta(static_cast<I>(ci.col0 + c)) - own.delta(static_cast<I>(ci.col0));
+                const I i = own.row_of(static_cast<I>(x0 + ii), static_cast<I>(ci.col0));
+                const int64_t local = static_cast<int64_t>(ii + a.Hlo) + d;
+                if (!in_range(i, a.rows) || !in_range(static_cast<uint64_t>(local), nstage)) continue;
+                *reinterpret_cast<U*>(ci.mat + static_cast<uint64_t>(i) * a.row_bytes + static_cast<uint64_t>(c) * a.E + u * US) =
+                    *reinterpret_cast<const U*>(buf + static_cast<uint32_t>(local) * a.pitch + c * a.w + u * US);
+            }
+        }
+        __syncthreads();  // this CTA's threads are done with the buffer before it is restaged
+    }
+    if constexpr (US >= 4) asm volatile("cp.async.wait_group 0;\n" ::: "memory");  // no copy outlives the CTA
+}
+
+// Launch-time self-test of the bounded wait: one CTA waits on a counter
+// that nothing increments and must give up, counting one sync timeout.
+__global__ void k_wait_selftest(unsigned* counters) {
+    if (threadIdx.x == 0) group_wait(counters, 1u, counters + 1);
+}
+
+// ---------------------------------------------------------------------------
 // Grid-staged row / column passes for items larger than shared memory.
 // Items [it0, it0 + n) are copied to scratch (item-major, natural layout
 // for gathers, permuted layout for scatters) by k_*_stage_in, then written
@@ -945,8 +1064,7 @@ int launch_col(uint8_t* data, const Pass& p, const FnOnChip& fn, const Fn64& fn6
     return 0;
 }
 
-template <int US, typename Own>
-int launch_col_owner(uint8_t* data, const Pass& p, const Staging& st, const Own& own, ExecContext& ctx) {
+ColOwnArgs col_owner_args(uint8_t* data, const Pass& p, const Staging& st, int US) {
     ColOwnArgs a;
     a.base = data + p.offset;
     a.E = p.elem;
@@ -962,7 +1080,8 @@ int launch_col_owner(uint8_t* data, const Pass& p, const Staging& st, const Own&
     a.nstrips = static_cast<uint32_t>((p.elem + st.w - 1) / st.w);
     a.last_upw = static_cast<uint32_t>((p.elem - (a.nstrips - 1) * st.w) / US);
     a.RU = a.tw * a.upw;
-    a.Q = static_cast<uint32_t>((p.rows + st.K - 1) / st.K);
+    const uint64_t parts = st.group ? static_cast<uint64_t>(st.G) : static_cast<uint64_t>(st.K);
+    a.Q = static_cast<uint32_t>((p.rows + parts - 1) / parts);
     a.Hlo = static_cast<uint32_t>(st.hlo);
     a.Hhi = static_cast<uint32_t>(st.hhi);
     a.hbase = static_cast<uint32_t>((p.rows - st.hlo % p.rows) % p.rows);
@@ -975,11 +1094,67 @@ int launch_col_owner(uint8_t* data, const Pass& p, const Staging& st, const Own&
     const uint64_t slots = static_cast<uint64_t>(a.Q) + a.Hlo + a.Hhi;
     a.buf_bytes = static_cast<uint32_t>((slots * st.pitch + 127) / 128 * 128);
     a.dbuf = st.dbuf;
+    return a;
+}
+
+template <int US, typename Own>
+int launch_col_owner(uint8_t* data, const Pass& p, const Staging& st, const Own& own, ExecContext& ctx) {
+    const ColOwnArgs a = col_owner_args(data, p, st, US);
     const size_t smem = (st.dbuf ? 2 : 1) * static_cast<size_t>(a.buf_bytes);
     if (kThreads % a.RU != 0)
         EI_CHECK(launch_clusters(k_col_owner<US, Own, false>, st.K, smem, a.items, ctx, a, own));
     else
         EI_CHECK(launch_clusters(k_col_owner<US, Own, true>, st.K, smem, a.items, ctx, a, own));
+    EI_CHECK(cudaGetLastError());
+    ctx.launches++;
+    return 0;
+}
+
+// Cooperative launch of nG groups of G CTAs, nG as large as residency
+// allows (at most one group per item, at most max_groups).
+template <typename Own>
+cudaError_t launch_groups(void (*kernel)(ColOwnArgs, Own, GroupSync), size_t smem, const ColOwnArgs& a,
+                          const Own& own, GroupSync gs, unsigned max_groups, ExecContext& ctx) {
+    const void* kp = reinterpret_cast<const void*>(kernel);
+    cudaError_t e = prep_smem(kp, smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kp, kThreads, smem);
+    if (e != cudaSuccess) return e;
+    const uint64_t resident = static_cast<uint64_t>(per_sm) * ctx.caps.sms;
+    if (resident < gs.G) return cudaErrorCooperativeLaunchTooLarge;
+    gs.nG = static_cast<unsigned>(std::min<uint64_t>({a.items, resident / gs.G, static_cast<uint64_t>(max_groups)}));
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = ctx.stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cfg.gridDim = dim3(gs.nG * gs.G);
+    return cudaLaunchKernelEx(&cfg, kernel, a, own, gs);
+}
+
+template <int US, typename Own>
+int launch_col_group(uint8_t* data, const Pass& p, const Staging& st, const Own& own, ExecContext& ctx) {
+    const ColOwnArgs a = col_owner_args(data, p, st, US);
+    const size_t smem = (st.dbuf ? 2 : 1) * static_cast<size_t>(a.buf_bytes);
+    if (ctx.scratch == nullptr || ctx.scratch_bytes < kGroupSyncBytes) {
+        ctx.err = "workspace too small for a group-synchronised column pass";
+        return EITHOT_STATUS_NOMEM;
+    }
+    GroupSync gs;
+    gs.counters = reinterpret_cast<unsigned*>(ctx.scratch);
+    gs.G = static_cast<unsigned>(st.G);
+    gs.nG = 0;
+    const unsigned max_groups = static_cast<unsigned>(kGroupSyncBytes / sizeof(unsigned)) - 1;
+    EI_CHECK(cudaMemsetAsync(ctx.scratch, 0, kGroupSyncBytes, ctx.stream));  // counters and abort flag
+    if (kThreads % a.RU != 0)
+        EI_CHECK(launch_groups(k_col_group<US, Own, false>, smem, a, own, gs, max_groups, ctx));
+    else
+        EI_CHECK(launch_groups(k_col_group<US, Own, true>, smem, a, own, gs, max_groups, ctx));
     EI_CHECK(cudaGetLastError());
     ctx.launches++;
     return 0;
@@ -1054,7 +1229,11 @@ int block_move(uint8_t* data, const Pass& p, ExecContext& ctx) {
 // ---- dispatch ------------------------------------------------------------------
 template <int US, template <typename> class FnT, typename Make32, typename Make64, typename Own32, typename Own64>
 int run_col(uint8_t* data, const Pass& p, ExecContext& ctx, Make32 m32, Make64 m64, Own32 o32, Own64 o64) {
-    const Staging st = plan_col_pass(p, smem_cap_of(ctx.caps));
+    const Staging st = plan_col_pass(p, ctx.caps);
+    if (st.owner && st.group) {
+        if (fits32(p)) return launch_col_group<US>(data, p, st, o32(p), ctx);
+        return launch_col_group<US>(data, p, st, o64(p), ctx);
+    }
     if (st.owner) {
         if (fits32(p)) return launch_col_owner<US>(data, p, st, o32(p), ctx);
         return launch_col_owner<US>(data, p, st, o64(p), ctx);
@@ -1126,7 +1305,8 @@ int run_pass_u(uint8_t* data, const Pass& p, ExecContext& ctx) {
     return EITHOT_STATUS_INVALID;
 }
 
-uint64_t pass_unit(const uint8_t* data, const Pass& p, size_t smem_cap) {
+uint64_t pass_unit(const uint8_t* data, const Pass& p, const DeviceCaps& caps) {
+    const size_t smem_cap = smem_cap_of(caps);
     const uint64_t addr = reinterpret_cast<uintptr_t>(data) + p.offset;
     switch (p.type) {
         case kSlabTranspose:
@@ -1137,7 +1317,7 @@ uint64_t pass_unit(const uint8_t* data, const Pass& p, size_t smem_cap) {
             return unit_for({addr, p.elem, st.w, p.elem % st.w == 0 ? st.w : p.elem % st.w});
         }
         case kColGather: {
-            const Staging st = plan_col_pass(p, smem_cap);
+            const Staging st = plan_col_pass(p, caps);
             return unit_for({addr, p.elem, st.w, st.pitch, p.elem % st.w == 0 ? st.w : p.elem % st.w});
         }
         case kBlockMove:
@@ -1158,8 +1338,9 @@ size_t pass_workspace_bytes(const Pass& p, const DeviceCaps& caps) {
             return st.on_chip ? 0 : p.cols * st.w;
         }
         case kColGather: {
-            const Staging st = plan_col_pass(p, cap);
-            return st.on_chip ? 0 : p.rows * st.tw * st.w;
+            const Staging st = plan_col_pass(p, caps);
+            if (st.on_chip) return st.group ? kGroupSyncBytes : 0;
+            return p.rows * st.tw * st.w;
         }
         case kBlockMove: {
             // scratch is needed only where a block's shift is smaller than
@@ -1184,8 +1365,8 @@ size_t pass_workspace_ideal(const Pass& p, const DeviceCaps& caps) {
             return p.batches * p.rows * ns * p.cols * st.w;
         }
         case kColGather: {
-            const Staging st = plan_col_pass(p, cap);
-            if (st.on_chip) return 0;
+            const Staging st = plan_col_pass(p, caps);
+            if (st.on_chip) return st.group ? kGroupSyncBytes : 0;
             const uint64_t ns = (p.elem + st.w - 1) / st.w;
             const uint64_t nt = (p.cols + st.tw - 1) / st.tw;
             return p.batches * nt * ns * p.rows * st.tw * st.w;
@@ -1198,7 +1379,6 @@ size_t pass_workspace_ideal(const Pass& p, const DeviceCaps& caps) {
 }
 
 int run_passes(uint8_t* data, const std::vector<Pass>& passes, ExecContext& ctx) {
-    const size_t cap = smem_cap_of(ctx.caps);
     // Profiling appends one event before the first pass and one after each
     // pass to the caller's pool; pass k spans events (first + k, first + k + 1).
     size_t ev = ctx.profile ? ctx.events_used : 0;
@@ -1216,7 +1396,7 @@ int run_passes(uint8_t* data, const std::vector<Pass>& passes, ExecContext& ctx)
         if (int rc = record()) return rc;
     }
     for (const Pass& p : passes) {
-        const uint64_t U = pass_unit(data, p, cap);
+        const uint64_t U = pass_unit(data, p, ctx.caps);
         int rc;
         switch (U) {
             case 16: rc = run_pass_u<16>(data, p, ctx); break;
@@ -1281,6 +1461,31 @@ int read_index_faults(unsigned int* out) {
     if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_index_faults, &zero, sizeof(zero));
     *out = v;
     return e == cudaSuccess ? 0 : EITHOT_STATUS_CUDA;
+}
+
+int read_sync_timeouts(unsigned int* out) {
+    unsigned int v = 0, zero = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(&v, g_sync_timeouts, sizeof(v));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_sync_timeouts, &zero, sizeof(zero));
+    *out = v;
+    return e == cudaSuccess ? 0 : EITHOT_STATUS_CUDA;
+}
+
+int run_wait_selftest(unsigned int* timeouts, std::string* err) {
+    unsigned int pending = 0;  // timeouts of earlier launches are cleared, not reported here
+    if (read_sync_timeouts(&pending)) { *err = "reading the sync-timeout counter failed"; return EITHOT_STATUS_CUDA; }
+    unsigned* flags = nullptr;
+    cudaError_t e = cudaMalloc(&flags, 2 * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(flags, 0, 2 * sizeof(unsigned));
+    if (e == cudaSuccess) {
+        k_wait_selftest<<<1, 32>>>(flags);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (flags) cudaFree(flags);
+    if (e != cudaSuccess) { *err = cudaGetErrorString(e); return EITHOT_STATUS_CUDA; }
+    if (read_sync_timeouts(timeouts)) { *err = "reading the sync-timeout counter failed"; return EITHOT_STATUS_CUDA; }
+    return 0;
 }
 
 bool query_caps(int device, DeviceCaps* caps, std::string* err) {

@@ -179,20 +179,51 @@ void owner_halo(int fn, uint64_t b, uint64_t tw, uint64_t* lo, uint64_t* hi) {
 }
 
 namespace {
-// Owner-computed column staging: the cluster's CTAs split the tile's rows,
-// each staging its share plus halo; writes read only the CTA's own shared
-// memory, so the cluster size costs only its barrier.
-Staging plan_col_owner(uint64_t rows, uint64_t E, int fn, uint64_t b, size_t cap) {
-    Staging s;
-    for (uint64_t occ_limit : {kTwoPerSm, static_cast<uint64_t>(cap)}) {
-        for (uint64_t tb : {uint64_t(128), uint64_t(64), uint64_t(32)}) {
-            if (tuning().col_chunk && tb != static_cast<uint64_t>(tuning().col_chunk)) continue;
-            uint64_t w, tw;
-            if (E <= tb) { w = E; tw = std::max<uint64_t>(1, tb / E); }
-            else { w = tb; tw = 1; }
-            const uint64_t pitch = tw * w;
-            uint64_t lo, hi;
-            owner_halo(fn, b, tw, &lo, &hi);
+// Relative DRAM efficiency of moving row pieces of `piece` contiguous bytes
+// scattered over rows (measured on GB300, read + write of 2.6 GB: 32 B 1.8
+// TB/s, 64 B 2.9-3.4, 128 B 5.1, 256 B and up 6.6 = a streaming copy).
+double piece_efficiency(uint64_t piece) {
+    if (piece >= 256) return 1.0;
+    if (piece >= 128) return 0.77;
+    if (piece >= 64) return 0.47;
+    return 0.28;
+}
+
+// Fraction of the SMs that clusters of K CTAs keep busy (clusters must fit
+// a GPC; GB300 runs 14 clusters of 16 two-per-SM CTAs, 112 of 152 SMs).
+double cluster_utilisation(int K) {
+    if (K >= 16) return 0.74;
+    if (K >= 8) return 0.95;
+    return 1.0;
+}
+
+// Owner-computed column staging.  Each CTA stages Q consecutive slots of
+// the tile plus the halo and writes whole output row pieces from its own
+// shared memory; the tile's CTAs need only a barrier between their loads
+// and their writes, a thread-block cluster's (K <= 16) or, for tiles too
+// large for a cluster, a global-memory barrier over a group of G
+// co-resident CTAs.  Candidates are costed by row-piece efficiency, SM
+// utilisation, halo re-reads and buffering.
+Staging plan_col_owner(uint64_t rows, uint64_t E, int fn, uint64_t b, const DeviceCaps& caps) {
+    const size_t cap = smem_cap_of(caps);
+    const int form = tuning().col_form;
+    Staging best;
+    best.on_chip = false;
+    best.cost = 1e30;
+    auto consider = [&](const Staging& s) {
+        if (s.cost < best.cost) best = s;
+    };
+    for (uint64_t tb : {uint64_t(512), uint64_t(256), uint64_t(128), uint64_t(64), uint64_t(32)}) {
+        if (tuning().col_chunk && tb != static_cast<uint64_t>(tuning().col_chunk)) continue;
+        uint64_t w, tw;
+        if (E <= tb) { w = E; tw = std::max<uint64_t>(1, tb / E); }
+        else { w = tb; tw = 1; }
+        const uint64_t pitch = tw * w;
+        uint64_t lo, hi;
+        owner_halo(fn, b, tw, &lo, &hi);
+        const double eff = piece_efficiency(pitch);
+        // thread-block clusters
+        if (form != 2) {
             for (int K : kClusterSizes) {
                 if (K > tuning().max_cluster) break;
                 const uint64_t Q = (rows + K - 1) / K;
@@ -200,30 +231,58 @@ Staging plan_col_owner(uint64_t rows, uint64_t E, int fn, uint64_t b, size_t cap
                 for (bool db : {true, false}) {
                     if (db && !tuning().dbuf) continue;
                     const uint64_t foot = per * (db ? 2 : 1);
-                    if (foot > cap || foot > occ_limit) continue;
+                    if (foot > cap) continue;
+                    Staging s;
                     s.w = w; s.tw = tw; s.pitch = pitch; s.K = K; s.per_cta = per;
                     s.item_bytes = rows * pitch; s.on_chip = true; s.dbuf = db;
                     s.owner = true; s.hlo = lo; s.hhi = hi;
-                    // halo rows are read twice; a barrier per item per doubling of K
-                    s.cost = 1.0 + 0.5 * static_cast<double>((lo + hi) * K) / static_cast<double>(rows) +
-                             0.03 * log2i(K) + (tb < 128 ? 0.1 : 0.0) + (db ? 0.0 : 0.1) +
-                             (foot > kTwoPerSm ? kOnePerSmPenalty : 0.0);
-                    return s;
+                    s.per_sm = foot <= kTwoPerSm ? 2 : 1;
+                    s.cost = 1.0 / (eff * cluster_utilisation(K)) +
+                             0.5 * static_cast<double>((lo + hi) * K) / static_cast<double>(rows) +
+                             0.03 * log2i(K) + (db ? 0.0 : 0.1) + (s.per_sm == 1 && !db ? kOnePerSmPenalty : 0.0);
+                    consider(s);
+                    break;  // double buffering preferred when it fits
+                }
+            }
+        }
+        // groups of co-resident CTAs
+        if (form != 1) {
+            for (int per_sm : {2, 1}) {
+                for (bool db : {true, false}) {
+                    if (db && !tuning().dbuf) continue;
+                    const uint64_t budget = (per_sm == 2 ? kTwoPerSm : cap) / (db ? 2 : 1);
+                    if (budget / pitch <= lo + hi) continue;
+                    const uint64_t qmax = budget / pitch - lo - hi;
+                    const uint64_t slots = static_cast<uint64_t>(per_sm) * caps.sms;
+                    const uint64_t gmin = (rows + qmax - 1) / qmax;
+                    if (gmin > slots) continue;
+                    const uint64_t ngroups = slots / gmin;
+                    uint64_t G = std::min<uint64_t>(slots / ngroups, rows);
+                    const uint64_t Q = (rows + G - 1) / G;
+                    G = (rows + Q - 1) / Q;  // CTAs that own at least one slot
+                    Staging s;
+                    s.w = w; s.tw = tw; s.pitch = pitch; s.K = 1; s.G = static_cast<int>(G);
+                    s.per_cta = (Q + lo + hi) * pitch;
+                    s.item_bytes = rows * pitch; s.on_chip = true; s.dbuf = db;
+                    s.owner = true; s.group = true; s.hlo = lo; s.hhi = hi; s.per_sm = per_sm;
+                    const double util = static_cast<double>(ngroups * G) / static_cast<double>(slots);
+                    s.cost = 1.0 / (eff * util) + 0.5 * static_cast<double>((lo + hi) * G) / static_cast<double>(rows) +
+                             (G > 1 ? 0.08 : 0.0) + (db ? 0.0 : 0.1) + (per_sm == 1 && !db ? kOnePerSmPenalty : 0.0);
+                    consider(s);
                 }
             }
         }
     }
-    s.on_chip = false;
-    return s;
+    return best;
 }
 }  // namespace
 
-Staging plan_col_pass(const Pass& p, size_t cap) {
+Staging plan_col_pass(const Pass& p, const DeviceCaps& caps) {
     if (tuning().col_owner) {
-        const Staging s = plan_col_owner(p.rows, p.elem, p.fn, p.b, cap);
+        const Staging s = plan_col_owner(p.rows, p.elem, p.fn, p.b, caps);
         if (s.on_chip) return s;
     }
-    return plan_col_staging(p.rows, p.elem, cap);
+    return plan_col_staging(p.rows, p.elem, smem_cap_of(caps));
 }
 
 Xpose xpose_of(const LowOp& op, uint64_t elem, uint64_t n_sub, uint64_t base_offset) {
@@ -247,10 +306,10 @@ namespace {
 double row_cost(uint64_t cols, uint64_t E, size_t cap, bool scatter) {
     return plan_row_staging(cols, E, cap, scatter).cost;
 }
-double col_cost(uint64_t rows, uint64_t E, int fn, uint64_t b, size_t cap) {
+double col_cost(uint64_t rows, uint64_t E, int fn, uint64_t b, const DeviceCaps& caps) {
     Pass p;
     p.rows = rows; p.elem = E; p.fn = fn; p.b = b;
-    return plan_col_pass(p, cap).cost;
+    return plan_col_pass(p, caps).cost;
 }
 
 std::string geom(const char* name, uint64_t B, uint64_t r, uint64_t c, uint64_t E) {
@@ -281,10 +340,10 @@ void lower_xpose(const Xpose& x, const DeviceCaps& caps, std::vector<Pass>* pass
     // Catanzaro: c2r on the R x C view, or r2c on the C x R view.
     uint64_t g, inv;
     gcd_inverse(x.R, x.C, &g, &inv);
-    const double c2r = (g > 1 ? col_cost(x.R, x.E, kFnC2RPreRot, x.C / g, cap) : 0.0) + row_cost(x.C, x.E, cap, false) +
-                       col_cost(x.R, x.E, kFnC2RColShuffle, x.C / g, cap);
-    const double r2c = col_cost(x.C, x.E, kFnR2CColShuffle, x.R / g, cap) + row_cost(x.R, x.E, cap, true) +
-                       (g > 1 ? col_cost(x.C, x.E, kFnR2CPostRot, x.R / g, cap) : 0.0);
+    const double c2r = (g > 1 ? col_cost(x.R, x.E, kFnC2RPreRot, x.C / g, caps) : 0.0) + row_cost(x.C, x.E, cap, false) +
+                       col_cost(x.R, x.E, kFnC2RColShuffle, x.C / g, caps);
+    const double r2c = col_cost(x.C, x.E, kFnR2CColShuffle, x.R / g, caps) + row_cost(x.R, x.E, cap, true) +
+                       (g > 1 ? col_cost(x.C, x.E, kFnR2CPostRot, x.R / g, caps) : 0.0);
     bool use_c2r = (c2r < r2c) || (c2r == r2c && x.C >= x.R);
     if (tuning().variant == 1) use_c2r = true;
     if (tuning().variant == 2) use_c2r = false;

@@ -72,6 +72,7 @@ struct Tuning {
     int col_batch = 4;     // remote loads in flight per thread in column passes (4 or 8)
     int col_chunk = 0;     // 0: cost model; 32/64/128: bytes per staged row piece of column passes
     int col_owner = 1;     // column passes: 1 owner-computed writes, 0 gathers through distributed smem
+    int col_form = 0;      // owner-computed column passes: 0 cost model, 1 clusters, 2 CTA groups
 };
 Tuning& tuning();
 
@@ -91,6 +92,9 @@ struct Staging {
     bool on_chip = false;  // the item fits the cluster's distributed shared memory
     bool owner = false;    // column pass run owner-computed (each CTA writes from its own rows)
     uint64_t hlo = 0, hhi = 0;  // owner-computed: halo rows staged below / above the owned ones
+    bool group = false;    // owner-computed over a group of G co-resident CTAs (global-memory
+    int G = 0;             //   barrier, any size) instead of a thread-block cluster
+    int per_sm = 1;        // CTAs per SM the footprint was sized for
     double cost = 0;       // modelled time in units of one streaming pass
 };
 
@@ -105,7 +109,11 @@ void owner_halo(int fn, uint64_t b, uint64_t tw, uint64_t* lo, uint64_t* hi);
 
 // Staging of column pass `p` (fn, rows, elem, b): owner-computed when the
 // tuning allows and the tile fits on chip, else plan_col_staging's.
-Staging plan_col_pass(const Pass& p, size_t smem_cap);
+Staging plan_col_pass(const Pass& p, const DeviceCaps& caps);
+
+// Bytes at the start of the workspace that group-synchronised passes use
+// for their barrier counters.
+constexpr size_t kGroupSyncBytes = 4096;
 
 // Lowers every step of `plan` for element size `elem` into passes.
 bool lower_plan(const NdPlan& plan, uint64_t elem, const DeviceCaps& caps,

@@ -164,9 +164,11 @@ int eithot_estimate(int rank, const int64_t* dims, const int* perm_1based,
  *   "max_cluster" largest thread-block cluster (1, 2, 4, 8, 16)
  *   "variant"     0 cost model, 1 force c2r, 2 force r2c for 2D transposes
  *   "col_batch"   remote loads in flight per thread in column passes (4, 8)
- *   "col_chunk"   0 cost model, or 32/64/128 bytes per staged column-row piece
+ *   "col_chunk"   0 cost model, or 32/64/128/256/512 bytes per staged column-row piece
  *   "col_owner"   1 column passes write from the rows each CTA staged itself,
- *                 0 gather through distributed shared memory */
+ *                 0 gather through distributed shared memory
+ *   "col_form"    owner-computed column passes: 0 cost model, 1 thread-block
+ *                 clusters only, 2 groups of co-resident CTAs only */
 int eithot_tune_set(const char* key, double value);
 int eithot_tune_get(const char* key, double* value);
 
@@ -189,6 +191,19 @@ int eithot_profile_get(int i, char* name, size_t name_len, double* ms, double* b
  * dereferenced) and counted.  Returns and clears the count; synchronises
  * the device. */
 int eithot_index_faults(unsigned int* count);
+
+/* Column passes whose tiles exceed a thread-block cluster synchronise a
+ * group of co-resident CTAs through a barrier in global memory.  Every wait
+ * on it is bounded (about half a second); a CTA that gives up aborts the
+ * launch's remaining writes and is counted here, and the call's output is
+ * then invalid.  Returns and clears the count; synchronises the device. */
+int eithot_sync_timeouts(unsigned int* count);
+
+/* Runs one bounded wait that nothing releases (a single 32-thread block
+ * waiting on a zeroed counter) and reports the timeouts it counted: 1 when
+ * the wait gave up as designed.  Allocates 8 bytes; synchronises the device;
+ * the context stays usable. */
+int eithot_selftest_wait(unsigned int* timeouts);
 
 /* ---- misc ------------------------------------------------------------- */
 const char* eithot_last_error(void);

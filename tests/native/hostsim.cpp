@@ -4,6 +4,7 @@
 // index-map chain on the CPU; the device kernels are checked separately by
 // the GPU tests.  Never loaded by the product.
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -115,6 +116,35 @@ int hs_describe(char* buf, size_t len, int rank, const int64_t* dims, const int*
     if (!lower_plan(plan, elem, caps, &passes, &g_err)) return -1;
     std::string s;
     for (const Pass& p : passes) s += p.what + "\n";
+    std::strncpy(buf, s.c_str(), len);
+    if (len) buf[len - 1] = 0;
+    return static_cast<int>(passes.size());
+}
+
+// One line per pass: its description and, for column passes, the staging
+// the executor will use (form, CTAs per tile, row-piece bytes, buffering).
+int hs_describe_staging(char* buf, size_t len, int rank, const int64_t* dims, const int* perm, size_t elem,
+                        int nb, double alpha, int order) {
+    NdPlan plan;
+    if (!make_nd_plan(rank, dims, perm, nb, alpha, order, &plan, &g_err)) return -1;
+    std::vector<Pass> passes;
+    DeviceCaps caps;
+    if (!lower_plan(plan, elem, caps, &passes, &g_err)) return -1;
+    std::string s;
+    for (const Pass& p : passes) {
+        s += p.what;
+        if (p.type == kColGather) {
+            const Staging st = plan_col_pass(p, caps);
+            char tmp[256];
+            std::snprintf(tmp, sizeof(tmp), " | %s K=%d G=%d piece=%llu dbuf=%d per_cta=%llu halo=%llu+%llu cost=%.3f",
+                          !st.on_chip ? "staged" : st.group ? "group" : st.owner ? "cluster-owner" : "cluster-gather",
+                          st.K, st.G, static_cast<unsigned long long>(st.pitch), st.dbuf ? 1 : 0,
+                          static_cast<unsigned long long>(st.per_cta), static_cast<unsigned long long>(st.hlo),
+                          static_cast<unsigned long long>(st.hhi), st.cost);
+            s += tmp;
+        }
+        s += "\n";
+    }
     std::strncpy(buf, s.c_str(), len);
     if (len) buf[len - 1] = 0;
     return static_cast<int>(passes.size());

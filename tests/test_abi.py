@@ -36,6 +36,7 @@ def test_errors_do_not_exit(E):
 
 
 def test_workspace_sizes_host_only(E):
-    assert E.workspace_size([3001, 4096], [2, 1], 4) == 0
+    # on-chip passes need at most the group barrier's counters
+    assert E.workspace_size([3001, 4096], [2, 1], 4) <= 4096
     ws = E.workspace_size([4, 20011, 8192, 2], [1, 3, 2, 4], 4)
     assert 0 <= ws <= 0.0101 * 4 * 20011 * 8192 * 8

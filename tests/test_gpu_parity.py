@@ -31,6 +31,7 @@ def run_case(E, dims, perm, elem, nb=1, alpha=0.01, order=0, slack=1.0, seed=1, 
     E.transpose_ptr(buf.data_ptr() + offset, cap, dims, perm, elem, nb, alpha, order, s.cuda_stream)
     s.synchronize()
     assert E.index_faults() == 0
+    assert E.sync_timeouts() == 0
     got = buf[offset:offset + n * elem].cpu().numpy()
     want = oracle.permute(host, dims, perm, elem)
     if not np.array_equal(got, want):
@@ -85,7 +86,7 @@ def test_catanzaro_2d(E, R, C, elem):
 
 @pytest.fixture
 def tuned(E):
-    keys = ("variant", "col_owner", "col_chunk", "max_cluster", "dbuf")
+    keys = ("variant", "col_owner", "col_chunk", "max_cluster", "dbuf", "col_form")
     saved = {k: E.tune_get(k) for k in keys}
 
     def set_(**kw):
@@ -100,25 +101,37 @@ def tuned(E):
                                       (70000, 5, 8), (5000, 60, 16), (40, 2000, 24), (1000, 999, 1),
                                       (2048, 1536, 32)])
 @pytest.mark.parametrize("variant", [1, 2])
-@pytest.mark.parametrize("owner", [0, 1])
-def test_column_kernels_both_forms(E, tuned, R, C, elem, variant, owner):
-    """c2r and r2c, each with owner-computed column passes and with column
-    gathers through distributed shared memory, on shapes with gcd 1 and
-    gcd > 1 (rotations), rows fewer than a tile's halo and wide elements."""
-    tuned(variant=variant, col_owner=owner)
+@pytest.mark.parametrize("form", ["gather", "cluster", "group"])
+def test_column_kernels_all_forms(E, tuned, R, C, elem, variant, form):
+    """c2r and r2c, with column gathers through distributed shared memory and
+    with owner-computed column passes synchronised by a cluster or by a
+    group of co-resident CTAs, on shapes with gcd 1 and gcd > 1
+    (rotations), rows fewer than a tile's halo and wide elements."""
+    tuned(variant=variant, col_owner=0 if form == "gather" else 1,
+          col_form={"gather": 0, "cluster": 1, "group": 2}[form])
     run_case(E, [C, R], [2, 1], elem)
 
 
-@pytest.mark.parametrize("chunk,max_cluster,dbuf", [(32, 16, 1), (64, 8, 1), (128, 4, 0), (64, 2, 1), (32, 1, 0)])
-def test_column_tilings(E, tuned, chunk, max_cluster, dbuf):
-    """Row-piece widths, cluster sizes and single/double buffering of the
-    column passes (the autotuner's search space)."""
-    tuned(col_chunk=chunk, max_cluster=max_cluster, dbuf=dbuf)
+@pytest.mark.parametrize("chunk,max_cluster,dbuf,form", [(32, 16, 1, 1), (64, 8, 1, 1), (128, 4, 0, 1), (64, 2, 1, 1),
+                                                         (32, 1, 0, 1), (128, 16, 1, 2), (256, 16, 1, 2),
+                                                         (512, 16, 0, 2), (256, 8, 1, 0), (512, 16, 1, 0)])
+def test_column_tilings(E, tuned, chunk, max_cluster, dbuf, form):
+    """Row-piece widths, cluster sizes, CTA groups and single/double
+    buffering of the column passes (the autotuner's search space)."""
+    tuned(col_chunk=chunk, max_cluster=max_cluster, dbuf=dbuf, col_form=form)
     for variant in (1, 2):
         E.tune_set("variant", variant)
         run_case(E, [4096, 3001], [2, 1], 4)
         run_case(E, [4, 20011, 819, 2], [1, 3, 2, 4], 4)
         run_case(E, [4000, 6000], [2, 1], 2)
+
+
+def test_bounded_wait_gives_up(E):
+    """A group-barrier wait that nothing releases gives up after its bound,
+    is counted, and leaves the context usable."""
+    assert E.selftest_wait() == 1
+    assert E.sync_timeouts() == 0
+    run_case(E, [4096, 3001], [2, 1], 4)
 
 
 @pytest.mark.parametrize("dims,perm", [([60000, 300], [2, 1]), ([300, 60000], [2, 1]),

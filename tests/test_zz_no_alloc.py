@@ -57,6 +57,7 @@ def test_noalloc_matches_allocating_entry_point(E, dims, perm, elem, nb, alpha):
         assert rc == E.OK, E.lib.eithot_last_error().decode()
         stream.synchronize()
         assert E.index_faults() == 0
+        assert E.sync_timeouts() == 0
         assert torch.equal(a[:n * elem], b[:n * elem])
     # and the first call alone matches the oracle
     c = torch.zeros(cap, dtype=torch.uint8, device=dev)
