@@ -238,7 +238,7 @@ def selftest_wait() -> int:
 
 def tune_set(key: str, value: float) -> None:
     """Process-wide lowering knob ("dbuf", "max_cluster", "variant", "col_batch", "col_chunk",
-    "col_owner", "col_form")."""
+    "col_owner", "col_form", "row_prefetch")."""
     _check(lib.eithot_tune_set(key.encode(), float(value)))
 
 

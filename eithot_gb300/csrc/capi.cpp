@@ -89,6 +89,8 @@ int eithot_tune_set(const char* key, double value) {
         t.col_batch = value >= 8 ? 8 : 4;
     } else if (k == "col_owner") {
         t.col_owner = value != 0.0 ? 1 : 0;
+    } else if (k == "row_prefetch") {
+        t.row_prefetch = value != 0.0 ? 1 : 0;
     } else if (k == "col_form") {
         const int v = static_cast<int>(value);
         if (v < 0 || v > 2) return fail(EITHOT_EINVAL, "col_form must be 0, 1 or 2");
@@ -120,6 +122,7 @@ int eithot_tune_get(const char* key, double* value) {
     else if (k == "col_batch") *value = t.col_batch;
     else if (k == "col_owner") *value = t.col_owner;
     else if (k == "col_form") *value = t.col_form;
+    else if (k == "row_prefetch") *value = t.row_prefetch;
     else if (k == "col_chunk") *value = t.col_chunk;
     else if (k == "max_cluster") *value = t.max_cluster;
     else if (k == "variant") *value = t.variant;

@@ -293,6 +293,62 @@ __global__ void __launch_bounds__(kThreads) k_row_cluster(RowArgs a, Fn fn) {
 }
 
 // ---------------------------------------------------------------------------
+// Row pass for rows that fill one CTA's shared memory (one CTA per SM, no
+// room for a second item buffer): the next item is prefetched into
+// registers (kRegs units of US bytes per thread, up to 128 KB per CTA)
+// while the current item is gathered out of shared memory, so HBM reads
+// overlap the write-back.  Gather form only (out[i][j] = in[i][fn(i,j)]).
+// ---------------------------------------------------------------------------
+template <int US, typename Fn, int kRegs>
+__global__ void __launch_bounds__(kThreads) k_row_solo(RowArgs a, Fn fn) {
+    using U = typename UnitOf<US>::T;
+    using I = typename Fn::index_type;
+    extern __shared__ __align__(16) uint8_t smem[];
+    // flat items only (w == E): unit x of a row is bytes [x*US, (x+1)*US)
+    const uint32_t units = a.cols * a.upw;
+    U v[kRegs];
+    auto fetch = [&](uint64_t it) {
+        const U* row = reinterpret_cast<const U*>(a.base + it * a.row_bytes) + threadIdx.x;
+#pragma unroll
+        for (int q = 0; q < kRegs; ++q)
+            if (threadIdx.x + q * kThreads < units) v[q] = row[q * kThreads];
+    };
+    if (blockIdx.x < a.items) fetch(blockIdx.x);
+    for (uint64_t it = blockIdx.x; it < a.items; it += gridDim.x) {
+        U* st = reinterpret_cast<U*>(smem) + threadIdx.x;
+#pragma unroll
+        for (int q = 0; q < kRegs; ++q)
+            if (threadIdx.x + q * kThreads < units) st[q * kThreads] = v[q];
+        __syncthreads();  // the item is in shared memory
+        const uint64_t nxt = it + gridDim.x;
+        if (nxt < a.items) fetch(nxt);  // in flight during the write-back below
+        const I i = static_cast<I>(a.div_rows.mod(it));
+        U* row = reinterpret_cast<U*>(a.base + it * a.row_bytes);
+        const U* sm = reinterpret_cast<const U*>(smem);
+        for (uint32_t x0 = threadIdx.x; x0 < units; x0 += kBatch * kThreads) {
+            U w[kBatch];
+            uint32_t dst[kBatch];
+#pragma unroll
+            for (int q = 0; q < kBatch; ++q) {
+                dst[q] = ~0u;
+                const uint32_t x = x0 + q * kThreads;
+                if (x >= units) continue;
+                uint32_t j, u;
+                a.div_upw.divmod(x, j, u);
+                const I src = fn(i, static_cast<I>(j));
+                if (!in_range(src, a.cols)) continue;
+                w[q] = sm[static_cast<uint32_t>(src) * a.upw + u];
+                dst[q] = x;
+            }
+#pragma unroll
+            for (int q = 0; q < kBatch; ++q)
+                if (dst[q] != ~0u) row[dst[q]] = w[q];
+        }
+        __syncthreads();  // shared memory is free for the next item
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Column pass staged in a K-CTA cluster: item = one strip of a tile of tw
 // adjacent columns over all rows; CTA k owns rows [k*Q, (k+1)*Q).  When the
 // tw*upw units of a staged row divide the block, every thread keeps one
@@ -925,6 +981,10 @@ int launch_slab(uint8_t* data, const Pass& p, ExecContext& ctx) {
 }
 
 // ---- rows ------------------------------------------------------------------
+// Rows larger than this leave no room for a second CTA or item buffer on
+// the SM; they prefetch the next row into registers instead.
+constexpr size_t kRowSoloMinBytes = 110 * 1024;
+
 template <int US, typename Fn, bool kScatter>
 int launch_row_staged(uint8_t* data, const Pass& p, const Staging& st, ExecContext& ctx, const Fn& fn);
 
@@ -953,6 +1013,20 @@ int launch_row(uint8_t* data, const Pass& p, const FnOnChip& fn, const Fn64& fn6
     a.buf_bytes = static_cast<uint32_t>((static_cast<uint64_t>(a.P) * st.w + 127) / 128 * 128);
     a.dbuf = st.dbuf;
     const size_t smem = (st.dbuf ? 2 : 1) * static_cast<size_t>(a.buf_bytes);
+    constexpr int kRegs = 256 / US;  // 64 registers of prefetched data per thread
+    if constexpr (US >= 4 && !kScatter) {
+        const uint64_t units = static_cast<uint64_t>(a.cols) * a.upw;
+        if (st.K == 1 && !st.dbuf && a.flat && a.nstrips == 1 && smem > kRowSoloMinBytes &&
+            units <= static_cast<uint64_t>(kRegs) * kThreads && tuning().row_prefetch) {
+            const void* k = reinterpret_cast<const void*>(&k_row_solo<US, FnOnChip, kRegs>);
+            EI_CHECK(prep_smem(k, smem));
+            const int grid = grid_for(k, smem, a.items, ctx);
+            k_row_solo<US, FnOnChip, kRegs><<<grid, kThreads, smem, ctx.stream>>>(a, fn);
+            EI_CHECK(cudaGetLastError());
+            ctx.launches++;
+            return 0;
+        }
+    }
     EI_CHECK(launch_clusters(k_row_cluster<US, FnOnChip, kScatter>, st.K, smem, a.items, ctx, a, fn));
     EI_CHECK(cudaGetLastError());
     ctx.launches++;

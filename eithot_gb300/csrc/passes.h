@@ -73,6 +73,7 @@ struct Tuning {
     int col_chunk = 0;     // 0: cost model; 32/64/128: bytes per staged row piece of column passes
     int col_owner = 1;     // column passes: 1 owner-computed writes, 0 gathers through distributed smem
     int col_form = 0;      // owner-computed column passes: 0 cost model, 1 clusters, 2 CTA groups
+    int row_prefetch = 1;  // rows filling a CTA: prefetch the next row into registers
 };
 Tuning& tuning();
 

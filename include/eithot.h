@@ -168,7 +168,9 @@ int eithot_estimate(int rank, const int64_t* dims, const int* perm_1based,
  *   "col_owner"   1 column passes write from the rows each CTA staged itself,
  *                 0 gather through distributed shared memory
  *   "col_form"    owner-computed column passes: 0 cost model, 1 thread-block
- *                 clusters only, 2 groups of co-resident CTAs only */
+ *                 clusters only, 2 groups of co-resident CTAs only
+ *   "row_prefetch" 1 rows that fill a CTA prefetch the next row into
+ *                 registers during the write-back, 0 no prefetch */
 int eithot_tune_set(const char* key, double value);
 int eithot_tune_get(const char* key, double* value);
 

@@ -86,7 +86,7 @@ def test_catanzaro_2d(E, R, C, elem):
 
 @pytest.fixture
 def tuned(E):
-    keys = ("variant", "col_owner", "col_chunk", "max_cluster", "dbuf", "col_form")
+    keys = ("variant", "col_owner", "col_chunk", "max_cluster", "dbuf", "col_form", "row_prefetch")
     saved = {k: E.tune_get(k) for k in keys}
 
     def set_(**kw):
@@ -124,6 +124,18 @@ def test_column_tilings(E, tuned, chunk, max_cluster, dbuf, form):
         run_case(E, [4096, 3001], [2, 1], 4)
         run_case(E, [4, 20011, 819, 2], [1, 3, 2, 4], 4)
         run_case(E, [4000, 6000], [2, 1], 2)
+
+
+@pytest.mark.parametrize("dims,perm,elem", [([4, 3001, 8192, 1], [1, 3, 2, 4], 4), ([2, 3001, 16384, 1], [1, 3, 2, 4], 4),
+                                            ([3001, 32768], [2, 1], 4), ([3001, 30000], [2, 1], 4),
+                                            ([777, 14000], [2, 1], 8), ([4, 4001, 7000, 2], [1, 3, 2, 4], 4)])
+@pytest.mark.parametrize("prefetch", [0, 1])
+def test_row_prefetch(E, tuned, dims, perm, elem, prefetch):
+    """Rows of 110-128 KB (one CTA per SM) with and without the register
+    prefetch of the next row, including rows that leave some threads'
+    last units empty."""
+    tuned(variant=2, row_prefetch=prefetch)
+    run_case(E, dims, perm, elem)
 
 
 def test_bounded_wait_gives_up(E):
