@@ -636,14 +636,19 @@ __global__ void __launch_bounds__(kThreads) k_col_owner(ColOwnArgs a, Own own) {
 struct GroupSync {
     unsigned* counters;  // nG arrival counters, then the abort flag
     unsigned G, nG;
+    unsigned sleep_ns;   // back-off between polls
+    bool relaxed;        // arrive without release semantics (the arriving CTA's loads have completed)
 };
 
 __device__ unsigned g_sync_timeouts;
 
-constexpr uint32_t kSpinLimit = 1u << 20;  // ~0.5 s of polling at ~0.5 us per poll
+constexpr uint32_t kSpinLimit = 1u << 20;  // at least ~0.5 s of polling (each poll is an L2 round trip)
 
-__device__ __forceinline__ void group_arrive(unsigned* ctr) {
-    asm volatile("red.release.gpu.global.add.u32 [%0], 1;\n" ::"l"(ctr) : "memory");
+__device__ __forceinline__ void group_arrive(unsigned* ctr, bool relaxed) {
+    if (relaxed)
+        asm volatile("red.relaxed.gpu.global.add.u32 [%0], 1;\n" ::"l"(ctr) : "memory");
+    else
+        asm volatile("red.release.gpu.global.add.u32 [%0], 1;\n" ::"l"(ctr) : "memory");
 }
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
@@ -653,12 +658,13 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
 }
 
 // Thread 0 waits until *ctr >= target; false when it gave up or the launch
-// was aborted.  Called by thread 0 only.
-__device__ bool group_wait(const unsigned* ctr, unsigned target, unsigned* abort_flag) {
+// was aborted.  (A fence after relaxed polls would also wait for the CTA's
+// own prefetches in flight; acquire loads do not.)
+__device__ bool group_wait(const unsigned* ctr, unsigned target, unsigned* abort_flag, unsigned sleep_ns) {
     for (uint32_t it = 0; it < kSpinLimit; ++it) {
         if (ld_acquire(ctr) >= target) return true;
         if ((it & 31) == 31 && ld_acquire(abort_flag) != 0) return false;
-        __nanosleep(256);
+        if (sleep_ns) __nanosleep(sleep_ns);
     }
     atomicAdd(&g_sync_timeouts, 1u);
     atomicExch(abort_flag, 1u);
@@ -692,11 +698,11 @@ __global__ void __launch_bounds__(kThreads) k_col_group(ColOwnArgs a, Own own, G
         if (!a.dbuf) own_stage_in<US, Own, kLanes>(a, own, smem, it, x0, nstage, lc, lu, ii0, step);
         if constexpr (US >= 4) asm volatile("cp.async.wait_group 0;\n" ::: "memory");
         __syncthreads();  // this CTA's slots of the item are in shared memory
-        if (threadIdx.x == 0 && gs.G > 1) group_arrive(ctr);
+        if (threadIdx.x == 0 && gs.G > 1) group_arrive(ctr, gs.relaxed);
         const uint64_t nxt = it + gs.nG;
         if (a.dbuf && nxt < a.items)
             own_stage_in<US, Own, kLanes>(a, own, smem + (boff ^ a.buf_bytes), nxt, x0, nstage, lc, lu, ii0, step);
-        if (threadIdx.x == 0) s_ok = gs.G <= 1 || group_wait(ctr, (k + 1) * gs.G, abort_flag);
+        if (threadIdx.x == 0) s_ok = gs.G <= 1 || group_wait(ctr, (k + 1) * gs.G, abort_flag, gs.sleep_ns);
         __syncthreads();  // every CTA of the group holds its slots: writes may start
         if (!s_ok) break;
         const OwnItem ci = own_item(a, it);
@@ -737,7 +743,7 @@ __global__ void __launch_bounds__(kThreads) k_col_group(ColOwnArgs a, Own own, G
 // Launch-time self-test of the bounded wait: one CTA waits on a counter
 // that nothing increments and must give up, counting one sync timeout.
 __global__ void k_wait_selftest(unsigned* counters) {
-    if (threadIdx.x == 0) group_wait(counters, 1u, counters + 1);
+    if (threadIdx.x == 0) group_wait(counters, 1u, counters + 1, 256);
 }
 
 // ---------------------------------------------------------------------------
@@ -1223,6 +1229,8 @@ int launch_col_group(uint8_t* data, const Pass& p, const Staging& st, const Own&
     gs.counters = reinterpret_cast<unsigned*>(ctx.scratch);
     gs.G = static_cast<unsigned>(st.G);
     gs.nG = 0;
+    gs.sleep_ns = static_cast<unsigned>(tuning().sync_sleep_ns);
+    gs.relaxed = tuning().sync_relaxed != 0;
     const unsigned max_groups = static_cast<unsigned>(kGroupSyncBytes / sizeof(unsigned)) - 1;
     EI_CHECK(cudaMemsetAsync(ctx.scratch, 0, kGroupSyncBytes, ctx.stream));  // counters and abort flag
     if (kThreads % a.RU != 0)

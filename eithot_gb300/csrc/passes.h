@@ -74,6 +74,9 @@ struct Tuning {
     int col_owner = 1;     // column passes: 1 owner-computed writes, 0 gathers through distributed smem
     int col_form = 0;      // owner-computed column passes: 0 cost model, 1 clusters, 2 CTA groups
     int row_prefetch = 1;  // rows filling a CTA: prefetch the next row into registers
+    int sync_sleep_ns = 64;  // group barriers: back-off between polls
+    int sync_relaxed = 0;    // group barriers: arrive without release semantics
+    int group_per_sm = 0;    // group form: 0 cost model, 1 or 2 CTAs per SM
 };
 Tuning& tuning();
 

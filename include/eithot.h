@@ -170,7 +170,10 @@ int eithot_estimate(int rank, const int64_t* dims, const int* perm_1based,
  *   "col_form"    owner-computed column passes: 0 cost model, 1 thread-block
  *                 clusters only, 2 groups of co-resident CTAs only
  *   "row_prefetch" 1 rows that fill a CTA prefetch the next row into
- *                 registers during the write-back, 0 no prefetch */
+ *                 registers during the write-back, 0 no prefetch
+ *   "sync_sleep_ns" back-off between polls of a group barrier (0..100000)
+ *   "sync_relaxed" 1 group-barrier arrivals without release semantics
+ *   "group_per_sm" group form: 0 cost model, 1..4 resident CTAs per SM */
 int eithot_tune_set(const char* key, double value);
 int eithot_tune_get(const char* key, double* value);
 
