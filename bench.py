@@ -47,7 +47,7 @@ WORKLOAD = "in-place 4D transpose (4,20011,8192,2) int32 perm (1 3 2 4), nb/alph
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="eithot", choices=["eithot", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=8)
@@ -215,40 +215,55 @@ def end_to_end(args, E, buf, nbytes, cap, nb, alpha, dev, world):
     host_out = [torch.empty(nbytes, dtype=torch.uint8, pin_memory=True) for _ in range(2)]
     dbuf = [buf, torch.empty(cap, dtype=torch.uint8, device=dev)]
     h2d, comp, d2h = (torch.cuda.Stream(dev) for _ in range(3))
-    steps = max(2, args.e2e_steps)
-    freed = [None, None]  # event: buffer k%2's previous D2H done
-    torch.cuda.synchronize(dev)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
     main = torch.cuda.current_stream(dev)
-    e0.record(main)
-    for st in (h2d, comp, d2h):
-        st.wait_stream(main)
-    for k in range(steps):
-        b = k % 2
-        with torch.cuda.stream(h2d):
-            if freed[b] is not None:
-                h2d.wait_event(freed[b])
-            dbuf[b][: nbytes].copy_(host_in, non_blocking=True)
-            loaded = torch.cuda.Event()
-            loaded.record(h2d)
-        comp.wait_event(loaded)
-        E.transpose_ptr(dbuf[b].data_ptr(), cap, DIMS, PERM, ELEM, nb, alpha, E.ORDER_MIXED, comp.cuda_stream)
-        done = torch.cuda.Event()
-        done.record(comp)
-        with torch.cuda.stream(d2h):
-            d2h.wait_event(done)
-            host_out[b].copy_(dbuf[b][: nbytes], non_blocking=True)
-            freed[b] = torch.cuda.Event()
-            freed[b].record(d2h)
-    for st in (h2d, comp, d2h):
-        main.wait_stream(st)
-    e1.record(main)
+
+    def run(steps):
+        freed = [None, None]  # event: buffer k%2's previous D2H done
+        for st in (h2d, comp, d2h):
+            st.wait_stream(main)
+        for k in range(steps):
+            b = k % 2
+            with torch.cuda.stream(h2d):
+                if freed[b] is not None:
+                    h2d.wait_event(freed[b])
+                dbuf[b][: nbytes].copy_(host_in, non_blocking=True)
+                loaded = torch.cuda.Event()
+                loaded.record(h2d)
+            comp.wait_event(loaded)
+            E.transpose_ptr(dbuf[b].data_ptr(), cap, DIMS, PERM, ELEM, nb, alpha, E.ORDER_MIXED, comp.cuda_stream)
+            done = torch.cuda.Event()
+            done.record(comp)
+            with torch.cuda.stream(d2h):
+                d2h.wait_event(done)
+                host_out[b].copy_(dbuf[b][: nbytes], non_blocking=True)
+                freed[b] = torch.cuda.Event()
+                freed[b].record(d2h)
+        for st in (h2d, comp, d2h):
+            main.wait_stream(st)
+
+    # untimed passes over both buffers: the first DMAs into or out of
+    # freshly pinned host pages run several times slower than later ones
+    for h in host_out:
+        h.fill_(0)
+    run(4)
     torch.cuda.synchronize(dev)
-    ms = e0.elapsed_time(e1) / steps
+    # host DMA on this machine stalls now and then for 0.1-0.2 s; the
+    # median of three timed runs keeps one stall from deciding the figure
+    steps = max(2, args.e2e_steps)
+    runs = []
+    for _ in range(3):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(main)
+        run(steps)
+        e1.record(main)
+        torch.cuda.synchronize(dev)
+        runs.append(e0.elapsed_time(e1) / steps)
+    ms = statistics.median(runs)
     del dbuf[1]
     return {"value": world * 2.0 * nbytes / (ms / 1e3) / 1e9, "unit": "GB/s", "h2d_bytes_per_step": nbytes,
             "d2h_bytes_per_step": nbytes, "ms_per_step": ms, "steps": steps,
+            "runs_ms_per_step": [round(r, 3) for r in runs],
             "pipeline": "2 device buffers; H2D, transpose and D2H of consecutive steps overlap"}
 
 
