@@ -72,6 +72,10 @@ def _load():
     lib.eithot_profile_get.argtypes = [ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t,
                                        ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
     lib.eithot_last_stats.argtypes = [ctypes.POINTER(_Stats)]
+    lib.eithot_fill_hash.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_size_t, ctypes.c_uint64, ctypes.c_int64,
+                                     ctypes.c_void_p]
+    lib.eithot_check_hash.argtypes = [ctypes.c_void_p, ctypes.c_int, I64P, IP, ctypes.c_size_t, ctypes.c_uint64,
+                                      ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_int64)]
     lib.eithot_tune_set.argtypes = [ctypes.c_char_p, ctypes.c_double]
     lib.eithot_tune_get.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double)]
     return lib
@@ -218,6 +222,24 @@ def index_faults() -> int:
     v = ctypes.c_uint()
     _check(lib.eithot_index_faults(ctypes.byref(v)))
     return v.value
+
+
+def fill_hash_ptr(ptr: int, n_elems: int, elem_size: int, seed: int, first_index: int = 0,
+                  stream: Optional[int] = None) -> None:
+    """Writes the counter-hash sequence (elements first_index ..) to device
+    memory at `ptr` (see eithot_fill_hash)."""
+    _check(lib.eithot_fill_hash(ctypes.c_void_p(ptr), n_elems, elem_size, seed & (2**64 - 1), first_index,
+                                ctypes.c_void_p(stream) if stream else None))
+
+
+def check_hash_ptr(ptr: int, dims, perm, elem_size: int, seed: int, stream: Optional[int] = None):
+    """(mismatches, first bad output index or -1) of the permutation (dims,
+    perm) of a counter-hash tensor at `ptr`; synchronises the stream."""
+    r, d, p = _arrays(dims, perm)
+    bad, first = ctypes.c_uint64(), ctypes.c_int64()
+    _check(lib.eithot_check_hash(ctypes.c_void_p(ptr), r, d, p, elem_size, seed & (2**64 - 1),
+                                 ctypes.c_void_p(stream) if stream else None, ctypes.byref(bad), ctypes.byref(first)))
+    return bad.value, first.value
 
 
 def sync_timeouts() -> int:

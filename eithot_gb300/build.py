@@ -22,7 +22,7 @@ LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libeithot.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["kernels.cu"]
+CU_SOURCES = ["kernels.cu", "checks.cu"]
 CPP_SOURCES = ["plan.cpp", "lower.cpp", "estimator.cpp", "capi.cpp"]
 
 

@@ -180,6 +180,28 @@ int eithot_index_faults(unsigned int* count) {
     return EITHOT_OK;
 }
 
+int eithot_fill_hash(void* d_data, int64_t n_elems, size_t elem_size, uint64_t seed, int64_t first_index,
+                     void* stream) {
+    if (!d_data && n_elems > 0) return fail(EITHOT_EINVAL, "null data");
+    if (elem_size < 1 || elem_size > 64) return fail(EITHOT_EINVAL, "element size must be 1..64 bytes");
+    if (n_elems < 0 || first_index < 0) return fail(EITHOT_EINVAL, "negative count or index");
+    std::string err;
+    if (int rc = eithot::fill_hash(d_data, n_elems, elem_size, seed, first_index, static_cast<cudaStream_t>(stream), &err))
+        return fail(rc, err);
+    return EITHOT_OK;
+}
+
+int eithot_check_hash(const void* d_data, int rank, const int64_t* dims, const int* perm_1based, size_t elem_size,
+                      uint64_t seed, void* stream, uint64_t* mismatches, int64_t* first_bad) {
+    if (!d_data || !dims || !perm_1based || !mismatches || !first_bad) return fail(EITHOT_EINVAL, "null argument");
+    if (elem_size < 1 || elem_size > 64) return fail(EITHOT_EINVAL, "element size must be 1..64 bytes");
+    std::string err;
+    if (int rc = eithot::check_hash(d_data, rank, dims, perm_1based, elem_size, seed, static_cast<cudaStream_t>(stream),
+                                    mismatches, first_bad, &err))
+        return fail(rc, err);
+    return EITHOT_OK;
+}
+
 int eithot_sync_timeouts(unsigned int* count) {
     if (!count) return fail(EITHOT_EINVAL, "null count");
     if (eithot::read_sync_timeouts(count)) return fail(EITHOT_ECUDA, "reading the sync-timeout counter failed");

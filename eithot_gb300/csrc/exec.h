@@ -62,6 +62,11 @@ int noalloc_scratch(uint8_t** ptr, std::string* err);
 // last read (the kernels skip such accesses).  Synchronises the device.
 int read_index_faults(unsigned int* out);
 
+// Counter-hash content and its permutation check (checks.cu).
+int fill_hash(void* d, int64_t n, size_t elem, uint64_t seed, int64_t first, cudaStream_t s, std::string* err);
+int check_hash(const void* d, int rank, const int64_t* dims, const int* perm1, size_t elem, uint64_t seed,
+               cudaStream_t s, uint64_t* mismatches, int64_t* first_bad, std::string* err);
+
 // Returns and clears the number of bounded group-barrier waits that gave up
 // (their launch aborted its writes); synchronises the device.
 int read_sync_timeouts(unsigned int* out);

@@ -210,6 +210,25 @@ int eithot_sync_timeouts(unsigned int* count);
  * the context stays usable. */
 int eithot_selftest_wait(unsigned int* timeouts);
 
+/* ---- content generator and permutation check ---------------------------
+ * No reference counterpart (the reference fills host iota data and compares
+ * host copies, ITNT/src/tensor_util.cpp:54-56, :113-142, which a 100 GB
+ * tensor cannot afford).  Element i of a generated tensor holds the low
+ * elem_size bytes of splitmix64's finaliser applied to
+ * seed ^ (i * 0xD1B54A32D192ED03) (byte k of a wider element is byte k mod 8
+ * of that value).  eithot_fill_hash writes elements first_index ..
+ * first_index + n_elems - 1 of that sequence to d_data, stream-ordered.
+ * eithot_check_hash checks that d_data holds the permutation (dims, perm)
+ * of such a tensor (generated with first_index 0): output element o must
+ * hold the value of the source element its output coordinates name.  It
+ * synchronises `stream` and returns the number of mismatching elements and
+ * the first mismatching output index (-1 if none).  Calls of
+ * eithot_check_hash that overlap on the GPU share one result slot. */
+int eithot_fill_hash(void* d_data, int64_t n_elems, size_t elem_size, uint64_t seed, int64_t first_index,
+                     void* stream);
+int eithot_check_hash(const void* d_data, int rank, const int64_t* dims, const int* perm_1based,
+                      size_t elem_size, uint64_t seed, void* stream, uint64_t* mismatches, int64_t* first_bad);
+
 /* ---- misc ------------------------------------------------------------- */
 const char* eithot_last_error(void);
 int eithot_last_stats(eithot_stats* out);

@@ -225,3 +225,55 @@ def test_config2_full_size(E):
     n = math.prod(dims)
     assert st["workspace_bytes"] <= alpha * n * 4 * 1.0001
     assert st["free_before"] - st["free_after_alloc"] <= alpha * n * 4 * 1.05 + (64 << 20)
+
+
+def test_device_hash_fill_and_check(E):
+    """The device content generator writes exactly the oracle's counter-hash
+    bytes; the device permutation check accepts the transposed tensor and
+    pinpoints a planted corruption."""
+    dims, perm = [37, 64, 5, 3], [3, 1, 4, 2]
+    n = math.prod(dims)
+    for elem in (1, 2, 4, 8, 6):
+        buf = torch.zeros(n * elem + 64, dtype=torch.uint8, device=dev())
+        E.fill_hash_ptr(buf.data_ptr(), n, elem, 0x1234 + elem)
+        torch.cuda.synchronize()
+        host = oracle.fill_hash(n, elem, 0x1234 + elem)
+        assert np.array_equal(buf[: n * elem].cpu().numpy(), host)
+        assert E.check_hash_ptr(buf.data_ptr(), dims, [1, 2, 3, 4], elem, 0x1234 + elem) == (0, -1)
+        E.transpose_ptr(buf.data_ptr(), n * elem + 64, dims, perm, elem)
+        torch.cuda.synchronize()
+        assert np.array_equal(buf[: n * elem].cpu().numpy(), oracle.permute(host, dims, perm, elem))
+        assert E.check_hash_ptr(buf.data_ptr(), dims, perm, elem, 0x1234 + elem) == (0, -1)
+        buf[777 * elem] ^= 1
+        assert E.check_hash_ptr(buf.data_ptr(), dims, perm, elem, 0x1234 + elem) == (1, 777)
+
+
+@pytest.mark.slow
+def test_config3_full_size_uint16(E):
+    """(16, 3001, 1024, 256, 4) uint16 (100.7 GB), perm (5 3 1 4 2), nb/alpha
+    from the estimator at alpha 0.05: the tensor no 32-bit planner can
+    describe.  Every output element is checked on the device against the
+    counter hash of the source index its coordinates name; a seeded sample
+    is checked on the host with the oracle's index map."""
+    dims, perm, elem, seed = [16, 3001, 1024, 256, 4], [5, 3, 1, 4, 2], 2, 0xC3
+    n = math.prod(dims)
+    nb, alpha, _ = E.estimate(dims, perm, elem, 1, 0.05)
+    plan = E.plan(dims, perm, nb, alpha)
+    cap = plan.padded_volume * elem
+    free, _ = torch.cuda.mem_get_info()
+    if free < cap * 1.08:
+        pytest.skip("needs %.0f GB of free device memory" % (cap * 1.08 / 1e9))
+    buf = torch.empty(cap, dtype=torch.uint8, device=dev())
+    E.fill_hash_ptr(buf.data_ptr(), n, elem, seed)
+    E.transpose_ptr(buf.data_ptr(), cap, dims, perm, elem, nb, alpha)
+    torch.cuda.synchronize()
+    st = E.last_stats()
+    assert E.index_faults() == 0 and E.sync_timeouts() == 0
+    assert st["workspace_bytes"] <= 0.05 * n * elem
+    assert E.check_hash_ptr(buf.data_ptr(), dims, perm, elem, seed) == (0, -1)
+    rng = np.random.default_rng(3)
+    src = rng.integers(0, n, size=2000)
+    dst = torch.tensor([oracle.dest_index(dims, perm, int(s)) for s in src], device=dev())
+    got = buf[: n * elem].view(torch.int16)[dst].cpu().numpy().view(np.uint16)
+    want = np.array([oracle.hash_value(seed, int(s)) & 0xFFFF for s in src], dtype=np.uint16)
+    assert np.array_equal(got, want)
