@@ -44,10 +44,10 @@ size_t choose_workspace(const std::vector<eithot::Pass>& passes, const eithot::D
     }
     if (lo == 0) return 0;
     const double cap = alpha * bytes;
-    size_t ws = ideal;
-    if (static_cast<double>(ws) > cap) ws = static_cast<size_t>(cap);
-    ws = std::max(ws, lo);
-    return (ws + 255) / 256 * 256;
+    size_t ws = (ideal + 255) / 256 * 256;
+    // under the cap: round down to 256 bytes, never below the minimum
+    if (static_cast<double>(ws) > cap) ws = static_cast<size_t>(cap) / 256 * 256;
+    return std::max(ws, (lo + 255) / 256 * 256);
 }
 
 int device_caps(eithot::DeviceCaps* caps) {
