@@ -4,7 +4,9 @@
 
 Host C++ is compiled by g++, CUDA by nvcc (one -gencode, sm_103a), in
 parallel; the library links the CUDA runtime statically and carries no torch
-dependency.  Objects go to eithot_gb300/_build/.
+dependency.  Objects go to eithot_gb300/_build/.  The drop-in replacements of
+the reference's command-line programs (test_inplace, Nd_estimation) are
+linked against the library into eithot_gb300/bin/.
 """
 from __future__ import annotations
 
@@ -20,6 +22,9 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libeithot.so")
+CLIDIR = os.path.join(PKG, "cli")
+BINDIR = os.path.join(PKG, "bin")
+CLI_PROGRAMS = {"test_inplace": "test_inplace.cpp", "Nd_estimation": "nd_estimation.cpp"}
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["kernels.cu", "checks.cu"]
@@ -79,6 +84,18 @@ def build(verbose: bool = False, force: bool = False) -> str:
                 print(out)
     if force or _stale(LIB, objs):
         _run([nvcc] + ARCH + ["-shared", "-Xcompiler", "-fPIC", "-o", LIB] + objs)
+    os.makedirs(BINDIR, exist_ok=True)
+    cli_jobs = []
+    for name, src in CLI_PROGRAMS.items():
+        s = os.path.join(CLIDIR, src)
+        b = os.path.join(BINDIR, name)
+        if force or _stale(b, [s, LIB, os.path.join(ROOT, "include", "eithot.h")]):
+            cli_jobs.append([nvcc, "-O2", "-std=c++17", "-Xcompiler", "-pthread"] + inc +
+                            [s, "-o", b, "-L", LIBDIR, "-leithot", "-Xlinker", "-rpath", "-Xlinker", "$ORIGIN/../_lib"])
+    with cf.ThreadPoolExecutor(max_workers=2) as ex:
+        for out in ex.map(_run, cli_jobs):
+            if verbose and out.strip():
+                print(out)
     return LIB
 
 

@@ -421,15 +421,15 @@ int eithot_transpose(void* d_data, size_t capacity_bytes, int rank, const int64_
                                num_sub_tensors, alpha, EITHOT_ORDER_MIXED, nullptr, 0, stream);
 }
 
-int eithot_estimate(int rank, const int64_t* dims, const int* perm_1based, size_t elem_size,
-                    int num_sub_tensors, double alpha, size_t smem_per_block, int padding_blocks,
-                    int* nb_out, double* alpha_out, size_t* extra_bytes_out) {
-    (void)num_sub_tensors;  // the reference estimator ignores the requested nb
+namespace {
+int run_estimate(int rank, const int64_t* dims, const int* perm_1based, size_t elem_size, double alpha,
+                 size_t smem_per_block, int padding_blocks, eithot::Estimate* est) {
     eithot::NdPlan plan;
     std::string err;
     if (!eithot::make_nd_plan(rank, dims, perm_1based, 1, alpha, EITHOT_ORDER_MIXED, &plan, &err))
         return fail(EITHOT_EINVAL, err);
     if (!elem_ok(elem_size)) return fail(EITHOT_EINVAL, "elem_size must be in [1, 64] bytes");
+    if (!(alpha > 0.0)) return fail(EITHOT_EINVAL, "alpha must be positive");
     if (smem_per_block == 0 || padding_blocks <= 0) {
         int dev = 0, v = 0, sms = 152;
         size_t smem = 49152;
@@ -442,13 +442,39 @@ int eithot_estimate(int rank, const int64_t* dims, const int* perm_1based, size_
         if (smem_per_block == 0) smem_per_block = smem;
         if (padding_blocks <= 0) padding_blocks = 2 * sms;
     }
-    eithot::Estimate est;
     std::vector<int64_t> d(dims, dims + rank);
     std::vector<int> p(perm_1based, perm_1based + rank);
-    eithot::estimate(d, p, elem_size, alpha, smem_per_block, static_cast<uint64_t>(padding_blocks), &est);
+    eithot::estimate(d, p, elem_size, alpha, smem_per_block, static_cast<uint64_t>(padding_blocks), est);
+    return EITHOT_OK;
+}
+}  // namespace
+
+int eithot_estimate(int rank, const int64_t* dims, const int* perm_1based, size_t elem_size,
+                    int num_sub_tensors, double alpha, size_t smem_per_block, int padding_blocks,
+                    int* nb_out, double* alpha_out, size_t* extra_bytes_out) {
+    (void)num_sub_tensors;  // the reference estimator ignores the requested nb
+    eithot::Estimate est;
+    if (int rc = run_estimate(rank, dims, perm_1based, elem_size, alpha, smem_per_block, padding_blocks, &est))
+        return rc;
     if (nb_out) *nb_out = est.nb;
     if (alpha_out) *alpha_out = est.alpha;
     if (extra_bytes_out) *extra_bytes_out = est.final_tmp;
+    return EITHOT_OK;
+}
+
+int eithot_estimate_report(int rank, const int64_t* dims, const int* perm_1based, size_t elem_size, double alpha,
+                           size_t smem_per_block, int padding_blocks, eithot_estimate_info* info) {
+    if (!info) return fail(EITHOT_EINVAL, "null info");
+    eithot::Estimate est;
+    if (int rc = run_estimate(rank, dims, perm_1based, elem_size, alpha, smem_per_block, padding_blocks, &est))
+        return rc;
+    info->nb = est.nb;
+    info->alpha = est.alpha;
+    info->init_extra_bytes = est.init_tmp;
+    info->alpha_raised = est.alpha_raised;
+    info->decomposed = est.decomposed ? 1 : 0;
+    info->final_extra_bytes = est.final_tmp;
+    info->final_ratio = est.ratio;
     return EITHOT_OK;
 }
 

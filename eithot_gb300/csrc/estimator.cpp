@@ -123,12 +123,14 @@ bool estimate(const std::vector<int64_t>& dims, const std::vector<int>& perm, ui
     int nb = percent <= 0 ? 1 : static_cast<int>(std::pow(2.0, std::ceil(std::log2(static_cast<double>(percent)))));
     if (nb == 0) nb = 1;
     if (transpose_tmp > 0) alpha = std::max(alpha, 1.0 / std::sqrt(static_cast<double>(vol) / 32.0));
+    out->alpha_raised = alpha;
     const int64_t large = static_cast<int64_t>(32.0 / alpha);
     if (!(dims[maxpos] > large && nb > 1)) {
         out->nb = nb;
         out->alpha = std::ceil(alpha * 100.0) / 100.0;
         out->final_tmp = transpose_tmp;
         out->decomposed = false;
+        out->ratio = static_cast<double>(transpose_tmp) / static_cast<double>(data_size);
         return true;
     }
     const bool pad = dims[maxpos] % nb != 0;
@@ -176,6 +178,7 @@ bool estimate(const std::vector<int64_t>& dims, const std::vector<int>& perm, ui
     out->alpha = alpha;
     out->final_tmp = final_tmp;
     out->decomposed = true;
+    out->ratio = ratio;
     return true;
 }
 

@@ -11,6 +11,8 @@ struct Estimate {
     uint64_t init_tmp = 0;   // max temp over the rounds of the undivided tensor
     uint64_t final_tmp = 0;  // modelled extra bytes for the chosen nb
     bool decomposed = false;
+    double alpha_raised = 0.0;  // alpha after the 1/sqrt(vol/32) floor (printed as "new ratio")
+    double ratio = 0.0;         // final_tmp / bytes as printed (rounded up to 0.01 when nb was searched)
 };
 
 // perm is 1-based.  smem_per_block: the reference's default shared memory per

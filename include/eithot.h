@@ -157,6 +157,23 @@ int eithot_estimate(int rank, const int64_t* dims, const int* perm_1based,
                     size_t smem_per_block, int padding_blocks,
                     int* nb_out, double* alpha_out, size_t* extra_bytes_out);
 
+/* Everything the reference estimator program prints for one request
+ * (Nd_memory_estimation/src/test_inplace.cpp:36-44, :61-77, :116-132), for
+ * drop-in replacements of that program.  Arguments as eithot_estimate. */
+typedef struct eithot_estimate_info {
+    int     nb;                  /* sub-tensor count written to proper_input.txt */
+    double  alpha;               /* alpha written to proper_input.txt */
+    size_t  init_extra_bytes;    /* "init Extra Memory size" */
+    double  alpha_raised;        /* "new ratio" (printed when init_extra_bytes > 0) */
+    int     decomposed;          /* 1: the sub-tensor branch ran ("Final Extra Memory Size" line) */
+    size_t  final_extra_bytes;   /* "Final Extra Memory Size" */
+    double  final_ratio;         /* "take ... percent input data size" */
+} eithot_estimate_info;
+
+int eithot_estimate_report(int rank, const int64_t* dims, const int* perm_1based,
+                           size_t elem_size, double alpha, size_t smem_per_block,
+                           int padding_blocks, eithot_estimate_info* info);
+
 /* ---- tuning ----------------------------------------------------------------
  * No reference counterpart (the reference fixes its kernel choices at
  * compile time).  Process-wide knobs of the lowering, used by the autotuner:

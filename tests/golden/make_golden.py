@@ -48,10 +48,13 @@ def ref_estimate(dims, perm, elem, nb, alpha):
         if proc.returncode != 0:
             return {"crash": proc.returncode}
         out = proc.stdout
+        with open(os.path.join(d, "proper_input.txt")) as f:
+            proper = f.read()
     lines = out.strip().splitlines()
     init = lines[0].split("=")[1].split()[0]
     last = lines[-1].split()
-    return {"init_extra_mb": init, "nb_out": int(last[-2]), "alpha_out": last[-1]}
+    return {"init_extra_mb": init, "nb_out": int(last[-2]), "alpha_out": last[-1], "stdout": out,
+            "proper_input": proper}
 
 
 def ref_seqtt(arr, dims, perm, elem):

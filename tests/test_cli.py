@@ -1,0 +1,86 @@
+"""The drop-in replacements of the reference's command-line programs
+(eithot_gb300/bin/Nd_estimation and eithot_gb300/bin/test_inplace): same
+argv, same stdout lines, same files appended in the working directory."""
+import json
+import os
+import subprocess
+
+import pytest
+
+from conftest import ROOT
+
+BIN = os.path.join(ROOT, "eithot_gb300", "bin")
+
+
+def run(prog, args, cwd, env=None):
+    exe = os.path.join(BIN, prog)
+    assert os.path.exists(exe), "%s is not built (run __graft_entry__.build())" % exe
+    return subprocess.run([exe] + [str(a) for a in args], cwd=cwd, capture_output=True, text=True, timeout=600,
+                          env=env)
+
+
+def test_nd_estimation_matches_reference_output(E, tmp_path):
+    """Every case the reference estimator ran without crashing: identical
+    stdout and identical proper_input.txt line (the reference was run with
+    48 KiB of shared memory per block and 304 padding blocks, the values
+    of a GB300 and of this program when no GPU is present)."""
+    cases = json.load(open(os.path.join(ROOT, "tests", "golden", "estimates_ref.json")))["cases"]
+    checked = 0
+    for c in cases:
+        if "crash" in c:
+            continue
+        d = tmp_path / ("c%d" % checked)
+        d.mkdir()
+        p = run("Nd_estimation", c["dims"] + c["perm"] + [c["elem"], c["nb"], c["alpha"]], d)
+        assert p.returncode == 0, p.stderr
+        assert p.stdout == c["stdout"], (c["dims"], c["perm"], c["elem"], c["alpha"])
+        assert (d / "proper_input.txt").read_text() == c["proper_input"]
+        checked += 1
+    assert checked >= 150
+
+
+def test_nd_estimation_appends(E, tmp_path):
+    for _ in range(2):
+        assert run("Nd_estimation", [3001, 4096, 2, 1, 4, 1, 0.01], tmp_path).returncode == 0
+    assert (tmp_path / "proper_input.txt").read_text() == "3001 4096 2 1 4 1 0.01\n" * 2
+
+
+def test_nd_estimation_beyond_reference_limits(E, tmp_path):
+    """The 100.7 GB uint16 tensor the reference estimator asserts on
+    (UPPER_BOUND_VOLUME 22e9) gets an estimate."""
+    p = run("Nd_estimation", [16, 3001, 1024, 256, 4, 5, 3, 1, 4, 2, 2, 1, 0.05], tmp_path)
+    assert p.returncode == 0, p.stderr
+    assert p.stdout.splitlines()[-1].startswith("\t16 3001 1024 256 4 5 3 1 4 2 2 ")
+
+
+def test_cli_usage_errors(E, tmp_path):
+    for prog in ("Nd_estimation", "test_inplace"):
+        p = run(prog, [3001, 4096, 2, 1], tmp_path)
+        assert p.returncode == 2 and "usage" in p.stderr
+    # the reference rejects element sizes below 4 it cannot move; 3 is invalid here too
+    p = run("test_inplace", [30, 40, 2, 1, 3, 1, 0.01], tmp_path)
+    assert p.returncode == 0 and p.stdout == "Invalid rank or type size\n"
+    assert not (tmp_path / "inplace_bench.txt").exists()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("args", [
+    [3001, 4096, 2, 1, 4, 1, 0.01],                   # first BASELINE config
+    [7249, 50, 2, 1, 4, 4, 0.02],                      # sub-tensors with padding
+    [33, 17, 9, 2, 3, 1, 8, 1, 0.01],                  # 64-bit elements
+    [16, 3001, 64, 3, 1, 2, 2, 1, 0.05],               # 16-bit elements (beyond the reference)
+    [6, 4, 3401, 3, 2, 1, 1, 2, 0.01]])                # 8-bit elements, sub-tensors
+def test_test_inplace_runs_and_verifies(E, tmp_path, args):
+    p = run("test_inplace", args, tmp_path)
+    assert p.returncode == 0, p.stdout + p.stderr
+    lines = p.stdout.splitlines()
+    rank = (len(args) - 3) // 2
+    assert lines[0].startswith("%dD Inplace " % rank) and lines[0].endswith(" transpose")
+    assert lines[1] == "number of sub_tensors = %d" % args[2 * rank + 1]
+    assert lines[2].startswith("Dims = " + " ".join(str(a) for a in args[:rank]) + ", Data size = ")
+    assert lines[3:5] == ["Inplace transpose verify_inplace", "Correct transpose"]
+    assert lines[5].startswith("Execution Time without h2d2h: ") and lines[6].startswith("Execution Time: ")
+    t = float(lines[6].split(": ")[1].rstrip("ms"))
+    assert (tmp_path / "inplace_bench.txt").read_text() == "%.5f\n" % t
+    thr = float((tmp_path / "inplace_bench_throughput.txt").read_text())
+    assert thr > 0
