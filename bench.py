@@ -170,6 +170,23 @@ def cpu_baseline(threads=0, budget_s=10.0):
                       "(1/16 of the workload, 328 MB), median of %d runs" % len(times)}
 
 
+def max_over_ranks(x: float, device) -> float:
+    """The largest of every rank's x (identity without a process group)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_gbs(bytes_per_rank: int, ms_per_step: float, world: int) -> float:
+    """Whole-job effective GB/s: every rank moves 2 * bytes per step; the
+    step time is the slowest rank's."""
+    return world * 2.0 * bytes_per_rank / (ms_per_step / 1e3) / 1e9
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -191,7 +208,7 @@ def run_reference(args):
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "i32", "data": "synthetic (seeded counter-hash int32, generated on the device)",
+        "scaling": "weak", "vs_baseline": None, "dtype": "i32", "data": "synthetic (seeded counter-hash int32, generated on the host)",
         "config": {"workload": WORKLOAD, "sample": "dims (4,20011,512,2), 1/16 of the workload", "dims": DIMS,
                    "perm": PERM, "elem_bytes": ELEM},
         "cpu_baseline": {"value": value, "unit": "GB/s", "cores": cores, "kind": "port",
@@ -259,9 +276,9 @@ def end_to_end(args, E, buf, nbytes, cap, nb, alpha, dev, world):
         e1.record(main)
         torch.cuda.synchronize(dev)
         runs.append(e0.elapsed_time(e1) / steps)
-    ms = statistics.median(runs)
+    ms = max_over_ranks(statistics.median(runs), dev)
     del dbuf[1]
-    return {"value": world * 2.0 * nbytes / (ms / 1e3) / 1e9, "unit": "GB/s", "h2d_bytes_per_step": nbytes,
+    return {"value": job_gbs(nbytes, ms, world), "unit": "GB/s", "h2d_bytes_per_step": nbytes,
             "d2h_bytes_per_step": nbytes, "ms_per_step": ms, "steps": steps,
             "runs_ms_per_step": [round(r, 3) for r in runs],
             "pipeline": "2 device buffers; H2D, transpose and D2H of consecutive steps overlap"}
@@ -334,13 +351,9 @@ def run_eithot(args):
         d["n"] += 1
     E.set_profiling(False)
     E.profile_reset()
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, dev)
     ms_per_step = total_ms / args.steps
-    value = world * 2.0 * nbytes / (ms_per_step / 1e3) / 1e9
+    value = job_gbs(nbytes, ms_per_step, world)
 
     # end-to-end through the C ABI from pinned host memory
     e2e = None
