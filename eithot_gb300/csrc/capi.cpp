@@ -98,6 +98,10 @@ int eithot_tune_set(const char* key, double value) {
         t.group_per_sm = v;
     } else if (k == "sync_relaxed") {
         t.sync_relaxed = value != 0.0 ? 1 : 0;
+    } else if (k == "slab_pack") {
+        t.slab_pack = value != 0.0 ? 1 : 0;
+    } else if (k == "row_block") {
+        t.row_block = value != 0.0 ? 1 : 0;
     } else if (k == "row_prefetch") {
         t.row_prefetch = value != 0.0 ? 1 : 0;
     } else if (k == "col_form") {
@@ -132,6 +136,8 @@ int eithot_tune_get(const char* key, double* value) {
     else if (k == "col_owner") *value = t.col_owner;
     else if (k == "col_form") *value = t.col_form;
     else if (k == "row_prefetch") *value = t.row_prefetch;
+    else if (k == "row_block") *value = t.row_block;
+    else if (k == "slab_pack") *value = t.slab_pack;
     else if (k == "sync_sleep_ns") *value = t.sync_sleep_ns;
     else if (k == "sync_relaxed") *value = t.sync_relaxed;
     else if (k == "group_per_sm") *value = t.group_per_sm;

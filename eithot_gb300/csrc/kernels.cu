@@ -156,6 +156,42 @@ __global__ void __launch_bounds__(kThreads) k_slab(SlabArgs a) {
     }
 }
 
+// Small matrices (a few KB or less): an item is a block of k consecutive
+// matrices, loaded contiguously; every output element reads its input in
+// shared memory.  Millions of 3x5 matrices would otherwise take one CTA item
+// each.  Whole elements only.
+struct SlabPackArgs {
+    uint8_t* base;
+    uint64_t batches, items, mat_bytes, E;
+    uint32_t k, R, C, upw, mat_units;
+    FastDiv32 div_mat_units, div_upw, div_R;
+};
+
+template <int US>
+__global__ void __launch_bounds__(kThreads) k_slab_pack(SlabPackArgs a) {
+    using U = typename UnitOf<US>::T;
+    extern __shared__ __align__(16) uint8_t smem[];
+    for (uint64_t it = blockIdx.x; it < a.items; it += gridDim.x) {
+        const uint64_t m0 = it * a.k;
+        const uint64_t left = a.batches - m0;
+        const uint32_t nm = static_cast<uint32_t>(left < a.k ? left : a.k);
+        uint8_t* blk = a.base + m0 * a.mat_bytes;
+        const uint32_t units = nm * a.mat_units;
+        for (uint32_t x = threadIdx.x; x < units; x += blockDim.x) copy_in<US, U>(smem + x * US, blk + x * US);
+        copy_in_wait<US>();
+        __syncthreads();
+        for (uint32_t x = threadIdx.x; x < units; x += blockDim.x) {
+            uint32_t m, rest, o, u, c, r;
+            a.div_mat_units.divmod(x, m, rest);
+            a.div_upw.divmod(rest, o, u);
+            a.div_R.divmod(o, c, r);  // output o = c*R + r holds input (r, c)
+            const uint32_t src = m * a.mat_units + (r * a.C + c) * a.upw + u;
+            *reinterpret_cast<U*>(blk + static_cast<uint64_t>(x) * US) = *reinterpret_cast<const U*>(smem + src * US);
+        }
+        __syncthreads();
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Row pass staged in the distributed shared memory of a K-CTA cluster: item
 // = one strip of one row; CTA k of the cluster owns pieces [k*P, (k+1)*P).
@@ -289,6 +325,61 @@ __global__ void __launch_bounds__(kThreads) k_row_cluster(RowArgs a, Fn fn) {
                 if (dst[q]) *reinterpret_cast<U*>(dst[q]) = v[q];
         }
         cluster_sync_reuse();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Row pass for short rows (a few KB or less): an item is a block of k
+// consecutive rows, loaded contiguously into one CTA's shared memory; each
+// output element of the block gathers from its own row there.  Tall, skinny
+// matrices (millions of rows of a few elements) would otherwise spend one
+// CTA item per row.  Gather form only.
+// ---------------------------------------------------------------------------
+struct RowBlockArgs {
+    uint8_t* base;
+    uint64_t total_rows, items, row_bytes, E;
+    uint32_t k, cols, upw, units_per_row;
+    FastDiv div_rows;          // global row -> row within its matrix
+    FastDiv32 div_units_row;   // unit of the block -> (row of the block, unit of the row)
+    FastDiv32 div_upw;
+};
+
+template <int US, typename Fn>
+__global__ void __launch_bounds__(kThreads) k_row_block(RowBlockArgs a, Fn fn) {
+    using U = typename UnitOf<US>::T;
+    using I = typename Fn::index_type;
+    extern __shared__ __align__(16) uint8_t smem[];
+    for (uint64_t it = blockIdx.x; it < a.items; it += gridDim.x) {
+        const uint64_t r0 = it * a.k;
+        const uint64_t left = a.total_rows - r0;
+        const uint32_t nr = static_cast<uint32_t>(left < a.k ? left : a.k);
+        uint8_t* blk = a.base + r0 * a.row_bytes;
+        const uint32_t units = nr * a.units_per_row;
+        for (uint32_t x = threadIdx.x; x < units; x += blockDim.x) copy_in<US, U>(smem + x * US, blk + x * US);
+        if constexpr (US >= 4) asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+        __syncthreads();
+        for (uint32_t x0 = threadIdx.x; x0 < units; x0 += kBatch * blockDim.x) {
+            U v[kBatch];
+            uint32_t dst[kBatch];
+#pragma unroll
+            for (int q = 0; q < kBatch; ++q) {
+                dst[q] = ~0u;
+                const uint32_t x = x0 + q * blockDim.x;
+                if (x >= units) continue;
+                uint32_t rr, jx, j, u;
+                a.div_units_row.divmod(x, rr, jx);
+                a.div_upw.divmod(jx, j, u);
+                const I i = static_cast<I>(a.div_rows.mod(r0 + rr));
+                const I src = fn(i, static_cast<I>(j));
+                if (!in_range(src, a.cols)) continue;
+                v[q] = *reinterpret_cast<const U*>(smem + rr * a.row_bytes + static_cast<uint32_t>(src) * a.E + u * US);
+                dst[q] = x;
+            }
+#pragma unroll
+            for (int q = 0; q < kBatch; ++q)
+                if (dst[q] != ~0u) *reinterpret_cast<U*>(blk + static_cast<uint64_t>(dst[q]) * US) = v[q];
+        }
+        __syncthreads();
     }
 }
 
@@ -954,9 +1045,45 @@ cudaError_t launch_clusters(void (*kernel)(KArgs...), int K, size_t smem, uint64
         }                                                                 \
     } while (0)
 
+// Rows larger than this leave no room for a second CTA or item buffer on
+// the SM; they prefetch the next row into registers instead.
+constexpr size_t kRowSoloMinBytes = 110 * 1024;
+// Rows this short are staged k at a time (k = kRowBlockBytes / row bytes,
+// at least kRowBlockMinRows) by k_row_block.
+constexpr uint64_t kRowBlockBytes = 48 * 1024;
+constexpr uint64_t kRowBlockMinRows = 8;
+// Matrices this small are transposed k at a time by k_slab_pack.
+constexpr uint64_t kSlabPackBytes = 48 * 1024;
+constexpr uint64_t kSlabPackMinMats = 8;
+
 // ---- slab ----------------------------------------------------------------
 template <int US>
 int launch_slab(uint8_t* data, const Pass& p, ExecContext& ctx) {
+    const uint64_t mat_bytes = p.rows * p.cols * p.elem;
+    if (p.strip == p.elem && mat_bytes * kSlabPackMinMats <= kSlabPackBytes && tuning().slab_pack) {
+        SlabPackArgs b;
+        b.base = data + p.offset;
+        b.batches = p.batches;
+        b.mat_bytes = mat_bytes;
+        b.E = p.elem;
+        b.k = static_cast<uint32_t>(kSlabPackBytes / mat_bytes);
+        b.items = (p.batches + b.k - 1) / b.k;
+        b.R = static_cast<uint32_t>(p.rows);
+        b.C = static_cast<uint32_t>(p.cols);
+        b.upw = static_cast<uint32_t>(p.elem / US);
+        b.mat_units = b.R * b.C * b.upw;
+        b.div_mat_units = FastDiv32::make(b.mat_units);
+        b.div_upw = FastDiv32::make(b.upw);
+        b.div_R = FastDiv32::make(b.R);
+        const size_t smem = (static_cast<size_t>(b.k) * mat_bytes + 127) / 128 * 128;
+        const void* k = reinterpret_cast<const void*>(&k_slab_pack<US>);
+        EI_CHECK(prep_smem(k, smem));
+        const int grid = grid_for(k, smem, b.items, ctx);
+        k_slab_pack<US><<<grid, kThreads, smem, ctx.stream>>>(b);
+        EI_CHECK(cudaGetLastError());
+        ctx.launches++;
+        return 0;
+    }
     SlabArgs a;
     a.base = data + p.offset;
     a.E = p.elem;
@@ -987,9 +1114,6 @@ int launch_slab(uint8_t* data, const Pass& p, ExecContext& ctx) {
 }
 
 // ---- rows ------------------------------------------------------------------
-// Rows larger than this leave no room for a second CTA or item buffer on
-// the SM; they prefetch the next row into registers instead.
-constexpr size_t kRowSoloMinBytes = 110 * 1024;
 
 template <int US, typename Fn, bool kScatter>
 int launch_row_staged(uint8_t* data, const Pass& p, const Staging& st, ExecContext& ctx, const Fn& fn);
@@ -999,6 +1123,32 @@ int launch_row(uint8_t* data, const Pass& p, const FnOnChip& fn, const Fn64& fn6
     const size_t cap = smem_cap_of(ctx.caps);
     const Staging st = plan_row_staging(p.cols, p.elem, cap, kScatter);
     if (!st.on_chip) return launch_row_staged<US, Fn64, kScatter>(data, p, st, ctx, fn64);
+    if constexpr (!kScatter) {
+        const uint64_t row_bytes = p.cols * p.elem;
+        if (st.w == p.elem && row_bytes * kRowBlockMinRows <= kRowBlockBytes && tuning().row_block) {
+            RowBlockArgs b;
+            b.base = data + p.offset;
+            b.total_rows = p.batches * p.rows;
+            b.row_bytes = row_bytes;
+            b.E = p.elem;
+            b.k = static_cast<uint32_t>(kRowBlockBytes / row_bytes);
+            b.items = (b.total_rows + b.k - 1) / b.k;
+            b.cols = static_cast<uint32_t>(p.cols);
+            b.upw = static_cast<uint32_t>(p.elem / US);
+            b.units_per_row = b.cols * b.upw;
+            b.div_rows = FastDiv::make(p.rows, b.total_rows);
+            b.div_units_row = FastDiv32::make(b.units_per_row);
+            b.div_upw = FastDiv32::make(b.upw);
+            const size_t smem = (static_cast<size_t>(b.k) * row_bytes + 127) / 128 * 128;
+            const void* k = reinterpret_cast<const void*>(&k_row_block<US, FnOnChip>);
+            EI_CHECK(prep_smem(k, smem));
+            const int grid = grid_for(k, smem, b.items, ctx);
+            k_row_block<US, FnOnChip><<<grid, kThreads, smem, ctx.stream>>>(b, fn);
+            EI_CHECK(cudaGetLastError());
+            ctx.launches++;
+            return 0;
+        }
+    }
     RowArgs a;
     a.base = data + p.offset;
     a.E = p.elem;
@@ -1106,7 +1256,7 @@ int launch_col_staged(uint8_t* data, const Pass& p, const Staging& st, ExecConte
 template <int US, typename FnOnChip, typename Fn64>
 int launch_col(uint8_t* data, const Pass& p, const FnOnChip& fn, const Fn64& fn64, ExecContext& ctx) {
     const size_t cap = smem_cap_of(ctx.caps);
-    const Staging st = plan_col_staging(p.rows, p.elem, cap);
+    const Staging st = plan_col_staging(p.rows, p.elem, cap, p.cols);
     if (!st.on_chip) return launch_col_staged<US, Fn64>(data, p, st, ctx, fn64);
     ColArgs a;
     a.base = data + p.offset;

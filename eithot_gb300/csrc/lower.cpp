@@ -127,13 +127,13 @@ Staging plan_row_staging(uint64_t cols, uint64_t E, size_t cap, bool scatter) {
     return s;
 }
 
-Staging plan_col_staging(uint64_t rows, uint64_t E, size_t cap) {
+Staging plan_col_staging(uint64_t rows, uint64_t E, size_t cap, uint64_t cols) {
     Staging s;
     for (uint64_t occ_limit : {kTwoPerSm, static_cast<uint64_t>(cap)}) {
         for (uint64_t tb : {uint64_t(128), uint64_t(64), uint64_t(32)}) {
             if (tuning().col_chunk && tb != static_cast<uint64_t>(tuning().col_chunk)) continue;
             uint64_t w, tw;
-            if (E <= tb) { w = E; tw = std::max<uint64_t>(1, tb / E); }
+            if (E <= tb) { w = E; tw = std::max<uint64_t>(1, std::min(tb / E, cols ? cols : tb / E)); }
             else { w = tb; tw = 1; }
             // tw*w contiguous bytes per staged row: a quarter-warp of 16-byte
             // reads (or a warp of 4-byte reads) covers one row piece, so the
@@ -157,7 +157,7 @@ Staging plan_col_staging(uint64_t rows, uint64_t E, size_t cap) {
     }
     // Global staging: 128-byte row pieces.
     s.w = E <= 128 ? E : 128;
-    s.tw = E <= 128 ? std::max<uint64_t>(1, 128 / E) : 1;
+    s.tw = E <= 128 ? std::max<uint64_t>(1, std::min<uint64_t>(128 / E, cols ? cols : 128 / E)) : 1;
     s.pitch = s.tw * s.w;
     s.K = 1;
     s.item_bytes = rows * s.pitch;
@@ -204,7 +204,7 @@ double cluster_utilisation(int K) {
 // large for a cluster, a global-memory barrier over a group of G
 // co-resident CTAs.  Candidates are costed by row-piece efficiency, SM
 // utilisation, halo re-reads and buffering.
-Staging plan_col_owner(uint64_t rows, uint64_t E, int fn, uint64_t b, const DeviceCaps& caps) {
+Staging plan_col_owner(uint64_t rows, uint64_t cols, uint64_t E, int fn, uint64_t b, const DeviceCaps& caps) {
     const size_t cap = smem_cap_of(caps);
     const int form = tuning().col_form;
     Staging best;
@@ -216,7 +216,7 @@ Staging plan_col_owner(uint64_t rows, uint64_t E, int fn, uint64_t b, const Devi
     for (uint64_t tb : {uint64_t(512), uint64_t(256), uint64_t(128), uint64_t(64), uint64_t(32)}) {
         if (tuning().col_chunk && tb != static_cast<uint64_t>(tuning().col_chunk)) continue;
         uint64_t w, tw;
-        if (E <= tb) { w = E; tw = std::max<uint64_t>(1, tb / E); }
+        if (E <= tb) { w = E; tw = std::max<uint64_t>(1, std::min(tb / E, cols ? cols : tb / E)); }
         else { w = tb; tw = 1; }
         const uint64_t pitch = tw * w;
         uint64_t lo, hi;
@@ -287,10 +287,10 @@ Staging plan_col_owner(uint64_t rows, uint64_t E, int fn, uint64_t b, const Devi
 
 Staging plan_col_pass(const Pass& p, const DeviceCaps& caps) {
     if (tuning().col_owner) {
-        const Staging s = plan_col_owner(p.rows, p.elem, p.fn, p.b, caps);
+        const Staging s = plan_col_owner(p.rows, p.cols, p.elem, p.fn, p.b, caps);
         if (s.on_chip) return s;
     }
-    return plan_col_staging(p.rows, p.elem, smem_cap_of(caps));
+    return plan_col_staging(p.rows, p.elem, smem_cap_of(caps), p.cols);
 }
 
 Xpose xpose_of(const LowOp& op, uint64_t elem, uint64_t n_sub, uint64_t base_offset) {
@@ -314,9 +314,9 @@ namespace {
 double row_cost(uint64_t cols, uint64_t E, size_t cap, bool scatter) {
     return plan_row_staging(cols, E, cap, scatter).cost;
 }
-double col_cost(uint64_t rows, uint64_t E, int fn, uint64_t b, const DeviceCaps& caps) {
+double col_cost(uint64_t rows, uint64_t cols, uint64_t E, int fn, uint64_t b, const DeviceCaps& caps) {
     Pass p;
-    p.rows = rows; p.elem = E; p.fn = fn; p.b = b;
+    p.rows = rows; p.cols = cols; p.elem = E; p.fn = fn; p.b = b;
     return plan_col_pass(p, caps).cost;
 }
 
@@ -348,10 +348,10 @@ void lower_xpose(const Xpose& x, const DeviceCaps& caps, std::vector<Pass>* pass
     // Catanzaro: c2r on the R x C view, or r2c on the C x R view.
     uint64_t g, inv;
     gcd_inverse(x.R, x.C, &g, &inv);
-    const double c2r = (g > 1 ? col_cost(x.R, x.E, kFnC2RPreRot, x.C / g, caps) : 0.0) + row_cost(x.C, x.E, cap, false) +
-                       col_cost(x.R, x.E, kFnC2RColShuffle, x.C / g, caps);
-    const double r2c = col_cost(x.C, x.E, kFnR2CColShuffle, x.R / g, caps) + row_cost(x.R, x.E, cap, true) +
-                       (g > 1 ? col_cost(x.C, x.E, kFnR2CPostRot, x.R / g, caps) : 0.0);
+    const double c2r = (g > 1 ? col_cost(x.R, x.C, x.E, kFnC2RPreRot, x.C / g, caps) : 0.0) + row_cost(x.C, x.E, cap, false) +
+                       col_cost(x.R, x.C, x.E, kFnC2RColShuffle, x.C / g, caps);
+    const double r2c = col_cost(x.C, x.R, x.E, kFnR2CColShuffle, x.R / g, caps) + row_cost(x.R, x.E, cap, true) +
+                       (g > 1 ? col_cost(x.C, x.R, x.E, kFnR2CPostRot, x.R / g, caps) : 0.0);
     bool use_c2r = (c2r < r2c) || (c2r == r2c && x.C >= x.R);
     if (tuning().variant == 1) use_c2r = true;
     if (tuning().variant == 2) use_c2r = false;

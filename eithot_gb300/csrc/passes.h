@@ -74,6 +74,8 @@ struct Tuning {
     int col_owner = 1;     // column passes: 1 owner-computed writes, 0 gathers through distributed smem
     int col_form = 0;      // owner-computed column passes: 0 cost model, 1 clusters, 2 CTA groups
     int row_prefetch = 1;  // rows filling a CTA: prefetch the next row into registers
+    int row_block = 1;     // short rows: stage blocks of consecutive rows per CTA item
+    int slab_pack = 1;     // small matrices: transpose blocks of consecutive matrices per CTA item
     int sync_sleep_ns = 64;  // group barriers: back-off between polls
     int sync_relaxed = 0;    // group barriers: arrive without release semantics
     int group_per_sm = 0;    // group form: 0 cost model, 1 or 2 CTAs per SM
@@ -105,7 +107,8 @@ struct Staging {
 // scatter: the row pass pushes elements to their destinations (r2c);
 // otherwise it pulls them (c2r).
 Staging plan_row_staging(uint64_t cols, uint64_t E, size_t smem_cap, bool scatter = false);
-Staging plan_col_staging(uint64_t rows, uint64_t E, size_t smem_cap);
+// cols: the matrix's column count (0: unknown); a tile never spans more.
+Staging plan_col_staging(uint64_t rows, uint64_t E, size_t smem_cap, uint64_t cols = 0);
 
 // Rows of halo an owner-computed column tile of tw columns needs below (lo)
 // and above (hi) its owned rows for column map `fn` (b = n / gcd(m, n)).

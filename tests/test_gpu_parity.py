@@ -86,7 +86,8 @@ def test_catanzaro_2d(E, R, C, elem):
 
 @pytest.fixture
 def tuned(E):
-    keys = ("variant", "col_owner", "col_chunk", "max_cluster", "dbuf", "col_form", "row_prefetch")
+    keys = ("variant", "col_owner", "col_chunk", "max_cluster", "dbuf", "col_form", "row_prefetch", "row_block",
+            "slab_pack")
     saved = {k: E.tune_get(k) for k in keys}
 
     def set_(**kw):
@@ -135,6 +136,29 @@ def test_row_prefetch(E, tuned, dims, perm, elem, prefetch):
     prefetch of the next row, including rows that leave some threads'
     last units empty."""
     tuned(variant=2, row_prefetch=prefetch)
+    run_case(E, dims, perm, elem)
+
+
+@pytest.mark.parametrize("dims,perm,elem", [([2, 300000], [2, 1], 1), ([3, 200001], [2, 1], 2), ([7, 70000], [2, 1], 4),
+                                            ([2, 5, 100000], [3, 1, 2], 1), ([13, 40000], [2, 1], 8),
+                                            ([300000, 2], [2, 1], 1), ([100, 3000], [2, 1], 2)])
+@pytest.mark.parametrize("variant", [1, 2])
+@pytest.mark.parametrize("block", [0, 1])
+def test_tall_skinny_rows_in_blocks(E, tuned, dims, perm, elem, variant, block):
+    """Matrices of a few columns (rows of a few bytes): row passes staged as
+    blocks of consecutive rows, and the one-row-per-item form."""
+    tuned(variant=variant, row_block=block)
+    run_case(E, dims, perm, elem)
+
+
+@pytest.mark.parametrize("dims,perm", [([3, 5, 100000], [2, 1, 3]), ([2, 2, 300001], [2, 1, 3]),
+                                       ([7, 3, 4, 5000], [3, 1, 2, 4]), ([5, 9, 1000], [3, 2, 1])])
+@pytest.mark.parametrize("elem", [1, 2, 4, 8])
+@pytest.mark.parametrize("pack", [0, 1])
+def test_many_small_matrices(E, tuned, dims, perm, elem, pack):
+    """Batches of tiny matrices transposed as blocks of consecutive
+    matrices per CTA, and one matrix per CTA item."""
+    tuned(slab_pack=pack)
     run_case(E, dims, perm, elem)
 
 
