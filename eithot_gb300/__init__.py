@@ -76,6 +76,13 @@ def _load():
                                      ctypes.c_void_p]
     lib.eithot_check_hash.argtypes = [ctypes.c_void_p, ctypes.c_int, I64P, IP, ctypes.c_size_t, ctypes.c_uint64,
                                       ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_int64)]
+    lib.eithot_batch_create.argtypes = [ctypes.c_int, IP, I64P, IP, ctypes.POINTER(ctypes.c_size_t), ctypes.c_int,
+                                        ctypes.c_double, ctypes.POINTER(ctypes.c_void_p)]
+    lib.eithot_batch_workspace_size.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t)]
+    lib.eithot_batch_run.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_size_t),
+                                     ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+    lib.eithot_batch_launches.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
+    lib.eithot_batch_destroy.argtypes = [ctypes.c_void_p]
     lib.eithot_tune_set.argtypes = [ctypes.c_char_p, ctypes.c_double]
     lib.eithot_tune_get.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double)]
     return lib
@@ -240,6 +247,60 @@ def check_hash_ptr(ptr: int, dims, perm, elem_size: int, seed: int, stream: Opti
     _check(lib.eithot_check_hash(ctypes.c_void_p(ptr), r, d, p, elem_size, seed & (2**64 - 1),
                                  ctypes.c_void_p(stream) if stream else None, ctypes.byref(bad), ctypes.byref(first)))
     return bad.value, first.value
+
+
+class Batch:
+    """Many independent in-place transposes planned once (eithot_batch_*).
+
+    tensors: sequence of (dims, perm_1based, elem_size)."""
+
+    def __init__(self, tensors, num_sub_tensors: int = 1, alpha: float = 0.01):
+        ranks, dims, perms, elems = [], [], [], []
+        for d, p, e in tensors:
+            if len(d) != len(p):
+                raise EithotError(EINVAL, "dims and permutation differ in length")
+            ranks.append(len(d))
+            dims += [int(x) for x in d]
+            perms += [int(x) for x in p]
+            elems.append(int(e))
+        self.count = len(ranks)
+        h = ctypes.c_void_p()
+        _check(lib.eithot_batch_create(self.count, (ctypes.c_int * max(1, len(ranks)))(*ranks),
+                                       (ctypes.c_int64 * max(1, len(dims)))(*dims),
+                                       (ctypes.c_int * max(1, len(perms)))(*perms),
+                                       (ctypes.c_size_t * max(1, len(elems)))(*elems),
+                                       num_sub_tensors, alpha, ctypes.byref(h)))
+        self._h = h
+
+    @property
+    def workspace_size(self) -> int:
+        v = ctypes.c_size_t()
+        _check(lib.eithot_batch_workspace_size(self._h, ctypes.byref(v)))
+        return v.value
+
+    def run(self, ptrs, capacities, workspace_ptr: int = 0, workspace_bytes: int = 0, stream: Optional[int] = None):
+        n = self.count
+        _check(lib.eithot_batch_run(self._h, (ctypes.c_void_p * max(1, n))(*ptrs),
+                                    (ctypes.c_size_t * max(1, n))(*capacities),
+                                    ctypes.c_void_p(workspace_ptr) if workspace_ptr else None, workspace_bytes,
+                                    ctypes.c_void_p(stream) if stream else None))
+
+    @property
+    def launches(self) -> int:
+        v = ctypes.c_int()
+        _check(lib.eithot_batch_launches(self._h, ctypes.byref(v)))
+        return v.value
+
+    def close(self):
+        if self._h:
+            lib.eithot_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def sync_timeouts() -> int:

@@ -1,0 +1,209 @@
+// The batched form: many independent in-place transposes planned once and
+// run together.  Each tensor's passes stay in order on one of up to 16
+// internal streams ("lanes"); tensors are spread over the lanes
+// largest-first onto the least-loaded lane, so the small passes of
+// different tensors overlap on the GPU instead of queueing behind one
+// another.  Column passes use thread-block clusters only (no
+// group-synchronised passes, which rely on all their CTAs being resident
+// while other lanes' kernels occupy SMs).  Every lane has its own scratch
+// slice of the batch workspace.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "api_util.h"
+#include "eithot.h"
+#include "exec.h"
+#include "passes.h"
+#include "plan.h"
+
+using namespace eithot;
+using namespace eithot::api;
+
+struct eithot_batch {
+    int device = -1;
+    DeviceCaps caps;
+    Tuning tuning;
+    struct Item {
+        std::vector<Pass> passes;
+        size_t need = 0;       // bytes the (padded) tensor occupies
+        size_t scratch = 0;    // workspace its passes use
+        double bytes = 0;      // tensor bytes
+        int lane = 0;
+    };
+    std::vector<Item> items;
+    std::vector<std::vector<int>> lane_items;
+    std::vector<size_t> lane_offset, lane_bytes;
+    size_t workspace = 0;
+    std::vector<cudaStream_t> streams;
+    std::vector<cudaEvent_t> done;
+    cudaEvent_t fork = nullptr;
+    int last_launches = 0;
+};
+
+namespace {
+
+constexpr int kMaxLanes = 16;
+
+int make_streams(eithot_batch* b) {
+    if (!b->streams.empty()) return EITHOT_OK;
+    const int lanes = static_cast<int>(b->lane_items.size());
+    cudaError_t e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+    for (int l = 0; l < lanes && e == cudaSuccess; ++l) {
+        cudaStream_t s = nullptr;
+        cudaEvent_t ev = nullptr;
+        e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        b->streams.push_back(s);
+        b->done.push_back(ev);
+    }
+    if (e != cudaSuccess) return fail(EITHOT_ECUDA, std::string("batch streams: ") + cudaGetErrorString(e));
+    return EITHOT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int eithot_batch_create(int count, const int* ranks, const int64_t* dims, const int* perms_1based,
+                        const size_t* elem_sizes, int num_sub_tensors, double alpha, eithot_batch** out) {
+    if (!out) return fail(EITHOT_EINVAL, "null out");
+    *out = nullptr;
+    if (count < 0 || (count > 0 && (!ranks || !dims || !perms_1based || !elem_sizes)))
+        return fail(EITHOT_EINVAL, "null or negative batch description");
+    auto* b = new eithot_batch();
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) {
+        std::string err;
+        if (!query_caps(dev, &b->caps, &err)) b->caps = DeviceCaps();
+        b->device = dev;
+    } else {
+        cudaGetLastError();
+    }
+    b->tuning = tuning();
+    b->tuning.col_form = 1;  // clusters only: no pass relies on grid-wide residency
+    ScopedTuning scope(b->tuning);
+    b->items.resize(count);
+    size_t off = 0;
+    for (int t = 0; t < count; ++t) {
+        NdPlan plan;
+        auto& it = b->items[t];
+        const int rc = build(ranks[t], dims + off, perms_1based + off, elem_sizes[t], num_sub_tensors, alpha,
+                             EITHOT_ORDER_MIXED, b->caps, &plan, &it.passes);
+        if (rc) {
+            delete b;
+            return fail(rc, "tensor " + std::to_string(t) + ": " + eithot_last_error());
+        }
+        off += static_cast<size_t>(ranks[t]);
+        it.need = static_cast<size_t>(plan.padded_volume) * elem_sizes[t];
+        it.bytes = static_cast<double>(plan.volume) * static_cast<double>(elem_sizes[t]);
+        it.scratch = choose_workspace(it.passes, b->caps, alpha, it.bytes);
+    }
+    // largest first onto the least-loaded lane
+    const int lanes = std::max(1, std::min(count, kMaxLanes));
+    std::vector<int> order(count);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return b->items[x].bytes > b->items[y].bytes; });
+    std::vector<double> load(lanes, 0.0);
+    b->lane_items.assign(lanes, {});
+    b->lane_bytes.assign(lanes, 0);
+    for (int t : order) {
+        const int l = static_cast<int>(std::min_element(load.begin(), load.end()) - load.begin());
+        load[l] += b->items[t].bytes + 64.0 * 1024;  // a launch's fixed cost, in bytes
+        b->items[t].lane = l;
+        b->lane_items[l].push_back(t);
+        b->lane_bytes[l] = std::max(b->lane_bytes[l], b->items[t].scratch);
+    }
+    b->lane_offset.assign(lanes, 0);
+    for (int l = 0; l < lanes; ++l) {
+        b->lane_offset[l] = b->workspace;
+        b->workspace += (b->lane_bytes[l] + 255) / 256 * 256;
+    }
+    *out = b;
+    return EITHOT_OK;
+}
+
+int eithot_batch_workspace_size(const eithot_batch* b, size_t* bytes) {
+    if (!b || !bytes) return fail(EITHOT_EINVAL, "null argument");
+    *bytes = b->workspace;
+    return EITHOT_OK;
+}
+
+int eithot_batch_run(eithot_batch* b, void* const* d_data, const size_t* capacities, void* d_workspace,
+                     size_t workspace_bytes, void* stream) {
+    if (!b || (!b->items.empty() && (!d_data || !capacities))) return fail(EITHOT_EINVAL, "null argument");
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || (b->device >= 0 && dev != b->device))
+        return fail(EITHOT_EINVAL, "the batch was planned for another device");
+    for (size_t t = 0; t < b->items.size(); ++t) {
+        if (!d_data[t]) return fail(EITHOT_EINVAL, "tensor " + std::to_string(t) + ": null data pointer");
+        if (capacities[t] < b->items[t].need)
+            return fail(EITHOT_EINVAL, "tensor " + std::to_string(t) + ": capacity below the (padded) tensor");
+    }
+    if (b->items.empty()) return EITHOT_OK;
+    if (int rc = make_streams(b)) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    uint8_t* ws = static_cast<uint8_t*>(d_workspace);
+    bool owned = false;
+    if (b->workspace > 0) {
+        if (ws) {
+            if (workspace_bytes < b->workspace) return fail(EITHOT_ENOMEM, "workspace smaller than eithot_batch_workspace_size()");
+        } else {
+            void* p = nullptr;
+            const cudaError_t e = cudaMallocAsync(&p, b->workspace, st);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                return fail(EITHOT_ENOMEM, std::string("batch workspace: ") + cudaGetErrorString(e));
+            }
+            ws = static_cast<uint8_t*>(p);
+            owned = true;
+        }
+    }
+    ScopedTuning scope(b->tuning);
+    cudaError_t e = cudaEventRecord(b->fork, st);
+    int rc = EITHOT_OK;
+    std::string err;
+    b->last_launches = 0;
+    for (size_t l = 0; l < b->streams.size() && e == cudaSuccess && rc == EITHOT_OK; ++l) {
+        e = cudaStreamWaitEvent(b->streams[l], b->fork, 0);
+        for (int t : b->lane_items[l]) {
+            if (e != cudaSuccess || rc != EITHOT_OK) break;
+            ExecContext ctx;
+            ctx.caps = b->caps;
+            ctx.stream = b->streams[l];
+            ctx.scratch = ws ? ws + b->lane_offset[l] : nullptr;
+            ctx.scratch_bytes = ws ? b->lane_bytes[l] : 0;
+            rc = run_passes(static_cast<uint8_t*>(d_data[t]), b->items[t].passes, ctx);
+            if (rc) err = "tensor " + std::to_string(t) + ": " + ctx.err;
+            b->last_launches += ctx.launches;
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(b->done[l], b->streams[l]);
+    }
+    // join every lane that was forked, whatever happened
+    for (size_t l = 0; l < b->streams.size(); ++l) cudaStreamWaitEvent(st, b->done[l], 0);
+    if (owned) cudaFreeAsync(ws, st);
+    if (rc) return fail(rc, err);
+    if (e != cudaSuccess) return fail(EITHOT_ECUDA, std::string("batch: ") + cudaGetErrorString(e));
+    return EITHOT_OK;
+}
+
+int eithot_batch_launches(const eithot_batch* b, int* launches) {
+    if (!b || !launches) return fail(EITHOT_EINVAL, "null argument");
+    *launches = b->last_launches;
+    return EITHOT_OK;
+}
+
+int eithot_batch_destroy(eithot_batch* b) {
+    if (!b) return EITHOT_OK;
+    for (auto s : b->streams) cudaStreamDestroy(s);
+    for (auto ev : b->done) cudaEventDestroy(ev);
+    if (b->fork) cudaEventDestroy(b->fork);
+    delete b;
+    return EITHOT_OK;
+}
+
+}  // extern "C"

@@ -9,6 +9,7 @@
 #include <string>
 #include <vector>
 
+#include "api_util.h"
 #include "estimator.h"
 #include "exec.h"
 #include "passes.h"
@@ -24,6 +25,11 @@ thread_local size_t g_events_used = 0;
 thread_local std::vector<std::pair<size_t, size_t>> g_spans;
 thread_local std::vector<std::string> g_pass_names;
 thread_local std::vector<double> g_pass_bytes;
+
+}  // namespace
+
+namespace eithot {
+namespace api {
 
 int fail(int code, const std::string& msg) {
     g_err = msg;
@@ -71,7 +77,10 @@ int build(int rank, const int64_t* dims, const int* perm, size_t elem, int nb, d
     return EITHOT_OK;
 }
 
-}  // namespace
+}  // namespace api
+}  // namespace eithot
+
+using namespace eithot::api;
 
 extern "C" {
 
@@ -328,8 +337,10 @@ int eithot_transpose_ex(void* d_data, size_t capacity_bytes, int rank, const int
     ctx.names = &g_pass_names;
     ctx.bytes = &g_pass_bytes;
     size_t fb = 0, tb = 0;
-    cudaMemGetInfo(&fb, &tb);
-    g_stats.free_before = fb;
+    if (g_profile) {  // a device-wide query: only while profiling
+        cudaMemGetInfo(&fb, &tb);
+        g_stats.free_before = fb;
+    }
     bool owned = false;
     if (d_workspace) {
         if (workspace_bytes < min_ws) return fail(EITHOT_ENOMEM, "caller workspace is smaller than eithot_workspace_size()");
@@ -349,8 +360,10 @@ int eithot_transpose_ex(void* d_data, size_t capacity_bytes, int rank, const int
             owned = true;
         }
     }
-    cudaMemGetInfo(&fb, &tb);
-    g_stats.free_after_alloc = fb;
+    if (g_profile) {
+        cudaMemGetInfo(&fb, &tb);
+        g_stats.free_after_alloc = fb;
+    }
     g_stats.workspace_bytes = ctx.scratch_bytes;
     rc = eithot::run_passes(static_cast<uint8_t*>(d_data), passes, ctx);
     g_events_used = ctx.events_used;

@@ -16,7 +16,9 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -592,9 +594,18 @@ struct ColOwnArgs {
     uint32_t rows, cols, tw, ntiles, pitch, Q, Hlo, Hhi, w, upw, last_upw, nstrips, RU, buf_bytes;
     uint32_t hbase;  // (-Hlo) mod m: slot x0 - Hlo is slot (x0 + hbase) mod m, also when Hlo > m
     bool dbuf;
+    bool whole;      // one CTA holds all m slots of a tile: no halo, slots indexed modulo m
+    uint32_t dofs;   // whole: a multiple of m above every |delta difference| of a tile
     FastDiv div_strips, div_tiles;
     FastDiv32 div_RU, div_upw, div_m;
 };
+
+// Staged slot holding the source of output slot ii's element at column
+// offset d = delta(j0 + c) - delta(j0).
+__device__ __forceinline__ int64_t own_local(const ColOwnArgs& a, uint32_t ii, int64_t d) {
+    if (a.whole) return a.div_m.mod(static_cast<uint32_t>(static_cast<int64_t>(ii) + d + a.dofs));
+    return static_cast<int64_t>(ii + a.Hlo) + d;
+}
 
 struct OwnItem {
     uint8_t* mat;
@@ -687,7 +698,7 @@ __global__ void __launch_bounds__(kThreads) k_col_owner(ColOwnArgs a, Own own) {
                 const uint64_t lane_off = static_cast<uint64_t>(lc) * a.E + lu * US;
                 for (uint32_t ii = ii0; ii < myrows; ii += step) {
                     const I i = own.row_of(static_cast<I>(x0 + ii), static_cast<I>(ci.col0));
-                    const int64_t local = static_cast<int64_t>(ii + a.Hlo) + d;
+                    const int64_t local = own_local(a, ii, d);
                     if (!in_range(i, a.rows) || !in_range(static_cast<uint64_t>(local), nstage)) continue;
                     *reinterpret_cast<U*>(ci.mat + static_cast<uint64_t>(i) * a.row_bytes + lane_off) =
                         *reinterpret_cast<const U*>(buf + static_cast<uint32_t>(local) * a.pitch + soff);
@@ -702,7 +713,7 @@ __global__ void __launch_bounds__(kThreads) k_col_owner(ColOwnArgs a, Own own) {
                 if (c >= ci.tcols || u >= ci.lim) continue;
                 const int64_t d = own.delta(static_cast<I>(ci.col0 + c)) - own.delta(static_cast<I>(ci.col0));
                 const I i = own.row_of(static_cast<I>(x0 + ii), static_cast<I>(ci.col0));
-                const int64_t local = static_cast<int64_t>(ii + a.Hlo) + d;
+                const int64_t local = own_local(a, ii, d);
                 if (!in_range(i, a.rows) || !in_range(static_cast<uint64_t>(local), nstage)) continue;
                 *reinterpret_cast<U*>(ci.mat + static_cast<uint64_t>(i) * a.row_bytes + static_cast<uint64_t>(c) * a.E + u * US) =
                     *reinterpret_cast<const U*>(buf + static_cast<uint32_t>(local) * a.pitch + c * a.w + u * US);
@@ -805,7 +816,7 @@ __global__ void __launch_bounds__(kThreads) k_col_group(ColOwnArgs a, Own own, G
                 const uint64_t lane_off = static_cast<uint64_t>(lc) * a.E + lu * US;
                 for (uint32_t ii = ii0; ii < myrows; ii += step) {
                     const I i = own.row_of(static_cast<I>(x0 + ii), static_cast<I>(ci.col0));
-                    const int64_t local = static_cast<int64_t>(ii + a.Hlo) + d;
+                    const int64_t local = own_local(a, ii, d);
                     if (!in_range(i, a.rows) || !in_range(static_cast<uint64_t>(local), nstage)) continue;
                     *reinterpret_cast<U*>(ci.mat + static_cast<uint64_t>(i) * a.row_bytes + lane_off) =
                         *reinterpret_cast<const U*>(buf + static_cast<uint32_t>(local) * a.pitch + soff);
@@ -820,7 +831,7 @@ __global__ void __launch_bounds__(kThreads) k_col_group(ColOwnArgs a, Own own, G
                 if (c >= ci.tcols || u >= ci.lim) continue;
                 const int64_t d = own.delta(static_cast<I>(ci.col0 + c)) - own.delta(static_cast<I>(ci.col0));
                 const I i = own.row_of(static_cast<I>(x0 + ii), static_cast<I>(ci.col0));
-                const int64_t local = static_cast<int64_t>(ii + a.Hlo) + d;
+                const int64_t local = own_local(a, ii, d);
                 if (!in_range(i, a.rows) || !in_range(static_cast<uint64_t>(local), nstage)) continue;
                 *reinterpret_cast<U*>(ci.mat + static_cast<uint64_t>(i) * a.row_bytes + static_cast<uint64_t>(c) * a.E + u * US) =
                     *reinterpret_cast<const U*>(buf + static_cast<uint32_t>(local) * a.pitch + c * a.w + u * US);
@@ -984,9 +995,50 @@ StripGeom make_strips(uint64_t E, uint64_t w, uint64_t U, uint64_t outer, uint64
     return g;
 }
 
+// Launch-configuration queries are costly host calls (several us each) and
+// their answers depend only on (device, kernel, shared memory, cluster
+// size): they are made once and remembered.
+struct LaunchKey {
+    int dev;
+    const void* kernel;
+    size_t smem;
+    int K;
+    int kind;
+    bool operator<(const LaunchKey& o) const {
+        return std::tie(dev, kernel, smem, K, kind) < std::tie(o.dev, o.kernel, o.smem, o.K, o.kind);
+    }
+};
+enum { kQuerySmemSet = 0, kQueryNonPortable = 1, kQueryBlocks = 2, kQueryClusters = 3 };
+
+std::mutex g_launch_mu;
+std::map<LaunchKey, int> g_launch_cache;
+
+int current_device() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return dev;
+}
+
+bool cached(const LaunchKey& k, int* v) {
+    std::lock_guard<std::mutex> lock(g_launch_mu);
+    auto it = g_launch_cache.find(k);
+    if (it == g_launch_cache.end()) return false;
+    *v = it->second;
+    return true;
+}
+
+void remember(const LaunchKey& k, int v) {
+    std::lock_guard<std::mutex> lock(g_launch_mu);
+    g_launch_cache[k] = v;
+}
+
 int grid_for(const void* kernel, size_t smem, uint64_t items, const ExecContext& ctx) {
+    const LaunchKey key{current_device(), kernel, smem, 1, kQueryBlocks};
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem);
+    if (!cached(key, &per_sm)) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem);
+        remember(key, per_sm);
+    }
     if (per_sm < 1) per_sm = 1;
     const uint64_t cap = static_cast<uint64_t>(per_sm) * ctx.caps.sms;
     return static_cast<int>(std::max<uint64_t>(1, std::min<uint64_t>(items, cap)));
@@ -998,9 +1050,16 @@ int grid_for_elems(uint64_t total, const ExecContext& ctx) {
     return static_cast<int>(std::max<uint64_t>(1, std::min<uint64_t>(blocks, cap)));
 }
 
+// Raises the kernel's dynamic shared-memory limit to at least `smem` (the
+// largest value set so far on this device is remembered).
 cudaError_t prep_smem(const void* kernel, size_t smem) {
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                static_cast<int>(smem));
+    const LaunchKey key{current_device(), kernel, 0, 0, kQuerySmemSet};
+    int have = -1;
+    if (cached(key, &have) && static_cast<size_t>(have) >= smem) return cudaSuccess;
+    const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               static_cast<int>(smem));
+    if (e == cudaSuccess) remember(key, static_cast<int>(smem));
+    return e;
 }
 
 // Launches `kernel` as clusters of K CTAs, as many clusters as can be
@@ -1009,11 +1068,14 @@ template <typename... KArgs, typename... Args>
 cudaError_t launch_clusters(void (*kernel)(KArgs...), int K, size_t smem, uint64_t items,
                             ExecContext& ctx, Args&&... args) {
     const void* kp = reinterpret_cast<const void*>(kernel);
+    const int dev = current_device();
     cudaError_t e = prep_smem(kp, smem);
     if (e != cudaSuccess) return e;
-    if (K > 8) {
+    int flag = 0;
+    if (K > 8 && !cached(LaunchKey{dev, kp, 0, 0, kQueryNonPortable}, &flag)) {
         e = cudaFuncSetAttribute(kp, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
         if (e != cudaSuccess) return e;
+        remember(LaunchKey{dev, kp, 0, 0, kQueryNonPortable}, 1);
     }
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr[1];
@@ -1027,9 +1089,13 @@ cudaError_t launch_clusters(void (*kernel)(KArgs...), int K, size_t smem, uint64
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     cfg.gridDim = dim3(K * 1024);
+    const LaunchKey key{dev, kp, smem, K, kQueryClusters};
     int max_clusters = 0;
-    e = cudaOccupancyMaxActiveClusters(&max_clusters, kp, &cfg);
-    if (e != cudaSuccess) return e;
+    if (!cached(key, &max_clusters)) {
+        e = cudaOccupancyMaxActiveClusters(&max_clusters, kp, &cfg);
+        if (e != cudaSuccess) return e;
+        remember(key, max_clusters);
+    }
     if (max_clusters < 1) return cudaErrorLaunchOutOfResources;
     const uint64_t nclusters = std::min<uint64_t>(items, static_cast<uint64_t>(max_clusters));
     cfg.gridDim = dim3(static_cast<unsigned>(nclusters * K));
@@ -1060,7 +1126,7 @@ constexpr uint64_t kSlabPackMinMats = 8;
 template <int US>
 int launch_slab(uint8_t* data, const Pass& p, ExecContext& ctx) {
     const uint64_t mat_bytes = p.rows * p.cols * p.elem;
-    if (p.strip == p.elem && mat_bytes * kSlabPackMinMats <= kSlabPackBytes && tuning().slab_pack) {
+    if (mat_bytes * kSlabPackMinMats <= kSlabPackBytes && tuning().slab_pack) {  // whole matrices: any strip
         SlabPackArgs b;
         b.base = data + p.offset;
         b.batches = p.batches;
@@ -1125,7 +1191,7 @@ int launch_row(uint8_t* data, const Pass& p, const FnOnChip& fn, const Fn64& fn6
     if (!st.on_chip) return launch_row_staged<US, Fn64, kScatter>(data, p, st, ctx, fn64);
     if constexpr (!kScatter) {
         const uint64_t row_bytes = p.cols * p.elem;
-        if (st.w == p.elem && row_bytes * kRowBlockMinRows <= kRowBlockBytes && tuning().row_block) {
+        if (row_bytes * kRowBlockMinRows <= kRowBlockBytes && tuning().row_block) {  // whole rows: any strip
             RowBlockArgs b;
             b.base = data + p.offset;
             b.total_rows = p.batches * p.rows;
@@ -1315,6 +1381,8 @@ ColOwnArgs col_owner_args(uint8_t* data, const Pass& p, const Staging& st, int U
     a.Hlo = static_cast<uint32_t>(st.hlo);
     a.Hhi = static_cast<uint32_t>(st.hhi);
     a.hbase = static_cast<uint32_t>((p.rows - st.hlo % p.rows) % p.rows);
+    a.whole = st.whole;
+    a.dofs = st.whole ? static_cast<uint32_t>((st.tw / p.rows + 1) * p.rows) : 0;
     a.items = p.batches * a.ntiles * a.nstrips;
     a.div_strips = FastDiv::make(a.nstrips, a.items);
     a.div_tiles = FastDiv::make(a.ntiles, p.batches * a.ntiles);
@@ -1348,9 +1416,13 @@ cudaError_t launch_groups(void (*kernel)(ColOwnArgs, Own, GroupSync), size_t sme
     const void* kp = reinterpret_cast<const void*>(kernel);
     cudaError_t e = prep_smem(kp, smem);
     if (e != cudaSuccess) return e;
+    const LaunchKey key{current_device(), kp, smem, 1, kQueryBlocks};
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kp, kThreads, smem);
-    if (e != cudaSuccess) return e;
+    if (!cached(key, &per_sm)) {
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kp, kThreads, smem);
+        if (e != cudaSuccess) return e;
+        remember(key, per_sm);
+    }
     const uint64_t resident = static_cast<uint64_t>(per_sm) * ctx.caps.sms;
     if (resident < gs.G) return cudaErrorCooperativeLaunchTooLarge;
     gs.nG = static_cast<unsigned>(std::min<uint64_t>({a.items, resident / gs.G, static_cast<uint64_t>(max_groups)}));

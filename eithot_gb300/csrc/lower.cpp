@@ -70,10 +70,17 @@ double dsmem_penalty(uint64_t g, bool push) {
 }
 }  // namespace
 
+namespace {
+thread_local Tuning* t_scoped = nullptr;
+}  // namespace
+
 Tuning& tuning() {
     static Tuning t;
-    return t;
+    return t_scoped ? *t_scoped : t;
 }
+
+ScopedTuning::ScopedTuning(const Tuning& t) : t_(t), prev_(t_scoped) { t_scoped = &t_; }
+ScopedTuning::~ScopedTuning() { t_scoped = prev_; }
 
 namespace {
 // A CTA footprint at most this large lets two CTAs share an SM (GB300:
@@ -204,7 +211,8 @@ double cluster_utilisation(int K) {
 // large for a cluster, a global-memory barrier over a group of G
 // co-resident CTAs.  Candidates are costed by row-piece efficiency, SM
 // utilisation, halo re-reads and buffering.
-Staging plan_col_owner(uint64_t rows, uint64_t cols, uint64_t E, int fn, uint64_t b, const DeviceCaps& caps) {
+Staging plan_col_owner(uint64_t rows, uint64_t cols, uint64_t batches, uint64_t E, int fn, uint64_t b,
+                       const DeviceCaps& caps) {
     const size_t cap = smem_cap_of(caps);
     const int form = tuning().col_form;
     Staging best;
@@ -213,6 +221,29 @@ Staging plan_col_owner(uint64_t rows, uint64_t cols, uint64_t E, int fn, uint64_
     auto consider = [&](const Staging& s) {
         if (s.cost < best.cost) best = s;
     };
+    // short columns: one CTA stages every row of a tile of as many columns
+    // as its share of shared memory holds (slots indexed modulo the row
+    // count, no halo); enough tiles are left for every SM
+    if (form != 2 && E <= 128 && !tuning().col_chunk) {
+        for (bool db : {true, false}) {
+            if (db && !tuning().dbuf) continue;
+            const uint64_t budget = kTwoPerSm / (db ? 2 : 1);
+            const uint64_t tw_cap = std::min<uint64_t>(cols, budget / (rows * E));
+            if (tw_cap < 1 || tw_cap * E < 128) continue;
+            const uint64_t want_tiles = 4 * static_cast<uint64_t>(caps.sms);
+            const uint64_t tiles_per_batch = (want_tiles + std::max<uint64_t>(batches, 1) - 1) / std::max<uint64_t>(batches, 1);
+            uint64_t tw = std::min<uint64_t>(tw_cap, std::max<uint64_t>((cols + tiles_per_batch - 1) / tiles_per_batch,
+                                                                        (256 + E - 1) / E));
+            tw = std::max<uint64_t>(1, std::min(tw, tw_cap));
+            Staging s;
+            s.w = E; s.tw = tw; s.pitch = tw * E; s.K = 1; s.per_cta = rows * s.pitch;
+            s.item_bytes = rows * s.pitch; s.on_chip = true; s.dbuf = db;
+            s.owner = true; s.whole = true; s.per_sm = 2;
+            s.cost = 1.0 / piece_efficiency(s.pitch) + (db ? 0.0 : 0.1);
+            consider(s);
+            break;
+        }
+    }
     for (uint64_t tb : {uint64_t(512), uint64_t(256), uint64_t(128), uint64_t(64), uint64_t(32)}) {
         if (tuning().col_chunk && tb != static_cast<uint64_t>(tuning().col_chunk)) continue;
         uint64_t w, tw;
@@ -287,7 +318,7 @@ Staging plan_col_owner(uint64_t rows, uint64_t cols, uint64_t E, int fn, uint64_
 
 Staging plan_col_pass(const Pass& p, const DeviceCaps& caps) {
     if (tuning().col_owner) {
-        const Staging s = plan_col_owner(p.rows, p.cols, p.elem, p.fn, p.b, caps);
+        const Staging s = plan_col_owner(p.rows, p.cols, p.batches, p.elem, p.fn, p.b, caps);
         if (s.on_chip) return s;
     }
     return plan_col_staging(p.rows, p.elem, smem_cap_of(caps), p.cols);
@@ -314,9 +345,9 @@ namespace {
 double row_cost(uint64_t cols, uint64_t E, size_t cap, bool scatter) {
     return plan_row_staging(cols, E, cap, scatter).cost;
 }
-double col_cost(uint64_t rows, uint64_t cols, uint64_t E, int fn, uint64_t b, const DeviceCaps& caps) {
+double col_cost(uint64_t rows, uint64_t cols, uint64_t batches, uint64_t E, int fn, uint64_t b, const DeviceCaps& caps) {
     Pass p;
-    p.rows = rows; p.cols = cols; p.elem = E; p.fn = fn; p.b = b;
+    p.rows = rows; p.cols = cols; p.batches = batches; p.elem = E; p.fn = fn; p.b = b;
     return plan_col_pass(p, caps).cost;
 }
 
@@ -348,10 +379,10 @@ void lower_xpose(const Xpose& x, const DeviceCaps& caps, std::vector<Pass>* pass
     // Catanzaro: c2r on the R x C view, or r2c on the C x R view.
     uint64_t g, inv;
     gcd_inverse(x.R, x.C, &g, &inv);
-    const double c2r = (g > 1 ? col_cost(x.R, x.C, x.E, kFnC2RPreRot, x.C / g, caps) : 0.0) + row_cost(x.C, x.E, cap, false) +
-                       col_cost(x.R, x.C, x.E, kFnC2RColShuffle, x.C / g, caps);
-    const double r2c = col_cost(x.C, x.R, x.E, kFnR2CColShuffle, x.R / g, caps) + row_cost(x.R, x.E, cap, true) +
-                       (g > 1 ? col_cost(x.C, x.R, x.E, kFnR2CPostRot, x.R / g, caps) : 0.0);
+    const double c2r = (g > 1 ? col_cost(x.R, x.C, x.B, x.E, kFnC2RPreRot, x.C / g, caps) : 0.0) + row_cost(x.C, x.E, cap, false) +
+                       col_cost(x.R, x.C, x.B, x.E, kFnC2RColShuffle, x.C / g, caps);
+    const double r2c = col_cost(x.C, x.R, x.B, x.E, kFnR2CColShuffle, x.R / g, caps) + row_cost(x.R, x.E, cap, true) +
+                       (g > 1 ? col_cost(x.C, x.R, x.B, x.E, kFnR2CPostRot, x.R / g, caps) : 0.0);
     bool use_c2r = (c2r < r2c) || (c2r == r2c && x.C >= x.R);
     if (tuning().variant == 1) use_c2r = true;
     if (tuning().variant == 2) use_c2r = false;

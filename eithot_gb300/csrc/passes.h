@@ -82,6 +82,20 @@ struct Tuning {
 };
 Tuning& tuning();
 
+// Makes tuning() return `t` on the calling thread for the scope's lifetime
+// (the batched form lowers and runs its passes under its own knobs).
+class ScopedTuning {
+public:
+    explicit ScopedTuning(const Tuning& t);
+    ~ScopedTuning();
+    ScopedTuning(const ScopedTuning&) = delete;
+    ScopedTuning& operator=(const ScopedTuning&) = delete;
+
+private:
+    Tuning t_;
+    Tuning* prev_;
+};
+
 // How one item of a row or column pass is staged.  A row item is one strip
 // (w bytes of every element) of one row; a column item is one strip of a
 // tile of `tw` adjacent columns over all rows.  An item is split over the K
@@ -101,6 +115,7 @@ struct Staging {
     bool group = false;    // owner-computed over a group of G co-resident CTAs (global-memory
     int G = 0;             //   barrier, any size) instead of a thread-block cluster
     int per_sm = 1;        // CTAs per SM the footprint was sized for
+    bool whole = false;    // owner-computed, one CTA holds every row of a tile (short columns)
     double cost = 0;       // modelled time in units of one streaming pass
 };
 

@@ -78,8 +78,8 @@ typedef struct eithot_plan_info {
 /* Execution statistics of the last eithot_transpose* call on this thread. */
 typedef struct eithot_stats {
     size_t  workspace_bytes;   /* device scratch the call used */
-    size_t  free_before;       /* cudaMemGetInfo free bytes at entry */
-    size_t  free_after_alloc;  /* cudaMemGetInfo free bytes once scratch was allocated */
+    size_t  free_before;       /* cudaMemGetInfo free bytes at entry (0 unless profiling is on) */
+    size_t  free_after_alloc;  /* cudaMemGetInfo free bytes once scratch was allocated (idem) */
     int     n_passes;          /* device passes launched (excl. no-ops) */
     int     n_launches;        /* kernel launches issued */
     double  algorithmic_bytes; /* 2 * volume * elem_size */
@@ -140,6 +140,33 @@ int eithot_transpose_noalloc(void* d_data, size_t capacity_bytes, int rank,
 int eithot_workspace_size(int rank, const int64_t* dims, const int* perm_1based,
                           size_t elem_size, int num_sub_tensors, double alpha,
                           int reorder_type, size_t* bytes_out);
+
+/* ---- the batched form -------------------------------------------------------
+ * No reference counterpart (the reference transposes one tensor per call).
+ * eithot_batch_create plans `count` independent transposes once, host only:
+ * tensor t has rank ranks[t]; its dims and 1-based permutation are the next
+ * ranks[t] entries of `dims` and `perms_1based` (tensors back to back);
+ * elem_sizes[t] as for eithot_transpose; num_sub_tensors and alpha apply to
+ * every tensor.  eithot_batch_run transposes all of them in place
+ * (d_data[t] with capacities[t] bytes, as for eithot_transpose), issuing
+ * the work on up to 16 internal streams forked from and joined back into
+ * `stream`: the call is stream-ordered with respect to `stream` and returns
+ * before the device work completes.  d_workspace (NULL: the library takes
+ * it from cudaMallocAsync on `stream`) must hold
+ * eithot_batch_workspace_size() bytes.  A batch may be run any number of
+ * times, on any buffers of the planned shapes, on the device it was planned
+ * on; runs of one batch must not overlap.  eithot_batch_launches reports the
+ * kernel launches of the last run. */
+typedef struct eithot_batch eithot_batch;
+
+int eithot_batch_create(int count, const int* ranks, const int64_t* dims, const int* perms_1based,
+                        const size_t* elem_sizes, int num_sub_tensors, double alpha,
+                        eithot_batch** out);
+int eithot_batch_workspace_size(const eithot_batch* batch, size_t* bytes);
+int eithot_batch_run(eithot_batch* batch, void* const* d_data, const size_t* capacities,
+                     void* d_workspace, size_t workspace_bytes, void* stream);
+int eithot_batch_launches(const eithot_batch* batch, int* launches);
+int eithot_batch_destroy(eithot_batch* batch);
 
 /* ---- the extra-memory estimator --------------------------------------- */
 

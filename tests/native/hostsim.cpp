@@ -137,7 +137,7 @@ int hs_describe_staging(char* buf, size_t len, int rank, const int64_t* dims, co
             const Staging st = plan_col_pass(p, caps);
             char tmp[256];
             std::snprintf(tmp, sizeof(tmp), " | %s K=%d G=%d piece=%llu dbuf=%d per_cta=%llu halo=%llu+%llu cost=%.3f",
-                          !st.on_chip ? "staged" : st.group ? "group" : st.owner ? "cluster-owner" : "cluster-gather",
+                          !st.on_chip ? "staged" : st.group ? "group" : st.whole ? "whole-tile" : st.owner ? "cluster-owner" : "cluster-gather",
                           st.K, st.G, static_cast<unsigned long long>(st.pitch), st.dbuf ? 1 : 0,
                           static_cast<unsigned long long>(st.per_cta), static_cast<unsigned long long>(st.hlo),
                           static_cast<unsigned long long>(st.hhi), st.cost);

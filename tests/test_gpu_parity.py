@@ -245,8 +245,14 @@ def test_config2_full_size(E):
     estimator, extra device memory within alpha * bytes."""
     dims, perm = [4, 20011, 8192, 2], [1, 3, 2, 4]
     nb, alpha, _ = E.estimate(dims, perm, 4)
-    st = run_case(E, dims, perm, 4, nb, alpha, seed=0xE17407)
+    E.set_profiling(True)  # fills the free-memory fields of the stats
+    try:
+        st = run_case(E, dims, perm, 4, nb, alpha, seed=0xE17407)
+    finally:
+        E.set_profiling(False)
+        E.profile_reset()
     n = math.prod(dims)
+    assert st["free_before"] > 0
     assert st["workspace_bytes"] <= alpha * n * 4 * 1.0001
     assert st["free_before"] - st["free_after_alloc"] <= alpha * n * 4 * 1.05 + (64 << 20)
 
