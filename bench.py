@@ -55,6 +55,11 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--dims", default=None,
                     help="comma-separated dims overriding the workload (small cases for ncu captures)")
+    ap.add_argument("--workload", default="transpose", choices=["transpose", "batched", "served"],
+                    help="transpose: the default line; batched: 4096 mixed tensors through the batched form "
+                         "against one call per tensor; served: Poisson-arriving requests through the server "
+                         "against serial calls")
+    ap.add_argument("--count", type=int, default=0, help="tensors (batched) or requests (served); 0: default")
     return ap.parse_args()
 
 
@@ -398,10 +403,203 @@ def run_eithot(args):
     return 0
 
 
+def mixed_tensors(count, seed, min_bytes, max_bytes, min_rank, max_rank):
+    """Seeded tensors: rank uniform in [min_rank, max_rank], total bytes
+    log-uniform in [min_bytes, max_bytes] split over the dims log-uniformly,
+    a uniform random permutation, element size uniform in {1, 2, 4, 8}."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        r = int(rng.integers(min_rank, max_rank + 1))
+        elem = int(rng.choice([1, 2, 4, 8]))
+        total = math.exp(rng.uniform(math.log(min_bytes), math.log(max_bytes)))
+        n = max(1, int(total / elem))
+        w = rng.uniform(0.05, 1.0, size=r)
+        w = w / w.sum() * math.log(n)
+        dims = [max(1, int(round(math.exp(x)))) for x in w]
+        perm = [int(x) + 1 for x in rng.permutation(r)]
+        out.append((dims, perm, elem))
+    return out
+
+
+def run_batched(args):
+    """4096 tensors of 4 KB-64 MB, rank 3-6: the batched form against one
+    eithot_transpose call per tensor on one stream (both device-resident,
+    wall-clock from the first issue to the device being idle)."""
+    import numpy as np
+    import torch
+    import eithot_gb300 as E
+    dev = torch.device("cuda", 0)
+    ts = mixed_tensors(args.count or 4096, 4, 4096, 64 << 20, 3, 6)
+    sizes = [math.prod(d) * e for d, p, e in ts]
+    caps = [int(s * 1.03) + 256 for s in sizes]
+    offs = np.cumsum([0] + [(c + 255) // 256 * 256 for c in caps])
+    buf = torch.empty(int(offs[-1]), dtype=torch.uint8, device=dev)
+    ptrs = [buf.data_ptr() + int(o) for o in offs[:-1]]
+    st = torch.cuda.current_stream(dev)
+    for t, ((d, p, e), q) in enumerate(zip(ts, ptrs)):
+        E.fill_hash_ptr(q, math.prod(d), e, SEED + t, 0, st.cuda_stream)
+    batch = E.Batch(ts)
+    ws = torch.empty(max(1, batch.workspace_size), dtype=torch.uint8, device=dev)
+    batch.run(ptrs, caps, ws.data_ptr(), batch.workspace_size, st.cuda_stream)
+    bad = 0
+    for t, ((d, p, e), q) in enumerate(zip(ts, ptrs)):
+        bad += E.check_hash_ptr(q, d, p, e, SEED + t, st.cuda_stream)[0]
+    if bad or E.index_faults() or E.sync_timeouts():
+        raise SystemExit("bench: batched run wrong (%d mismatching elements)" % bad)
+
+    def timed(fn):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize(dev)
+        return time.perf_counter() - t0
+
+    def plain():
+        for (d, p, e), q, c in zip(ts, ptrs, caps):
+            E.transpose_ptr(q, c, d, p, e, 1, 0.01, E.ORDER_MIXED, st.cuda_stream)
+
+    def batched():
+        batch.run(ptrs, caps, ws.data_ptr(), batch.workspace_size, st.cuda_stream)
+
+    plain()
+    t_plain = statistics.median(timed(plain) for _ in range(max(3, args.steps // 4)))
+    t_batch = statistics.median(timed(batched) for _ in range(max(3, args.steps // 4)))
+    total = sum(sizes)
+    line = {"metric": "batched in-place GB/s (2*bytes/s), %d mixed tensors" % len(ts), "value": 2 * total / t_batch / 1e9,
+            "unit": "GB/s", "higher_is_better": True, "n_gpus": 1, "ms_per_batch": t_batch * 1e3,
+            "one_at_a_time": {"value": 2 * total / t_plain / 1e9, "ms": t_plain * 1e3},
+            "speedup_vs_one_at_a_time": t_plain / t_batch, "launches_per_batch": batch.launches,
+            "data": "synthetic (seeded counter hash per tensor, checked on the device after the first run)",
+            "config": {"workload": "4096 tensors, rank U{3..6}, bytes log-uniform [4 KB, 64 MB], elem U{1,2,4,8}, "
+                                   "random permutations (seed 4)", "tensors": len(ts), "bytes": total}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+class _Arena:
+    """First-fit placement of request tensors in one device buffer."""
+
+    def __init__(self, size):
+        self.free = [(0, size)]
+
+    def take(self, n):
+        n = (n + 255) // 256 * 256
+        for i, (o, l) in enumerate(self.free):
+            if l >= n:
+                self.free[i] = (o + n, l - n)
+                return o
+        return None
+
+    def give(self, o, n):
+        n = (n + 255) // 256 * 256
+        self.free.append((o, n))
+        self.free.sort()
+        merged = []
+        for a, l in self.free:
+            if merged and merged[-1][0] + merged[-1][1] == a:
+                merged[-1] = (merged[-1][0], merged[-1][1] + l)
+            elif l:
+                merged.append((a, l))
+        self.free = merged
+
+
+def run_served(args):
+    """Poisson arrivals (200 requests/s, seeded) of tensors of 1 MB-40 GB,
+    rank 2-8, resident in one device arena: the server (4 streams, 5 %
+    workspace pool, continuous batching) against serial eithot_transpose
+    calls in arrival order.  Latency = finish - arrival."""
+    import numpy as np
+    import torch
+    import eithot_gb300 as E
+    dev = torch.device("cuda", 0)
+    count = args.count or 200
+    reqs = mixed_tensors(count, 5, 1 << 20, 40 << 30, 2, 8)
+    rng = np.random.default_rng(6)
+    arrivals = np.cumsum(rng.exponential(1.0 / 200.0, size=count))
+    sizes = [math.prod(d) * e for d, p, e in reqs]
+    free, _ = torch.cuda.mem_get_info(dev)
+    arena_bytes = int(min(free * 0.55, 160e9))
+    arena = torch.empty(arena_bytes, dtype=torch.uint8, device=dev)
+    base = arena.data_ptr()
+    # the pool holds the largest request's scratch plus room for batches
+    pool = max(E.workspace_size(d, p, e, 1, 0.05) for d, p, e in reqs) + (256 << 20)
+
+    def drive(serial):
+        alloc = _Arena(arena_bytes)
+        srv = None if serial else E.Server(pool, streams=4)
+        st = torch.cuda.Stream(dev)
+        placed, start, finish = {}, None, {}
+        nxt = 0
+        t0 = time.perf_counter()
+        waiting = []
+        while len(finish) < count:
+            now = time.perf_counter() - t0
+            while nxt < count and arrivals[nxt] <= now:
+                waiting.append(nxt)
+                nxt += 1
+            if serial:
+                if waiting:
+                    i = waiting.pop(0)
+                    d, p, e = reqs[i]
+                    o = alloc.take(sizes[i] + 256)
+                    E.transpose_ptr(base + o, sizes[i] + 256, d, p, e, 1, 0.05, E.ORDER_MIXED, st.cuda_stream)
+                    st.synchronize()
+                    finish[i] = time.perf_counter() - t0
+                    alloc.give(o, sizes[i] + 256)
+                elif nxt < count:
+                    time.sleep(max(0.0, min(0.001, arrivals[nxt] - now)))
+                continue
+            while waiting:
+                i = waiting[0]
+                o = alloc.take(sizes[i] + 256)
+                if o is None:
+                    break
+                d, p, e = reqs[i]
+                tk = srv.submit(base + o, sizes[i] + 256, d, p, e, 1, 0.05)
+                placed[tk] = (i, o)
+                waiting.pop(0)
+            for tk in srv.poll():
+                i, o = placed.pop(tk)
+                finish[i] = time.perf_counter() - t0
+                alloc.give(o, sizes[i] + 256)
+            if not placed and not waiting and nxt < count:
+                time.sleep(max(0.0, min(0.001, arrivals[nxt] - (time.perf_counter() - t0))))
+        if srv:
+            srv.close()
+        lat = np.array([finish[i] - arrivals[i] for i in range(count)])
+        span = max(finish.values())
+        return lat, span
+
+    drive(False)  # warm every kernel the requests need
+    lat_s, span_s = drive(True)
+    lat_v, span_v = drive(False)
+    if E.index_faults() or E.sync_timeouts():
+        raise SystemExit("bench: served run reported index faults or sync timeouts")
+    total = sum(sizes)
+    line = {"metric": "served in-place transposes: p50/p99 latency and GB/s", "unit": "ms", "higher_is_better": False,
+            "n_gpus": 1, "value": float(np.percentile(lat_v, 99) * 1e3),
+            "served": {"p50_ms": float(np.percentile(lat_v, 50) * 1e3), "p99_ms": float(np.percentile(lat_v, 99) * 1e3),
+                       "GBs": 2 * total / span_v / 1e9, "span_s": span_v},
+            "serial": {"p50_ms": float(np.percentile(lat_s, 50) * 1e3), "p99_ms": float(np.percentile(lat_s, 99) * 1e3),
+                       "GBs": 2 * total / span_s / 1e9, "span_s": span_s},
+            "data": "synthetic shapes; tensor contents are not generated (the kernels move bytes whatever they hold)",
+            "config": {"workload": "%d requests, Poisson 200/s (seed 6), rank U{2..8}, bytes log-uniform [1 MB, 40 GB], "
+                                   "elem U{1,2,4,8}, random permutations (seed 5), alpha 0.05" % count,
+                       "bytes": total, "server": {"streams": 4, "workspace_pool_bytes": pool}}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batched":
+        return run_batched(args)
+    if args.workload == "served":
+        return run_served(args)
     return run_eithot(args)
 
 

@@ -83,6 +83,14 @@ def _load():
                                      ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
     lib.eithot_batch_launches.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
     lib.eithot_batch_destroy.argtypes = [ctypes.c_void_p]
+    lib.eithot_server_create.argtypes = [ctypes.c_size_t, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
+    lib.eithot_server_submit.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, I64P, IP,
+                                         ctypes.c_size_t, ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_uint64)]
+    lib.eithot_server_poll.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64), ctypes.c_int,
+                                       ctypes.POINTER(ctypes.c_int)]
+    lib.eithot_server_pending.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+    lib.eithot_server_launches.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
+    lib.eithot_server_destroy.argtypes = [ctypes.c_void_p]
     lib.eithot_tune_set.argtypes = [ctypes.c_char_p, ctypes.c_double]
     lib.eithot_tune_get.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double)]
     return lib
@@ -294,6 +302,56 @@ class Batch:
     def close(self):
         if self._h:
             lib.eithot_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """The served form (eithot_server_*): submit resident tensors, poll for
+    the tickets of finished ones."""
+
+    def __init__(self, workspace_bytes: int, streams: int = 4):
+        h = ctypes.c_void_p()
+        _check(lib.eithot_server_create(workspace_bytes, streams, ctypes.byref(h)))
+        self._h = h
+        self._done = (ctypes.c_uint64 * 4096)()
+
+    def submit(self, ptr: int, capacity_bytes: int, dims, perm, elem_size: int, num_sub_tensors: int = 1,
+               alpha: float = 0.01) -> int:
+        r, d, p = _arrays(dims, perm)
+        t = ctypes.c_uint64()
+        _check(lib.eithot_server_submit(self._h, ctypes.c_void_p(ptr), capacity_bytes, r, d, p, elem_size,
+                                        num_sub_tensors, alpha, ctypes.byref(t)))
+        return t.value
+
+    def poll(self) -> List[int]:
+        out = []
+        while True:
+            n = ctypes.c_int()
+            _check(lib.eithot_server_poll(self._h, self._done, len(self._done), ctypes.byref(n)))
+            out += list(self._done[: n.value])
+            if n.value < len(self._done):
+                return out
+
+    def pending(self):
+        q, r = ctypes.c_int(), ctypes.c_int()
+        _check(lib.eithot_server_pending(self._h, ctypes.byref(q), ctypes.byref(r)))
+        return q.value, r.value
+
+    @property
+    def launches(self) -> int:
+        v = ctypes.c_int()
+        _check(lib.eithot_server_launches(self._h, ctypes.byref(v)))
+        return v.value
+
+    def close(self):
+        if self._h:
+            lib.eithot_server_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -28,7 +28,7 @@ CLI_PROGRAMS = {"test_inplace": "test_inplace.cpp", "Nd_estimation": "nd_estimat
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["kernels.cu", "checks.cu"]
-CPP_SOURCES = ["plan.cpp", "lower.cpp", "estimator.cpp", "capi.cpp", "batch.cpp"]
+CPP_SOURCES = ["plan.cpp", "lower.cpp", "estimator.cpp", "capi.cpp", "batch.cpp", "server.cpp"]
 
 
 def cuda_home() -> str:

@@ -30,7 +30,12 @@ size_t smem_cap_of(const DeviceCaps& caps) {
     return caps.smem_optin > 2048 ? caps.smem_optin - 2048 : caps.smem_optin;
 }
 
-uint64_t strip_width(uint64_t E) { return E <= 128 ? E : 128; }
+uint64_t strip_width(uint64_t E, uint64_t count, uint64_t budget) {
+    if (E <= 128) return E;
+    const uint64_t w = budget / std::max<uint64_t>(count, 1) / 128 * 128;
+    if (w >= E) return E;
+    return std::max<uint64_t>(128, w);
+}
 
 namespace {
 uint64_t pow2_divisor(uint64_t v, uint64_t cap) {
@@ -93,8 +98,8 @@ constexpr double kOnePerSmPenalty = 0.25;
 Staging plan_row_staging(uint64_t cols, uint64_t E, size_t cap, bool scatter) {
     (void)scatter;
     Staging s;
-    const uint64_t w0 = strip_width(E);
-    for (uint64_t w : {w0, uint64_t(64), uint64_t(32)}) {
+    const uint64_t w0 = strip_width(E, cols, kWideStripBytes);
+    for (uint64_t w : {w0, uint64_t(128), uint64_t(64), uint64_t(32)}) {
         if (w > w0 || w < std::min<uint64_t>(E, 32)) continue;
         // a whole row strip in one CTA
         if (cols * w <= cap) {
@@ -105,7 +110,7 @@ Staging plan_row_staging(uint64_t cols, uint64_t E, size_t cap, bool scatter) {
         }
     }
     for (uint64_t occ_limit : {kTwoPerSm, static_cast<uint64_t>(cap)}) {
-        for (uint64_t w : {w0, uint64_t(64), uint64_t(32)}) {
+        for (uint64_t w : {w0, uint64_t(128), uint64_t(64), uint64_t(32)}) {
             if (w > w0 || w < std::min<uint64_t>(E, 32)) continue;
             for (int K : kClusterSizes) {
                 if (K > tuning().max_cluster) break;
@@ -362,8 +367,8 @@ std::string geom(const char* name, uint64_t B, uint64_t r, uint64_t c, uint64_t 
 void lower_xpose(const Xpose& x, const DeviceCaps& caps, std::vector<Pass>* passes) {
     if (x.B == 0 || x.R <= 1 || x.C <= 1) return;  // identity
     const size_t cap = smem_cap_of(caps);
-    const uint64_t w0 = strip_width(x.E);
-    for (uint64_t w : {w0, uint64_t(64), uint64_t(32)}) {
+    const uint64_t w0 = strip_width(x.E, x.R * x.C, kWideStripBytes);
+    for (uint64_t w : {w0, uint64_t(128), uint64_t(64), uint64_t(32)}) {
         if (w > w0 || w < std::min<uint64_t>(x.E, 32)) continue;
         if (slab_smem_bytes(x.R, x.C, w) <= cap) {
             Pass p;

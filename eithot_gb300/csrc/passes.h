@@ -156,8 +156,11 @@ void gcd_inverse(uint64_t a, uint64_t b, uint64_t* g, uint64_t* inv);
 uint64_t slab_pitch(uint64_t C, uint64_t w);
 size_t slab_smem_bytes(uint64_t R, uint64_t C, uint64_t w);
 
-// Strip width (bytes) for elements of E bytes: whole elements up to 128 B,
-// 128-byte strips of larger elements.
-uint64_t strip_width(uint64_t E);
+// Strip width (bytes) for elements of E bytes when `count` elements are
+// staged together: whole elements up to 128 B; wider elements in strips of
+// a multiple of 128 B, as wide as keeps count * strip within `budget`
+// (few, very wide elements move in long contiguous strips).
+constexpr uint64_t kWideStripBytes = 32 * 1024;
+uint64_t strip_width(uint64_t E, uint64_t count, uint64_t budget);
 
 }  // namespace eithot

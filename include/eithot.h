@@ -168,6 +168,31 @@ int eithot_batch_run(eithot_batch* batch, void* const* d_data, const size_t* cap
 int eithot_batch_launches(const eithot_batch* batch, int* launches);
 int eithot_batch_destroy(eithot_batch* batch);
 
+/* ---- the served form ---------------------------------------------------------
+ * No reference counterpart.  A server takes requests for in-place
+ * transposes of tensors already resident on the device and runs them on
+ * `streams` executor streams (1..16) with scratch from a pool of
+ * `workspace_bytes` device bytes that eithot_server_create allocates once
+ * (admission: a request whose scratch can never fit the pool is refused
+ * with EITHOT_EBUSY; one that does not fit now waits).  Requests run in
+ * arrival order; consecutive requests under 64 MB at the head of the queue
+ * are run together as one batch (continuous batching), larger ones alone.
+ * The server has no thread of its own: work is retired and dispatched
+ * inside eithot_server_submit and eithot_server_poll, which never block.
+ * eithot_server_poll hands back up to max_done tickets of finished
+ * requests; a request's buffer must stay untouched until its ticket comes
+ * back.  eithot_server_destroy waits for the work in flight. */
+typedef struct eithot_server eithot_server;
+
+int eithot_server_create(size_t workspace_bytes, int streams, eithot_server** out);
+int eithot_server_submit(eithot_server* server, void* d_data, size_t capacity_bytes, int rank,
+                         const int64_t* dims, const int* perm_1based, size_t elem_size,
+                         int num_sub_tensors, double alpha, uint64_t* ticket);
+int eithot_server_poll(eithot_server* server, uint64_t* done, int max_done, int* n_done);
+int eithot_server_pending(const eithot_server* server, int* queued, int* running);
+int eithot_server_launches(const eithot_server* server, int* launches);
+int eithot_server_destroy(eithot_server* server);
+
 /* ---- the extra-memory estimator --------------------------------------- */
 
 /* Replaces Nd_estimation (Nd_memory_estimation/src/test_inplace.cpp:19-147):

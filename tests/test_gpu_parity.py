@@ -162,6 +162,16 @@ def test_many_small_matrices(E, tuned, dims, perm, elem, pack):
     run_case(E, dims, perm, elem)
 
 
+@pytest.mark.parametrize("dims,perm,elem", [([3000, 3, 200], [1, 3, 2], 4), ([5000, 16, 2], [1, 3, 2], 2),
+                                            ([20000, 5, 7], [1, 3, 2], 1), ([4001, 3, 50], [1, 3, 2], 3),
+                                            ([2048, 2, 3, 40], [1, 4, 3, 2], 8), ([100000, 3, 2], [1, 3, 2], 4)])
+def test_few_very_wide_elements(E, dims, perm, elem):
+    """Elements of many KB (a permutation that keeps a large leading block
+    together): rows and slabs staged in strips of up to 32 KB, with a
+    shorter last strip."""
+    run_case(E, dims, perm, elem)
+
+
 def test_bounded_wait_gives_up(E):
     """A group-barrier wait that nothing releases gives up after its bound,
     is counted, and leaves the context usable."""
