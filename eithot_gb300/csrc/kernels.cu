@@ -158,6 +158,87 @@ __global__ void __launch_bounds__(kThreads) k_slab(SlabArgs a) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Slab transpose of a matrix over a K-CTA cluster, owner-computed: CTA k
+// stages input rows [k*Q, (k+1)*Q) and, after the cluster barrier, writes
+// its band's segment of every output row (output row c, positions k*Q ..
+// k*Q+Q-1) from its own shared memory.  One pass for matrices up to K x
+// 110 KB; the barrier only orders every CTA's loads of a matrix before any
+// CTA's writes to it.  kPack > 1: elements of US bytes packed kPack to a
+// 4-byte store.
+// ---------------------------------------------------------------------------
+struct SlabClusterArgs {
+    uint8_t* base;
+    uint64_t items, mat_bytes, row_bytes;
+    uint32_t R, C, E, Q, pitch, upr, upw;
+    FastDiv32 div_upr, div_upw, div_Qupw, div_Qpack;
+};
+
+template <int US, int kPack>
+__global__ void __launch_bounds__(kThreads) k_slab_cluster(SlabClusterArgs a) {
+    using U = typename UnitOf<US>::T;
+    extern __shared__ __align__(16) uint8_t smem[];
+    cg::cluster_group cl = cg::this_cluster();
+    const unsigned K = cl.num_blocks();
+    const unsigned kr = cl.block_rank();
+    const uint64_t cid = blockIdx.x / K, ncl = gridDim.x / K;
+    const uint32_t r0 = kr * a.Q;
+    const uint32_t nr = r0 < a.R ? min(a.Q, a.R - r0) : 0;
+    for (uint64_t it = cid; it < a.items; it += ncl) {
+        uint8_t* mat = a.base + it * a.mat_bytes;
+        const uint8_t* band = mat + static_cast<uint64_t>(r0) * a.row_bytes;
+        const uint32_t in_units = nr * a.upr;
+        for (uint32_t x = threadIdx.x; x < in_units; x += blockDim.x) {
+            uint32_t rr, cu;
+            a.div_upr.divmod(x, rr, cu);
+            copy_in<US, U>(smem + rr * a.pitch + cu * US, band + static_cast<uint64_t>(x) * US);
+        }
+        copy_in_wait<US>();
+        cluster_sync_reuse();  // every CTA holds its band: writes may start
+        if constexpr (kPack > 1) {
+            const uint32_t groups = a.C * (a.Q / kPack);
+            for (uint32_t x = threadIdx.x; x < groups; x += blockDim.x) {
+                uint32_t c, g;
+                a.div_Qpack.divmod(x, c, g);
+                const uint32_t rr = g * kPack;
+                if (rr >= nr) continue;  // nr is a multiple of kPack
+                uint32_t word = 0;
+#pragma unroll
+                for (int k = 0; k < kPack; ++k)
+                    word |= static_cast<uint32_t>(*reinterpret_cast<const U*>(smem + (rr + k) * a.pitch + c * US))
+                            << (8 * US * k);
+                *reinterpret_cast<uint32_t*>(mat + (static_cast<uint64_t>(c) * a.R + r0 + rr) * US) = word;
+            }
+        } else {
+            const uint32_t out_units = a.C * a.Q * a.upw;
+            for (uint32_t x = threadIdx.x; x < out_units; x += blockDim.x) {
+                uint32_t c, rest, rr, u;
+                a.div_Qupw.divmod(x, c, rest);
+                a.div_upw.divmod(rest, rr, u);
+                if (rr >= nr) continue;
+                *reinterpret_cast<U*>(mat + (static_cast<uint64_t>(c) * a.R + r0 + rr) * a.E + u * US) =
+                    *reinterpret_cast<const U*>(smem + rr * a.pitch + c * a.E + u * US);
+            }
+        }
+        __syncthreads();  // the band's buffer is free for the next matrix
+    }
+}
+
+// Copies `bytes` contiguous bytes from global memory into shared memory:
+// 16-byte cp.async chunks when both ends and the size allow it (vec16),
+// else US-byte units.  Completes before returning.
+template <int US>
+__device__ __forceinline__ void block_copy_in(uint8_t* sm, const uint8_t* g, uint32_t bytes, bool vec16) {
+    using U = typename UnitOf<US>::T;
+    if (vec16) {
+        for (uint32_t x = threadIdx.x; x < bytes / 16; x += blockDim.x) copy_in<16, uint4>(sm + x * 16, g + x * 16);
+        copy_in_wait<16>();
+    } else {
+        for (uint32_t x = threadIdx.x; x < bytes / US; x += blockDim.x) copy_in<US, U>(sm + x * US, g + x * US);
+        copy_in_wait<US>();
+    }
+}
+
 // Small matrices (a few KB or less): an item is a block of k consecutive
 // matrices, loaded contiguously; every output element reads its input in
 // shared memory.  Millions of 3x5 matrices would otherwise take one CTA item
@@ -166,10 +247,11 @@ struct SlabPackArgs {
     uint8_t* base;
     uint64_t batches, items, mat_bytes, E;
     uint32_t k, R, C, upw, mat_units;
+    bool vec16;  // base and matrix size are 16-byte multiples
     FastDiv32 div_mat_units, div_upw, div_R;
 };
 
-template <int US>
+template <int US, int kPack>
 __global__ void __launch_bounds__(kThreads) k_slab_pack(SlabPackArgs a) {
     using U = typename UnitOf<US>::T;
     extern __shared__ __align__(16) uint8_t smem[];
@@ -179,16 +261,33 @@ __global__ void __launch_bounds__(kThreads) k_slab_pack(SlabPackArgs a) {
         const uint32_t nm = static_cast<uint32_t>(left < a.k ? left : a.k);
         uint8_t* blk = a.base + m0 * a.mat_bytes;
         const uint32_t units = nm * a.mat_units;
-        for (uint32_t x = threadIdx.x; x < units; x += blockDim.x) copy_in<US, U>(smem + x * US, blk + x * US);
-        copy_in_wait<US>();
+        block_copy_in<US>(smem, blk, units * US, a.vec16 && (units * US) % 16 == 0);
         __syncthreads();
-        for (uint32_t x = threadIdx.x; x < units; x += blockDim.x) {
-            uint32_t m, rest, o, u, c, r;
-            a.div_mat_units.divmod(x, m, rest);
-            a.div_upw.divmod(rest, o, u);
-            a.div_R.divmod(o, c, r);  // output o = c*R + r holds input (r, c)
-            const uint32_t src = m * a.mat_units + (r * a.C + c) * a.upw + u;
-            *reinterpret_cast<U*>(blk + static_cast<uint64_t>(x) * US) = *reinterpret_cast<const U*>(smem + src * US);
+        if constexpr (kPack > 1) {
+            // kPack consecutive outputs of one output row (R is a multiple
+            // of kPack) gathered into one 4-byte store
+            const uint32_t groups = units / kPack;
+            for (uint32_t g = threadIdx.x; g < groups; g += blockDim.x) {
+                const uint32_t x = g * kPack;
+                uint32_t m, o, c, r;
+                a.div_mat_units.divmod(x, m, o);
+                a.div_R.divmod(o, c, r);
+                uint32_t word = 0;
+#pragma unroll
+                for (int k = 0; k < kPack; ++k)
+                    word |= static_cast<uint32_t>(*reinterpret_cast<const U*>(smem + (m * a.mat_units + (r + k) * a.C + c) * US))
+                            << (8 * US * k);
+                *reinterpret_cast<uint32_t*>(blk + static_cast<uint64_t>(x) * US) = word;
+            }
+        } else {
+            for (uint32_t x = threadIdx.x; x < units; x += blockDim.x) {
+                uint32_t m, rest, o, u, c, r;
+                a.div_mat_units.divmod(x, m, rest);
+                a.div_upw.divmod(rest, o, u);
+                a.div_R.divmod(o, c, r);  // output o = c*R + r holds input (r, c)
+                const uint32_t src = m * a.mat_units + (r * a.C + c) * a.upw + u;
+                *reinterpret_cast<U*>(blk + static_cast<uint64_t>(x) * US) = *reinterpret_cast<const U*>(smem + src * US);
+            }
         }
         __syncthreads();
     }
@@ -341,6 +440,7 @@ struct RowBlockArgs {
     uint8_t* base;
     uint64_t total_rows, items, row_bytes, E;
     uint32_t k, cols, upw, units_per_row;
+    bool vec16;                // base and row size are 16-byte multiples
     FastDiv div_rows;          // global row -> row within its matrix
     FastDiv32 div_units_row;   // unit of the block -> (row of the block, unit of the row)
     FastDiv32 div_upw;
@@ -357,8 +457,7 @@ __global__ void __launch_bounds__(kThreads) k_row_block(RowBlockArgs a, Fn fn) {
         const uint32_t nr = static_cast<uint32_t>(left < a.k ? left : a.k);
         uint8_t* blk = a.base + r0 * a.row_bytes;
         const uint32_t units = nr * a.units_per_row;
-        for (uint32_t x = threadIdx.x; x < units; x += blockDim.x) copy_in<US, U>(smem + x * US, blk + x * US);
-        if constexpr (US >= 4) asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+        block_copy_in<US>(smem, blk, units * US, a.vec16 && (units * US) % 16 == 0);
         __syncthreads();
         for (uint32_t x0 = threadIdx.x; x0 < units; x0 += kBatch * blockDim.x) {
             U v[kBatch];
@@ -1119,8 +1218,8 @@ constexpr size_t kRowSoloMinBytes = 110 * 1024;
 constexpr uint64_t kRowBlockBytes = 48 * 1024;
 constexpr uint64_t kRowBlockMinRows = 8;
 // Matrices this small are transposed k at a time by k_slab_pack.
-constexpr uint64_t kSlabPackBytes = 48 * 1024;
-constexpr uint64_t kSlabPackMinMats = 8;
+constexpr uint64_t kSlabPackBytes = 64 * 1024;
+constexpr uint64_t kSlabPackMinMats = 4;
 
 // ---- slab ----------------------------------------------------------------
 template <int US>
@@ -1141,11 +1240,21 @@ int launch_slab(uint8_t* data, const Pass& p, ExecContext& ctx) {
         b.div_mat_units = FastDiv32::make(b.mat_units);
         b.div_upw = FastDiv32::make(b.upw);
         b.div_R = FastDiv32::make(b.R);
+        b.vec16 = reinterpret_cast<uintptr_t>(b.base) % 16 == 0 && mat_bytes % 16 == 0;
         const size_t smem = (static_cast<size_t>(b.k) * mat_bytes + 127) / 128 * 128;
-        const void* k = reinterpret_cast<const void*>(&k_slab_pack<US>);
-        EI_CHECK(prep_smem(k, smem));
-        const int grid = grid_for(k, smem, b.items, ctx);
-        k_slab_pack<US><<<grid, kThreads, smem, ctx.stream>>>(b);
+        constexpr int kPack = US < 4 ? 4 / US : 1;
+        const uint64_t addr = reinterpret_cast<uintptr_t>(b.base);
+        if (kPack > 1 && p.elem == US && p.rows % kPack == 0 && addr % 4 == 0 && mat_bytes % 4 == 0) {
+            const void* k = reinterpret_cast<const void*>(&k_slab_pack<US, kPack>);
+            EI_CHECK(prep_smem(k, smem));
+            const int grid = grid_for(k, smem, b.items, ctx);
+            k_slab_pack<US, kPack><<<grid, kThreads, smem, ctx.stream>>>(b);
+        } else {
+            const void* k = reinterpret_cast<const void*>(&k_slab_pack<US, 1>);
+            EI_CHECK(prep_smem(k, smem));
+            const int grid = grid_for(k, smem, b.items, ctx);
+            k_slab_pack<US, 1><<<grid, kThreads, smem, ctx.stream>>>(b);
+        }
         EI_CHECK(cudaGetLastError());
         ctx.launches++;
         return 0;
@@ -1179,6 +1288,46 @@ int launch_slab(uint8_t* data, const Pass& p, ExecContext& ctx) {
     return 0;
 }
 
+template <int US>
+int launch_slab_cluster(uint8_t* data, const Pass& p, ExecContext& ctx) {
+    if constexpr (US > 4) {  // staged rows sit at a pitch of odd 4-byte words
+        ctx.err = "internal: cluster slab with a unit above 4 bytes";
+        return EITHOT_STATUS_INVALID;
+    } else {
+    SlabClusterArgs a;
+    a.base = data + p.offset;
+    a.items = p.batches;
+    a.row_bytes = p.cols * p.elem;
+    a.mat_bytes = p.rows * a.row_bytes;
+    a.R = static_cast<uint32_t>(p.rows);
+    a.C = static_cast<uint32_t>(p.cols);
+    a.E = static_cast<uint32_t>(p.elem);
+    a.pitch = static_cast<uint32_t>(slab_cluster_pitch(a.row_bytes));
+    const int K = p.cluster;
+    a.upr = static_cast<uint32_t>(a.row_bytes / US);
+    a.upw = static_cast<uint32_t>(p.elem / US);
+    // pack 4/US elements to a 4-byte store when every store stays aligned
+    constexpr int kPack = US < 4 ? 4 / US : 1;
+    const uint64_t addr = reinterpret_cast<uintptr_t>(a.base);
+    uint32_t Q = static_cast<uint32_t>((p.rows + K - 1) / K);
+    const bool pack = kPack > 1 && p.elem == US && p.rows % kPack == 0 && addr % 4 == 0 && a.mat_bytes % 4 == 0;
+    if (pack) Q = (Q + kPack - 1) / kPack * kPack;
+    a.Q = Q;
+    a.div_upr = FastDiv32::make(a.upr);
+    a.div_upw = FastDiv32::make(a.upw);
+    a.div_Qupw = FastDiv32::make(static_cast<uint64_t>(Q) * a.upw);
+    a.div_Qpack = FastDiv32::make(kPack > 1 ? Q / kPack : 1);
+    const size_t smem = (static_cast<size_t>(Q) * a.pitch + 127) / 128 * 128;
+    if (pack)
+        EI_CHECK(launch_clusters(k_slab_cluster<US, kPack>, K, smem, a.items, ctx, a));
+    else
+        EI_CHECK(launch_clusters(k_slab_cluster<US, 1>, K, smem, a.items, ctx, a));
+    EI_CHECK(cudaGetLastError());
+    ctx.launches++;
+    return 0;
+    }
+}
+
 // ---- rows ------------------------------------------------------------------
 
 template <int US, typename Fn, bool kScatter>
@@ -1205,6 +1354,7 @@ int launch_row(uint8_t* data, const Pass& p, const FnOnChip& fn, const Fn64& fn6
             b.div_rows = FastDiv::make(p.rows, b.total_rows);
             b.div_units_row = FastDiv32::make(b.units_per_row);
             b.div_upw = FastDiv32::make(b.upw);
+            b.vec16 = reinterpret_cast<uintptr_t>(b.base) % 16 == 0 && row_bytes % 16 == 0;
             const size_t smem = (static_cast<size_t>(b.k) * row_bytes + 127) / 128 * 128;
             const void* k = reinterpret_cast<const void*>(&k_row_block<US, FnOnChip>);
             EI_CHECK(prep_smem(k, smem));
@@ -1551,6 +1701,7 @@ template <int US>
 int run_pass_u(uint8_t* data, const Pass& p, ExecContext& ctx) {
     switch (p.type) {
         case kSlabTranspose: return launch_slab<US>(data, p, ctx);
+        case kSlabCluster: return launch_slab_cluster<US>(data, p, ctx);
         case kRowGather:
         case kRowScatter: {
             // A row pass is run as a gather when one CTA holds the whole row
@@ -1615,6 +1766,8 @@ uint64_t pass_unit(const uint8_t* data, const Pass& p, const DeviceCaps& caps) {
     switch (p.type) {
         case kSlabTranspose:
             return unit_for({addr, p.elem, p.strip, p.elem % p.strip == 0 ? p.strip : p.elem % p.strip});
+        case kSlabCluster:  // staged rows sit at a pitch of odd 4-byte words
+            return unit_for({addr, p.elem, 4});
         case kRowGather:
         case kRowScatter: {
             const Staging st = plan_row_staging(p.cols, p.elem, smem_cap, p.type == kRowScatter);

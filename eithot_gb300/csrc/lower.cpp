@@ -54,6 +54,12 @@ uint64_t slab_pitch(uint64_t C, uint64_t w) {
 
 size_t slab_smem_bytes(uint64_t R, uint64_t C, uint64_t w) { return R * slab_pitch(C, w); }
 
+uint64_t slab_cluster_pitch(uint64_t row_bytes) {
+    uint64_t pitch = (row_bytes + 3) / 4 * 4;
+    if ((pitch / 4) % 2 == 0) pitch += 4;  // odd words: a column read walks distinct banks
+    return pitch;
+}
+
 namespace {
 constexpr int kClusterSizes[] = {1, 2, 4, 8, 16};
 
@@ -368,6 +374,28 @@ void lower_xpose(const Xpose& x, const DeviceCaps& caps, std::vector<Pass>* pass
     if (x.B == 0 || x.R <= 1 || x.C <= 1) return;  // identity
     const size_t cap = smem_cap_of(caps);
     const uint64_t w0 = strip_width(x.E, x.R * x.C, kWideStripBytes);
+    // A matrix beyond two-per-SM shared memory: one owner-computed pass over
+    // a cluster of K CTAs (each stages a band of rows and writes that band's
+    // segment of every output row) instead of a one-CTA-per-SM slab or the
+    // two or three Catanzaro passes.
+    if (tuning().slab_cluster && slab_smem_bytes(x.R, x.C, w0) > kTwoPerSm && x.C * x.E <= kTwoPerSm) {
+        const uint64_t pitch = slab_cluster_pitch(x.C * x.E);
+        for (int K : kClusterSizes) {
+            if (K > tuning().max_cluster) break;
+            if (K == 1) continue;
+            const uint64_t Q = (x.R + K - 1) / K;
+            if (Q * pitch > kTwoPerSm) continue;
+            Pass p;
+            p.type = kSlabCluster;
+            p.offset = x.offset;
+            p.batches = x.B; p.rows = x.R; p.cols = x.C; p.elem = x.E;
+            p.strip = x.E;
+            p.cluster = K;
+            p.what = geom("slab-cluster", x.B, x.R, x.C, x.E);
+            passes->push_back(p);
+            return;
+        }
+    }
     for (uint64_t w : {w0, uint64_t(128), uint64_t(64), uint64_t(32)}) {
         if (w > w0 || w < std::min<uint64_t>(x.E, 32)) continue;
         if (slab_smem_bytes(x.R, x.C, w) <= cap) {

@@ -23,6 +23,7 @@ enum PassType {
     kRowScatter = 2,     // out[i][f(i,j)] = in[i][j]
     kColGather = 3,      // out[i][j] = in[g(i,j)][j]
     kBlockMove = 4,      // n_blocks blocks of `block` bytes: s*src_pitch -> s*dst_pitch
+    kSlabCluster = 5,    // each of B matrices (R x C) transposed by a K-CTA cluster, owner-computed
 };
 
 enum FnType {
@@ -42,6 +43,7 @@ struct Pass {
     // Catanzaro parameters of the view (m rows x n cols)
     uint64_t m = 0, n = 0, c = 1, k = 0, a = 0, b = 0, q = 0;
     uint64_t strip = 0;                  // slab passes: strip width in bytes
+    int cluster = 1;                     // kSlabCluster: CTAs per matrix
     // block moves
     uint64_t block = 0, n_blocks = 0, src_pitch = 0, dst_pitch = 0;
     std::string what;
@@ -76,6 +78,7 @@ struct Tuning {
     int row_prefetch = 1;  // rows filling a CTA: prefetch the next row into registers
     int row_block = 1;     // short rows: stage blocks of consecutive rows per CTA item
     int slab_pack = 1;     // small matrices: transpose blocks of consecutive matrices per CTA item
+    int slab_cluster = 1;  // matrices beyond one CTA's share: one owner-computed pass over a cluster
     int sync_sleep_ns = 64;  // group barriers: back-off between polls
     int sync_relaxed = 0;    // group barriers: arrive without release semantics
     int group_per_sm = 0;    // group form: 0 cost model, 1 or 2 CTAs per SM
@@ -155,6 +158,8 @@ void gcd_inverse(uint64_t a, uint64_t b, uint64_t* g, uint64_t* inv);
 // pitch so that the transposed reads hit distinct banks.
 uint64_t slab_pitch(uint64_t C, uint64_t w);
 size_t slab_smem_bytes(uint64_t R, uint64_t C, uint64_t w);
+// Row pitch (bytes) of a cluster slab's staged rows of row_bytes each.
+uint64_t slab_cluster_pitch(uint64_t row_bytes);
 
 // Strip width (bytes) for elements of E bytes when `count` elements are
 // staged together: whole elements up to 128 B; wider elements in strips of

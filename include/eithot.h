@@ -242,8 +242,10 @@ int eithot_estimate_report(int rank, const int64_t* dims, const int* perm_1based
  *                 registers during the write-back, 0 no prefetch
  *   "row_block"   1 rows of 6 KB or less are staged in blocks of consecutive
  *                 rows per CTA, 0 one row per CTA item
- *   "slab_pack"   1 matrices of 6 KB or less are transposed in blocks of
+ *   "slab_pack"   1 matrices of 16 KB or less are transposed in blocks of
  *                 consecutive matrices per CTA, 0 one matrix per CTA item
+ *   "slab_cluster" 1 matrices of up to 16 x 110 KB are transposed in one
+ *                 owner-computed pass over a thread-block cluster, 0 not
  *   "sync_sleep_ns" back-off between polls of a group barrier (0..100000)
  *   "sync_relaxed" 1 group-barrier arrivals without release semantics
  *   "group_per_sm" group form: 0 cost model, 1..4 resident CTAs per SM */

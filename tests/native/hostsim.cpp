@@ -36,6 +36,7 @@ void apply(uint8_t* data, const Pass& p) {
     uint8_t* base = data + p.offset;
     const uint64_t E = p.elem;
     switch (p.type) {
+        case kSlabCluster:
         case kSlabTranspose: {
             const uint64_t R = p.rows, C = p.cols;
             std::vector<uint8_t> tmp(R * C * E);

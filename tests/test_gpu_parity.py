@@ -87,7 +87,7 @@ def test_catanzaro_2d(E, R, C, elem):
 @pytest.fixture
 def tuned(E):
     keys = ("variant", "col_owner", "col_chunk", "max_cluster", "dbuf", "col_form", "row_prefetch", "row_block",
-            "slab_pack")
+            "slab_pack", "slab_cluster")
     saved = {k: E.tune_get(k) for k in keys}
 
     def set_(**kw):
@@ -152,7 +152,8 @@ def test_tall_skinny_rows_in_blocks(E, tuned, dims, perm, elem, variant, block):
 
 
 @pytest.mark.parametrize("dims,perm", [([3, 5, 100000], [2, 1, 3]), ([2, 2, 300001], [2, 1, 3]),
-                                       ([7, 3, 4, 5000], [3, 1, 2, 4]), ([5, 9, 1000], [3, 2, 1])])
+                                       ([7, 3, 4, 5000], [3, 1, 2, 4]), ([5, 9, 1000], [3, 2, 1]),
+                                       ([16, 8, 5000], [2, 1, 3]), ([1024, 4, 300], [2, 1, 3])])
 @pytest.mark.parametrize("elem", [1, 2, 4, 8])
 @pytest.mark.parametrize("pack", [0, 1])
 def test_many_small_matrices(E, tuned, dims, perm, elem, pack):
@@ -169,6 +170,20 @@ def test_few_very_wide_elements(E, dims, perm, elem):
     """Elements of many KB (a permutation that keeps a large leading block
     together): rows and slabs staged in strips of up to 32 KB, with a
     shorter last strip."""
+    run_case(E, dims, perm, elem)
+
+
+@pytest.mark.parametrize("dims,perm,elem", [([16, 4096, 50], [2, 1, 3], 2), ([300, 700], [2, 1], 4),
+                                            ([3001, 200], [2, 1], 1), ([3001, 201], [2, 1], 1),
+                                            ([1000, 150], [2, 1], 8), ([999, 130], [2, 1], 6),
+                                            ([5, 600, 300], [1, 3, 2], 2), ([64, 2001, 3], [2, 1, 3], 2)])
+@pytest.mark.parametrize("on", [0, 1])
+def test_cluster_slabs(E, tuned, dims, perm, elem, on):
+    """Matrices of 110 KB - 1.7 MB transposed in one owner-computed pass
+    over a thread-block cluster (packed 4-byte stores for 1- and 2-byte
+    elements, odd row counts, elements of several units), against the
+    multi-pass decomposition."""
+    tuned(slab_cluster=on)
     run_case(E, dims, perm, elem)
 
 
