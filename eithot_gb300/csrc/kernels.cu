@@ -170,8 +170,9 @@ __global__ void __launch_bounds__(kThreads) k_slab(SlabArgs a) {
 struct SlabClusterArgs {
     uint8_t* base;
     uint64_t items, mat_bytes, row_bytes;
-    uint32_t R, C, E, Q, pitch, upr, upw;
-    FastDiv32 div_upr, div_upw, div_Qupw, div_Qpack;
+    uint32_t R, C, E, Q, pitch, upr, upw, wpr;
+    bool load4;  // rows are whole 4-byte words at a 4-byte aligned base: load words
+    FastDiv32 div_upr, div_upw, div_Qupw, div_Qpack, div_wpr;
 };
 
 template <int US, int kPack>
@@ -187,13 +188,23 @@ __global__ void __launch_bounds__(kThreads) k_slab_cluster(SlabClusterArgs a) {
     for (uint64_t it = cid; it < a.items; it += ncl) {
         uint8_t* mat = a.base + it * a.mat_bytes;
         const uint8_t* band = mat + static_cast<uint64_t>(r0) * a.row_bytes;
-        const uint32_t in_units = nr * a.upr;
-        for (uint32_t x = threadIdx.x; x < in_units; x += blockDim.x) {
-            uint32_t rr, cu;
-            a.div_upr.divmod(x, rr, cu);
-            copy_in<US, U>(smem + rr * a.pitch + cu * US, band + static_cast<uint64_t>(x) * US);
+        if (a.load4) {  // rows of whole 4-byte words, 4-byte aligned: word copies
+            const uint32_t in_words = nr * a.wpr;
+            for (uint32_t x = threadIdx.x; x < in_words; x += blockDim.x) {
+                uint32_t rr, cw;
+                a.div_wpr.divmod(x, rr, cw);
+                copy_in<4, uint32_t>(smem + rr * a.pitch + cw * 4, band + static_cast<uint64_t>(x) * 4);
+            }
+            copy_in_wait<4>();
+        } else {
+            const uint32_t in_units = nr * a.upr;
+            for (uint32_t x = threadIdx.x; x < in_units; x += blockDim.x) {
+                uint32_t rr, cu;
+                a.div_upr.divmod(x, rr, cu);
+                copy_in<US, U>(smem + rr * a.pitch + cu * US, band + static_cast<uint64_t>(x) * US);
+            }
+            copy_in_wait<US>();
         }
-        copy_in_wait<US>();
         cluster_sync_reuse();  // every CTA holds its band: writes may start
         if constexpr (kPack > 1) {
             const uint32_t groups = a.C * (a.Q / kPack);
@@ -1315,6 +1326,9 @@ int launch_slab_cluster(uint8_t* data, const Pass& p, ExecContext& ctx) {
     a.Q = Q;
     a.div_upr = FastDiv32::make(a.upr);
     a.div_upw = FastDiv32::make(a.upw);
+    a.load4 = US < 4 && a.row_bytes % 4 == 0 && addr % 4 == 0;
+    a.wpr = static_cast<uint32_t>(a.row_bytes / 4);
+    a.div_wpr = FastDiv32::make(a.wpr ? a.wpr : 1);
     a.div_Qupw = FastDiv32::make(static_cast<uint64_t>(Q) * a.upw);
     a.div_Qpack = FastDiv32::make(kPack > 1 ? Q / kPack : 1);
     const size_t smem = (static_cast<size_t>(Q) * a.pitch + 127) / 128 * 128;
