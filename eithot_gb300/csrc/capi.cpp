@@ -101,6 +101,8 @@ int eithot_tune_set(const char* key, double value) {
     } else if (k == "sync_sleep_ns") {
         if (value < 0 || value > 100000) return fail(EITHOT_EINVAL, "sync_sleep_ns must be 0..100000");
         t.sync_sleep_ns = static_cast<int>(value);
+    } else if (k == "l2_prefetch") {
+        t.l2_prefetch = value != 0.0 ? 1 : 0;
     } else if (k == "group_per_sm") {
         const int v = static_cast<int>(value);
         if (v < 0 || v > 4) return fail(EITHOT_EINVAL, "group_per_sm must be 0..4");
@@ -153,6 +155,7 @@ int eithot_tune_get(const char* key, double* value) {
     else if (k == "sync_sleep_ns") *value = t.sync_sleep_ns;
     else if (k == "sync_relaxed") *value = t.sync_relaxed;
     else if (k == "group_per_sm") *value = t.group_per_sm;
+    else if (k == "l2_prefetch") *value = t.l2_prefetch;
     else if (k == "col_chunk") *value = t.col_chunk;
     else if (k == "max_cluster") *value = t.max_cluster;
     else if (k == "variant") *value = t.variant;

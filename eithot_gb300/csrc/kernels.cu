@@ -850,6 +850,7 @@ struct GroupSync {
     unsigned G, nG;
     unsigned sleep_ns;   // back-off between polls
     bool relaxed;        // arrive without release semantics (the arriving CTA's loads have completed)
+    bool l2_prefetch;    // single-buffered: prefetch the next item into L2 while waiting
 };
 
 __device__ unsigned g_sync_timeouts;
@@ -883,6 +884,27 @@ __device__ bool group_wait(const unsigned* ctr, unsigned target, unsigned* abort
     return false;
 }
 
+// Asks L2 for the row pieces of item `it` that this CTA will stage (one
+// prefetch per 128-byte line), so that its loads after the barrier hit L2.
+template <typename Own>
+__device__ __forceinline__ void own_prefetch_l2(const ColOwnArgs& a, const Own& own, uint64_t it, uint32_t x0,
+                                                uint32_t nstage) {
+    using I = typename Own::index_type;
+    const OwnItem ci = own_item(a, it);
+    const uint32_t piece = ci.tcols * a.w;  // bytes of a staged row piece (whole elements: w == E)
+    const uint32_t lines = (piece + 127) / 128 + 1;  // +1: a piece need not start on a line
+    const uint32_t tbase = x0 + a.hbase;
+    for (uint32_t x = threadIdx.x; x < nstage * lines; x += blockDim.x) {
+        const uint32_t ii = x / lines, l = x - ii * lines;
+        const I gr = own.stage_of(static_cast<I>(a.div_m.mod(tbase + ii)));
+        if (!in_range(gr, a.rows)) continue;
+        // an address inside the piece on every line it touches (the last one
+        // is the piece's last byte)
+        const uint8_t* p = ci.mat + static_cast<uint64_t>(gr) * a.row_bytes + min(l * 128, piece - 1);
+        asm volatile("prefetch.global.L2 [%0];\n" ::"l"(p));
+    }
+}
+
 template <int US, typename Own, bool kLanes>
 __global__ void __launch_bounds__(kThreads) k_col_group(ColOwnArgs a, Own own, GroupSync gs) {
     using U = typename UnitOf<US>::T;
@@ -914,6 +936,8 @@ __global__ void __launch_bounds__(kThreads) k_col_group(ColOwnArgs a, Own own, G
         const uint64_t nxt = it + gs.nG;
         if (a.dbuf && nxt < a.items)
             own_stage_in<US, Own, kLanes>(a, own, smem + (boff ^ a.buf_bytes), nxt, x0, nstage, lc, lu, ii0, step);
+        if (!a.dbuf && gs.l2_prefetch && nxt < a.items)  // the next item's rows head for L2 during the wait
+            own_prefetch_l2(a, own, nxt, x0, nstage);
         if (threadIdx.x == 0) s_ok = gs.G <= 1 || group_wait(ctr, (k + 1) * gs.G, abort_flag, gs.sleep_ns);
         __syncthreads();  // every CTA of the group holds its slots: writes may start
         if (!s_ok) break;
@@ -1617,6 +1641,7 @@ int launch_col_group(uint8_t* data, const Pass& p, const Staging& st, const Own&
     gs.nG = 0;
     gs.sleep_ns = static_cast<unsigned>(tuning().sync_sleep_ns);
     gs.relaxed = tuning().sync_relaxed != 0;
+    gs.l2_prefetch = tuning().l2_prefetch != 0;
     const unsigned max_groups = static_cast<unsigned>(kGroupSyncBytes / sizeof(unsigned)) - 1;
     EI_CHECK(cudaMemsetAsync(ctx.scratch, 0, kGroupSyncBytes, ctx.stream));  // counters and abort flag
     if (kThreads % a.RU != 0)

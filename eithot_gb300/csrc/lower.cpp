@@ -289,8 +289,7 @@ Staging plan_col_owner(uint64_t rows, uint64_t cols, uint64_t batches, uint64_t 
         }
         // groups of co-resident CTAs: several single-buffered CTAs per SM
         // overlap one another's barrier waits better than one
-        // double-buffered CTA (measured on GB300: 2 per SM single 2.26 ms,
-        // 2 per SM double 2.32, 1 per SM double 2.64 for 20011 x 256 B tiles)
+        // double-buffered CTA
         if (form != 1) {
             for (int per_sm : {2, 3, 4, 1}) {
                 if (tuning().group_per_sm && per_sm != tuning().group_per_sm) continue;
@@ -315,7 +314,11 @@ Staging plan_col_owner(uint64_t rows, uint64_t cols, uint64_t batches, uint64_t 
                     s.item_bytes = rows * pitch; s.on_chip = true; s.dbuf = db;
                     s.owner = true; s.group = true; s.hlo = lo; s.hhi = hi; s.per_sm = per_sm;
                     const double util = static_cast<double>(ngroups * G) / static_cast<double>(slots);
-                    const double residency = per_sm == 1 ? (db ? 0.17 : 0.4) : per_sm == 2 ? (db ? 0.03 : 0.0) : 0.02;
+                    // measured on GB300 (20011-row pass, 256-byte pieces): 3 single-buffered
+                    // CTAs per SM 2.13 ms, 2 per SM 2.22, 2 double-buffered 2.32, 1 double 2.64
+                    const double residency = per_sm == 1 ? (db ? 0.17 : 0.4)
+                                           : per_sm == 2 ? (db ? 0.05 : 0.02)
+                                           : per_sm == 3 ? (db ? 0.04 : 0.0) : 0.03;
                     s.cost = 1.0 / (eff * util) + 0.5 * static_cast<double>((lo + hi) * G) / static_cast<double>(rows) +
                              (G > 1 ? 0.08 : 0.0) + residency;
                     consider(s);

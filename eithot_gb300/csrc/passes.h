@@ -82,6 +82,7 @@ struct Tuning {
     int sync_sleep_ns = 64;  // group barriers: back-off between polls
     int sync_relaxed = 0;    // group barriers: arrive without release semantics
     int group_per_sm = 0;    // group form: 0 cost model, 1 or 2 CTAs per SM
+    int l2_prefetch = 0;     // group form, single-buffered: prefetch the next item into L2 (slower on GB300)
 };
 Tuning& tuning();
 

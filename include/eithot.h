@@ -248,7 +248,9 @@ int eithot_estimate_report(int rank, const int64_t* dims, const int* perm_1based
  *                 owner-computed pass over a thread-block cluster, 0 not
  *   "sync_sleep_ns" back-off between polls of a group barrier (0..100000)
  *   "sync_relaxed" 1 group-barrier arrivals without release semantics
- *   "group_per_sm" group form: 0 cost model, 1..4 resident CTAs per SM */
+ *   "group_per_sm" group form: 0 cost model, 1..4 resident CTAs per SM
+ *   "l2_prefetch" 1 single-buffered group passes prefetch the next item into
+ *                 L2 while they wait at the barrier, 0 not (default; slower) */
 int eithot_tune_set(const char* key, double value);
 int eithot_tune_get(const char* key, double* value);
 
