@@ -93,6 +93,8 @@ def _load():
     lib.eithot_server_destroy.argtypes = [ctypes.c_void_p]
     lib.eithot_tune_set.argtypes = [ctypes.c_char_p, ctypes.c_double]
     lib.eithot_tune_get.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double)]
+    lib.eithot_tune_shape_set.argtypes = [ctypes.c_int, I64P, IP, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_double]
+    lib.eithot_tune_shape_count.argtypes = [ctypes.POINTER(ctypes.c_int)]
     return lib
 
 
@@ -382,6 +384,22 @@ def tune_set(key: str, value: float) -> None:
     "col_owner", "col_form", "row_prefetch", "row_block", "slab_pack", "slab_cluster", "sync_sleep_ns", "sync_relaxed",
     "group_per_sm", "l2_prefetch")."""
     _check(lib.eithot_tune_set(key.encode(), float(value)))
+
+
+def tune_shape_set(dims, perm, elem_size: int, key: str, value: float) -> None:
+    """Knob for one exact (dims, perm, element size) request (autotuner)."""
+    r, d, p = _arrays(dims, perm)
+    _check(lib.eithot_tune_shape_set(r, d, p, elem_size, key.encode(), float(value)))
+
+
+def tune_shape_clear() -> None:
+    _check(lib.eithot_tune_shape_clear())
+
+
+def tune_shape_count() -> int:
+    v = ctypes.c_int()
+    _check(lib.eithot_tune_shape_count(ctypes.byref(v)))
+    return v.value
 
 
 def tune_get(key: str) -> float:

@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <optional>
 #include <string>
 #include <vector>
 
@@ -82,15 +83,24 @@ int build(int rank, const int64_t* dims, const int* perm, size_t elem, int nb, d
 
 using namespace eithot::api;
 
+namespace {
+std::vector<int64_t> dims_of(int rank, const int64_t* dims) { return std::vector<int64_t>(dims, dims + rank); }
+std::vector<int> perm_of(int rank, const int* perm) { return std::vector<int>(perm, perm + rank); }
+}  // namespace
+
 extern "C" {
 
 const char* eithot_last_error(void) { return g_err.c_str(); }
 
 int eithot_version(void) { return 100; }
 
-int eithot_tune_set(const char* key, double value) {
+}  // extern "C"
+
+namespace {
+
+// Sets knob `key` of `t` (the keys of eithot_tune_set).
+int apply_knob(eithot::Tuning& t, const char* key, double value) {
     if (!key) return fail(EITHOT_EINVAL, "null key");
-    eithot::Tuning& t = eithot::tuning();
     const std::string k(key);
     if (k == "dbuf") {
         t.dbuf = value != 0.0 ? 1 : 0;
@@ -137,6 +147,33 @@ int eithot_tune_set(const char* key, double value) {
     } else {
         return fail(EITHOT_EINVAL, "unknown tuning key " + k);
     }
+    return EITHOT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int eithot_tune_set(const char* key, double value) { return apply_knob(eithot::tuning(), key, value); }
+
+int eithot_tune_shape_set(int rank, const int64_t* dims, const int* perm_1based, size_t elem_size,
+                          const char* key, double value) {
+    if (rank < 1 || !dims || !perm_1based) return fail(EITHOT_EINVAL, "null or empty shape");
+    eithot::Tuning t;
+    if (!eithot::shape_tuning(dims_of(rank, dims), perm_of(rank, perm_1based), elem_size, &t)) t = eithot::tuning();
+    if (int rc = apply_knob(t, key, value)) return rc;
+    eithot::set_shape_tuning(dims_of(rank, dims), perm_of(rank, perm_1based), elem_size, t);
+    return EITHOT_OK;
+}
+
+int eithot_tune_shape_clear(void) {
+    eithot::clear_shape_tuning();
+    return EITHOT_OK;
+}
+
+int eithot_tune_shape_count(int* count) {
+    if (!count) return fail(EITHOT_EINVAL, "null count");
+    *count = eithot::shape_tuning_count();
     return EITHOT_OK;
 }
 
@@ -294,6 +331,11 @@ int eithot_workspace_size(int rank, const int64_t* dims, const int* perm_1based,
     } else {
         cudaGetLastError();
     }
+    eithot::Tuning shape_t;
+    std::optional<eithot::ScopedTuning> shape_scope;
+    if (rank >= 1 && dims && perm_1based &&
+        eithot::shape_tuning(dims_of(rank, dims), perm_of(rank, perm_1based), elem_size, &shape_t))
+        shape_scope.emplace(shape_t);
     eithot::NdPlan plan;
     std::vector<eithot::Pass> passes;
     int rc = build(rank, dims, perm_1based, elem_size, num_sub_tensors, alpha, reorder_type, caps, &plan, &passes);
@@ -320,6 +362,13 @@ int eithot_transpose_ex(void* d_data, size_t capacity_bytes, int rank, const int
         if (attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged)
             return fail(EITHOT_EINVAL, "data must be device or managed memory");
     }
+    // knobs recorded for this exact shape (an autotuner's choice) hold for
+    // the planning and the run of this call
+    eithot::Tuning shape_t;
+    std::optional<eithot::ScopedTuning> shape_scope;
+    if (rank >= 1 && dims && perm_1based &&
+        eithot::shape_tuning(dims_of(rank, dims), perm_of(rank, perm_1based), elem_size, &shape_t))
+        shape_scope.emplace(shape_t);
     eithot::NdPlan plan;
     std::vector<eithot::Pass> passes;
     rc = build(rank, dims, perm_1based, elem_size, num_sub_tensors, alpha, reorder_type, caps, &plan, &passes);

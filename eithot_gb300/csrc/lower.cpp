@@ -2,7 +2,10 @@
 #include "passes.h"
 
 #include <algorithm>
+#include <map>
+#include <mutex>
 #include <sstream>
+#include <tuple>
 
 namespace eithot {
 
@@ -92,6 +95,40 @@ Tuning& tuning() {
 
 ScopedTuning::ScopedTuning(const Tuning& t) : t_(t), prev_(t_scoped) { t_scoped = &t_; }
 ScopedTuning::~ScopedTuning() { t_scoped = prev_; }
+
+namespace {
+using ShapeKey = std::tuple<std::vector<int64_t>, std::vector<int>, uint64_t>;
+std::mutex g_shape_mu;
+std::map<ShapeKey, Tuning>& shape_table() {
+    static std::map<ShapeKey, Tuning> table;
+    return table;
+}
+}  // namespace
+
+bool shape_tuning(const std::vector<int64_t>& dims, const std::vector<int>& perm, uint64_t elem, Tuning* out) {
+    std::lock_guard<std::mutex> lock(g_shape_mu);
+    auto& tab = shape_table();
+    if (tab.empty()) return false;
+    auto it = tab.find(ShapeKey{dims, perm, elem});
+    if (it == tab.end()) return false;
+    *out = it->second;
+    return true;
+}
+
+void set_shape_tuning(const std::vector<int64_t>& dims, const std::vector<int>& perm, uint64_t elem, const Tuning& t) {
+    std::lock_guard<std::mutex> lock(g_shape_mu);
+    shape_table()[ShapeKey{dims, perm, elem}] = t;
+}
+
+void clear_shape_tuning() {
+    std::lock_guard<std::mutex> lock(g_shape_mu);
+    shape_table().clear();
+}
+
+int shape_tuning_count() {
+    std::lock_guard<std::mutex> lock(g_shape_mu);
+    return static_cast<int>(shape_table().size());
+}
 
 namespace {
 // A CTA footprint at most this large lets two CTAs share an SM (GB300:

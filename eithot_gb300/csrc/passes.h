@@ -86,6 +86,13 @@ struct Tuning {
 };
 Tuning& tuning();
 
+// Knobs recorded for one exact request shape (dims, 1-based perm, element
+// size), e.g. by an autotuner; looked up by the single-tensor entry points.
+bool shape_tuning(const std::vector<int64_t>& dims, const std::vector<int>& perm, uint64_t elem, Tuning* out);
+void set_shape_tuning(const std::vector<int64_t>& dims, const std::vector<int>& perm, uint64_t elem, const Tuning& t);
+void clear_shape_tuning();
+int shape_tuning_count();
+
 // Makes tuning() return `t` on the calling thread for the scope's lifetime
 // (the batched form lowers and runs its passes under its own knobs).
 class ScopedTuning {

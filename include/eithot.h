@@ -254,6 +254,17 @@ int eithot_estimate_report(int rank, const int64_t* dims, const int* perm_1based
 int eithot_tune_set(const char* key, double value);
 int eithot_tune_get(const char* key, double* value);
 
+/* Knobs for one exact request (dims, 1-based perm, element size), for an
+ * autotuner: the first call for a shape copies the process-wide knobs, then
+ * sets `key`; eithot_transpose, eithot_transpose_ex and
+ * eithot_workspace_size use the shape's knobs for that shape (the
+ * allocation-free entry point and the batched form do not).  Clear drops
+ * every shape's entry. */
+int eithot_tune_shape_set(int rank, const int64_t* dims, const int* perm_1based, size_t elem_size,
+                          const char* key, double value);
+int eithot_tune_shape_clear(void);
+int eithot_tune_shape_count(int* count);
+
 /* ---- per-pass profiling -------------------------------------------------
  * No reference counterpart (the reference times only whole calls,
  * ITNT/src/test_inplace.cpp:43-69).  When enabled for the calling thread,

@@ -1,0 +1,55 @@
+"""Per-shape knobs (eithot_tune_shape_*) and the autotuner built on them."""
+import json
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+
+
+def test_shape_knobs_apply_to_that_shape_only(E):
+    d, p = [4, 20011, 8192, 2], [1, 3, 2, 4]
+    E.tune_shape_clear()
+    base = E.workspace_size(d, p, 4)
+    other = E.workspace_size([3001, 4096], [2, 1], 4)
+    E.tune_shape_set(d, p, 4, "col_form", 1)    # clusters only: no group barrier counters
+    assert E.tune_shape_count() == 1
+    assert E.workspace_size(d, p, 4) != base
+    assert E.workspace_size([3001, 4096], [2, 1], 4) == other
+    assert E.workspace_size(d, p, 2) == E.workspace_size(d, p, 2)  # other element size: untouched entry
+    with pytest.raises(E.EithotError):
+        E.tune_shape_set(d, p, 4, "no_such_knob", 1)
+    E.tune_shape_clear()
+    assert E.tune_shape_count() == 0 and E.workspace_size(d, p, 4) == base
+
+
+def test_saved_results_load_back(E, tmp_path):
+    from eithot_gb300 import autotune
+    E.tune_shape_clear()
+    res = {autotune.key([300, 700], [2, 1], 4): {"config": {"variant": 2}, "ms": 0.1, "tried": 3},
+           autotune.key([5, 6, 7], [3, 1, 2], 1): {"config": {}, "ms": 0.01, "tried": 1}}
+    path = tmp_path / "tuned.json"
+    autotune.save(str(path), res)
+    assert json.load(open(path)) == res
+    assert autotune.load(str(path)) == 2
+    assert E.tune_shape_count() == 2
+    E.tune_shape_clear()
+
+
+@pytest.mark.gpu
+def test_autotune_keeps_results_exact(E):
+    torch = pytest.importorskip("torch")
+    from eithot_gb300 import autotune
+    E.tune_shape_clear()
+    dims, perm, elem = [3001, 409], [2, 1], 4
+    r = autotune.autotune(dims, perm, elem, candidates=[{}, {"variant": 1}, {"variant": 2}, {"slab_cluster": 0}],
+                          reps=2)
+    assert r["tried"] == 4 and r["ms"] > 0 and E.tune_shape_count() == 1
+    n = math.prod(dims)
+    host = oracle.fill_hash(n, elem, 31)
+    t = torch.from_numpy(host.copy()).cuda()
+    E.transpose_ptr(t.data_ptr(), t.numel(), dims, perm, elem)
+    torch.cuda.synchronize()
+    assert np.array_equal(t.cpu().numpy(), oracle.permute(host, dims, perm, elem))
+    E.tune_shape_clear()
