@@ -55,10 +55,10 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--dims", default=None,
                     help="comma-separated dims overriding the workload (small cases for ncu captures)")
-    ap.add_argument("--workload", default="transpose", choices=["transpose", "batched", "served"],
+    ap.add_argument("--workload", default="transpose", choices=["transpose", "batched", "served", "study"],
                     help="transpose: the default line; batched: 4096 mixed tensors through the batched form "
                          "against one call per tensor; served: Poisson-arriving requests through the server "
-                         "against serial calls")
+                         "against serial calls; study: REORDER_TYPE pre/post/mixed and sub-tensor count sweeps")
     ap.add_argument("--count", type=int, default=0, help="tensors (batched) or requests (served); 0: default")
     return ap.parse_args()
 
@@ -592,6 +592,56 @@ def run_served(args):
     return 0
 
 
+def run_study(args):
+    """The reference's experiments on GB300: REORDER_TYPE (pre, post,
+    mixed) on rank 4-6 permutations, and the sub-tensor count nb at fixed
+    alpha on large tensors (time and scratch).  One JSON line per case."""
+    import numpy as np
+    import torch
+    import eithot_gb300 as E
+    dev = torch.device("cuda", 0)
+    st = torch.cuda.current_stream(dev)
+
+    def time_case(dims, perm, elem, nb, alpha, order):
+        info = E.plan(dims, perm, nb, alpha, order)
+        cap = info.padded_volume * elem
+        buf = torch.empty(cap, dtype=torch.uint8, device=dev)
+        E.transpose_ptr(buf.data_ptr(), cap, dims, perm, elem, nb, alpha, order, st.cuda_stream)
+        torch.cuda.synchronize(dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(3):
+            E.transpose_ptr(buf.data_ptr(), cap, dims, perm, elem, nb, alpha, order, st.cuda_stream)
+        e1.record(st)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / 3
+        return ms, E.workspace_size(dims, perm, elem, nb, alpha, order), info
+
+    rng = np.random.default_rng(7)
+    for r in (4, 5, 6):
+        for _ in range(4):
+            total = 1 << 30
+            w = rng.uniform(0.3, 1.0, size=r)
+            w = w / w.sum() * math.log(total / 4)
+            dims = [max(2, int(round(math.exp(x)))) for x in w]
+            perm = [int(x) + 1 for x in rng.permutation(r)]
+            row = {"study": "reorder_type", "dims": dims, "perm": perm, "elem": 4}
+            for name, order in (("mixed", E.ORDER_MIXED), ("pre", E.ORDER_PRE), ("post", E.ORDER_POST)):
+                ms, ws, info = time_case(dims, perm, 4, 1, 0.01, order)
+                row[name] = {"ms": round(ms, 3), "GBs": round(2 * math.prod(dims) * 4 / ms / 1e6, 1),
+                             "rounds": sum(1 for s in info.steps if s.role == 0)}
+            print(json.dumps(row), flush=True)
+    for dims, perm in (([4, 20011, 8192, 2], [1, 3, 2, 4]), ([7248, 50, 3000], [2, 1, 3]),
+                       ([16, 3001, 64, 256], [4, 3, 1, 2])):
+        for nb in (1, 2, 4, 8, 16):
+            ms, ws, info = time_case(dims, perm, 4, nb, 0.01, E.ORDER_MIXED)
+            print(json.dumps({"study": "sub_tensors", "dims": dims, "perm": perm, "elem": 4, "nb_requested": nb,
+                              "nb_applied": info.num_sub_tensors, "padded": info.padded, "ms": round(ms, 3),
+                              "GBs": round(2 * math.prod(dims) * 4 / ms / 1e6, 1), "workspace_bytes": ws}), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -600,6 +650,8 @@ def main():
         return run_batched(args)
     if args.workload == "served":
         return run_served(args)
+    if args.workload == "study":
+        return run_study(args)
     return run_eithot(args)
 
 

@@ -1654,6 +1654,7 @@ int launch_col_group(uint8_t* data, const Pass& p, const Staging& st, const Own&
 }
 
 // ---- block moves -------------------------------------------------------------
+constexpr uint64_t kBlockPieceMin = 4ull << 20;  // smallest scratch for a block move, bytes
 template <int US>
 int copy_blocks(const uint8_t* src, uint8_t* dst, uint64_t blk, uint64_t sp, uint64_t dp,
                 uint64_t s0, uint64_t count, ExecContext& ctx) {
@@ -1679,6 +1680,23 @@ int block_move(uint8_t* data, const Pass& p, ExecContext& ctx) {
     if (n <= 1 || sp == dp) return 0;
     const uint64_t scratch_blocks = ctx.scratch ? ctx.scratch_bytes / blk : 0;
     int rc;
+    // One block through scratch smaller than the block: in pieces, from the
+    // end moved towards first (front to back when moving down, back to front
+    // when moving up), so a piece's destination covers only pieces already
+    // moved and the piece itself, which is in scratch by then.
+    auto piecewise = [&](uint64_t b) -> int {
+        const uint64_t S = ctx.scratch ? ctx.scratch_bytes / US * US : 0;
+        if (S == 0) { ctx.err = "workspace too small for padding"; return EITHOT_STATUS_NOMEM; }
+        const uint64_t pieces = (blk + S - 1) / S;
+        for (uint64_t k = 0; k < pieces; ++k) {
+            const uint64_t idx = dp < sp ? k : pieces - 1 - k;
+            const uint64_t off = idx * S, len = std::min<uint64_t>(S, blk - off);
+            int r;
+            if ((r = copy_blocks<US>(data + b * sp + off, ctx.scratch, len, 0, 0, 0, 1, ctx))) return r;
+            if ((r = copy_blocks<US>(ctx.scratch, data + b * dp + off, len, 0, 0, 0, 1, ctx))) return r;
+        }
+        return 0;
+    };
     if (dp > sp) {
         uint64_t s = n - 1;  // highest block not yet moved
         while (s >= 1) {
@@ -1689,7 +1707,11 @@ int block_move(uint8_t* data, const Pass& p, ExecContext& ctx) {
                 if ((rc = copy_blocks<US>(data, data, blk, sp, dp, lo, s - lo + 1, ctx))) return rc;
                 s = lo - 1;
             } else {
-                if (scratch_blocks == 0) { ctx.err = "workspace too small for padding"; return EITHOT_STATUS_NOMEM; }
+                if (scratch_blocks == 0) {
+                    if ((rc = piecewise(s))) return rc;
+                    --s;
+                    continue;
+                }
                 const uint64_t lo = s + 1 > scratch_blocks ? std::max<uint64_t>(1, s + 1 - scratch_blocks) : 1;
                 const uint64_t cnt = s - lo + 1;
                 if ((rc = copy_blocks<US>(data + lo * sp, ctx.scratch, blk, sp, blk, 0, cnt, ctx))) return rc;
@@ -1708,7 +1730,11 @@ int block_move(uint8_t* data, const Pass& p, ExecContext& ctx) {
                 if ((rc = copy_blocks<US>(data, data, blk, sp, dp, s, hi - s, ctx))) return rc;
                 s = hi;
             } else {
-                if (scratch_blocks == 0) { ctx.err = "workspace too small for padding"; return EITHOT_STATUS_NOMEM; }
+                if (scratch_blocks == 0) {
+                    if ((rc = piecewise(s))) return rc;
+                    ++s;
+                    continue;
+                }
                 const uint64_t cnt = std::min<uint64_t>(scratch_blocks, n - s);
                 if ((rc = copy_blocks<US>(data + s * sp, ctx.scratch, blk, sp, blk, 0, cnt, ctx))) return rc;
                 if ((rc = copy_blocks<US>(ctx.scratch, data + s * dp, blk, blk, dp, 0, cnt, ctx))) return rc;
@@ -1843,7 +1869,8 @@ size_t pass_workspace_bytes(const Pass& p, const DeviceCaps& caps) {
             // the block itself
             const uint64_t sh = p.dst_pitch > p.src_pitch ? p.dst_pitch - p.src_pitch : p.src_pitch - p.dst_pitch;
             if (p.n_blocks <= 1 || sh == 0) return 0;
-            return sh >= p.block ? 0 : p.block;
+            // blocks larger than this move through scratch in pieces
+            return sh >= p.block ? 0 : std::min<uint64_t>(p.block, kBlockPieceMin);
         }
         default:
             return 0;

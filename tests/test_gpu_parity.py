@@ -210,6 +210,17 @@ def test_subtensors_and_padding(E, dims, perm, nb, alpha, elem):
     run_case(E, dims, perm, elem, nb, alpha, slack=1.1)
 
 
+@pytest.mark.parametrize("elem", [2, 4])
+def test_padding_blocks_larger_than_scratch(E, elem):
+    """Sub-tensors with padding where each padded block is far larger than
+    the alpha-bounded scratch: blocks move through scratch in pieces."""
+    dims, perm = [4, 20011, 819, 2], [1, 3, 2, 4]
+    ws = E.workspace_size(dims, perm, elem, 2, 0.01)
+    assert ws <= 0.01 * math.prod(dims) * elem + (4 << 20)
+    st = run_case(E, dims, perm, elem, 2, 0.01, slack=1.01)
+    assert st["workspace_bytes"] == ws
+
+
 def test_wide_elements(E):
     run_case(E, [700, 3, 600], [1, 3, 2], 2)
     run_case(E, [64, 6, 5, 70], [1, 3, 2, 4], 4)
