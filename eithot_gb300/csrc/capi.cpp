@@ -119,6 +119,8 @@ int apply_knob(eithot::Tuning& t, const char* key, double value) {
         t.group_per_sm = v;
     } else if (k == "sync_relaxed") {
         t.sync_relaxed = value != 0.0 ? 1 : 0;
+    } else if (k == "factor") {
+        t.factor = value != 0.0 ? 1 : 0;
     } else if (k == "slab_cluster") {
         t.slab_cluster = value != 0.0 ? 1 : 0;
     } else if (k == "slab_pack") {
@@ -189,6 +191,7 @@ int eithot_tune_get(const char* key, double* value) {
     else if (k == "row_block") *value = t.row_block;
     else if (k == "slab_pack") *value = t.slab_pack;
     else if (k == "slab_cluster") *value = t.slab_cluster;
+    else if (k == "factor") *value = t.factor;
     else if (k == "sync_sleep_ns") *value = t.sync_sleep_ns;
     else if (k == "sync_relaxed") *value = t.sync_relaxed;
     else if (k == "group_per_sm") *value = t.group_per_sm;

@@ -1345,8 +1345,10 @@ int launch_slab_cluster(uint8_t* data, const Pass& p, ExecContext& ctx) {
     constexpr int kPack = US < 4 ? 4 / US : 1;
     const uint64_t addr = reinterpret_cast<uintptr_t>(a.base);
     uint32_t Q = static_cast<uint32_t>((p.rows + K - 1) / K);
-    const bool pack = kPack > 1 && p.elem == US && p.rows % kPack == 0 && addr % 4 == 0 && a.mat_bytes % 4 == 0;
-    if (pack) Q = (Q + kPack - 1) / kPack * kPack;
+    const uint32_t Qp = (Q + kPack - 1) / kPack * kPack;  // bands start on a packed word
+    const bool pack = kPack > 1 && p.elem == US && p.rows % kPack == 0 && addr % 4 == 0 && a.mat_bytes % 4 == 0 &&
+                      static_cast<uint64_t>(Qp) * a.pitch + 127 <= smem_cap_of(ctx.caps);
+    if (pack) Q = Qp;
     a.Q = Q;
     a.div_upr = FastDiv32::make(a.upr);
     a.div_upw = FastDiv32::make(a.upw);

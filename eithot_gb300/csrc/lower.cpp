@@ -410,7 +410,97 @@ std::string geom(const char* name, uint64_t B, uint64_t r, uint64_t c, uint64_t 
 
 }  // namespace
 
+namespace {
+void lower_xpose_direct(const Xpose& x, const DeviceCaps& caps, std::vector<Pass>* passes);
+
+// Modelled time of a pass list, in units of one streaming pass; *staged is
+// set when a pass goes through global scratch.
+double passes_cost(const std::vector<Pass>& ps, const DeviceCaps& caps, bool* staged) {
+    const size_t cap = smem_cap_of(caps);
+    double c = 0;
+    for (const Pass& p : ps) {
+        switch (p.type) {
+            case kSlabTranspose: c += slab_smem_bytes(p.rows, p.cols, p.strip) > kTwoPerSm ? 1.25 : 1.0; break;
+            case kSlabCluster: c += 1.05; break;
+            case kRowGather:
+            case kRowScatter: {
+                const Staging st = plan_row_staging(p.cols, p.elem, cap, p.type == kRowScatter);
+                if (!st.on_chip) *staged = true;
+                c += st.on_chip ? st.cost : 3.0;
+                break;
+            }
+            case kColGather: {
+                const Staging st = plan_col_pass(p, caps);
+                if (!st.on_chip) *staged = true;
+                c += st.on_chip ? st.cost : 3.0;
+                break;
+            }
+            default: break;
+        }
+    }
+    return c;
+}
+
+// Divisors d of v with 2 <= d <= v / 2, at most `limit` of them spread over
+// the range.
+std::vector<uint64_t> divisors(uint64_t v, size_t limit) {
+    std::vector<uint64_t> lo, hi;
+    for (uint64_t d = 2; d * d <= v; ++d) {
+        if (v % d) continue;
+        lo.push_back(d);
+        if (d * d != v) hi.push_back(v / d);
+    }
+    lo.insert(lo.end(), hi.rbegin(), hi.rend());
+    if (lo.size() <= limit) return lo;
+    std::vector<uint64_t> out;
+    for (size_t i = 0; i < limit; ++i) out.push_back(lo[i * lo.size() / limit]);
+    return out;
+}
+}  // namespace
+
+// A batched transpose whose Catanzaro passes would stage through global
+// scratch (a row or a column too long for on-chip staging) may instead be
+// split along a factorisation of its rows R = Ra*Rb (or columns C = Ca*Cb)
+// into two transposes that each stay on chip:
+//   R: Rb x C matrices (B*Ra of them), then Ra x C with elements of Rb*E bytes;
+//   C: R x Ca with elements of Cb*E bytes, then R x Cb matrices (B*Ca of them).
 void lower_xpose(const Xpose& x, const DeviceCaps& caps, std::vector<Pass>* passes) {
+    if (x.B == 0 || x.R <= 1 || x.C <= 1) return;  // identity
+    std::vector<Pass> direct;
+    lower_xpose_direct(x, caps, &direct);
+    bool staged = false;
+    const double direct_cost = passes_cost(direct, caps, &staged);
+    if (!staged || !tuning().factor) {
+        passes->insert(passes->end(), direct.begin(), direct.end());
+        return;
+    }
+    double best = direct_cost - 0.25;  // factor only for a clear gain
+    std::vector<Pass> chosen;
+    auto consider = [&](const Xpose& a, const Xpose& b) {
+        std::vector<Pass> ps;
+        lower_xpose_direct(a, caps, &ps);
+        lower_xpose_direct(b, caps, &ps);
+        bool st = false;
+        const double c = passes_cost(ps, caps, &st);
+        if (c < best) {
+            best = c;
+            chosen.swap(ps);
+        }
+    };
+    for (uint64_t rb : divisors(x.R, 48)) {
+        const uint64_t ra = x.R / rb;
+        consider(Xpose{x.offset, x.B * ra, rb, x.C, x.E}, Xpose{x.offset, x.B, ra, x.C, rb * x.E});
+    }
+    for (uint64_t cb : divisors(x.C, 48)) {
+        const uint64_t ca = x.C / cb;
+        consider(Xpose{x.offset, x.B, x.R, ca, cb * x.E}, Xpose{x.offset, x.B * ca, x.R, cb, x.E});
+    }
+    if (chosen.empty()) chosen.swap(direct);
+    passes->insert(passes->end(), chosen.begin(), chosen.end());
+}
+
+namespace {
+void lower_xpose_direct(const Xpose& x, const DeviceCaps& caps, std::vector<Pass>* passes) {
     if (x.B == 0 || x.R <= 1 || x.C <= 1) return;  // identity
     const size_t cap = smem_cap_of(caps);
     const uint64_t w0 = strip_width(x.E, x.R * x.C, kWideStripBytes);
@@ -418,13 +508,16 @@ void lower_xpose(const Xpose& x, const DeviceCaps& caps, std::vector<Pass>* pass
     // a cluster of K CTAs (each stages a band of rows and writes that band's
     // segment of every output row) instead of a one-CTA-per-SM slab or the
     // two or three Catanzaro passes.
-    if (tuning().slab_cluster && slab_smem_bytes(x.R, x.C, w0) > kTwoPerSm && x.C * x.E <= kTwoPerSm) {
+    if (tuning().slab_cluster && slab_smem_bytes(x.R, x.C, w0) > kTwoPerSm && x.C * x.E <= cap - 4) {
         const uint64_t pitch = slab_cluster_pitch(x.C * x.E);
+        // two CTAs per SM if a cluster of 16 allows it, else one (still one pass)
+        const uint64_t need = (x.R + std::min(16, tuning().max_cluster) - 1) / std::min(16, tuning().max_cluster) * pitch;
+        const uint64_t budget = need <= kTwoPerSm ? kTwoPerSm : static_cast<uint64_t>(cap) - 4;
         for (int K : kClusterSizes) {
             if (K > tuning().max_cluster) break;
             if (K == 1) continue;
             const uint64_t Q = (x.R + K - 1) / K;
-            if (Q * pitch > kTwoPerSm) continue;
+            if (Q * pitch > budget) continue;
             Pass p;
             p.type = kSlabCluster;
             p.offset = x.offset;
@@ -501,6 +594,8 @@ void lower_xpose(const Xpose& x, const DeviceCaps& caps, std::vector<Pass>* pass
         }
     }
 }
+
+}  // namespace
 
 bool lower_plan(const NdPlan& plan, uint64_t elem, const DeviceCaps& caps,
                 std::vector<Pass>* passes, std::string* err) {

@@ -79,6 +79,7 @@ struct Tuning {
     int row_block = 1;     // short rows: stage blocks of consecutive rows per CTA item
     int slab_pack = 1;     // small matrices: transpose blocks of consecutive matrices per CTA item
     int slab_cluster = 1;  // matrices beyond one CTA's share: one owner-computed pass over a cluster
+    int factor = 1;        // split a transpose along a factor of R or C when a pass would stage globally
     int sync_sleep_ns = 64;  // group barriers: back-off between polls
     int sync_relaxed = 0;    // group barriers: arrive without release semantics
     int group_per_sm = 0;    // group form: 0 cost model, 1 or 2 CTAs per SM

@@ -246,6 +246,9 @@ int eithot_estimate_report(int rank, const int64_t* dims, const int* perm_1based
  *                 consecutive matrices per CTA, 0 one matrix per CTA item
  *   "slab_cluster" 1 matrices of up to 16 x 110 KB are transposed in one
  *                 owner-computed pass over a thread-block cluster, 0 not
+ *   "factor"      1 a transpose whose passes would stage through global
+ *                 scratch is split along a factor of its rows or columns
+ *                 into two on-chip transposes when that is cheaper, 0 not
  *   "sync_sleep_ns" back-off between polls of a group barrier (0..100000)
  *   "sync_relaxed" 1 group-barrier arrivals without release semantics
  *   "group_per_sm" group form: 0 cost model, 1..4 resident CTAs per SM

@@ -294,3 +294,20 @@ long hs_check_owner(int rank, const int64_t* dims, const int* perm, size_t elem,
 }
 
 }  // extern "C"
+
+extern "C" {
+
+// Sets one lowering knob of this process (max_cluster, col_form, factor,
+// slab_cluster); returns 0, or -1 for an unknown key.
+int hs_tune(const char* key, int value) {
+    const std::string k(key);
+    Tuning& t = tuning();
+    if (k == "max_cluster") t.max_cluster = value;
+    else if (k == "col_form") t.col_form = value;
+    else if (k == "factor") t.factor = value;
+    else if (k == "slab_cluster") t.slab_cluster = value;
+    else return -1;
+    return 0;
+}
+
+}  // extern "C"

@@ -87,7 +87,7 @@ def test_catanzaro_2d(E, R, C, elem):
 @pytest.fixture
 def tuned(E):
     keys = ("variant", "col_owner", "col_chunk", "max_cluster", "dbuf", "col_form", "row_prefetch", "row_block",
-            "slab_pack", "slab_cluster")
+            "slab_pack", "slab_cluster", "factor")
     saved = {k: E.tune_get(k) for k in keys}
 
     def set_(**kw):
@@ -184,6 +184,17 @@ def test_cluster_slabs(E, tuned, dims, perm, elem, on):
     elements, odd row counts, elements of several units), against the
     multi-pass decomposition."""
     tuned(slab_cluster=on)
+    run_case(E, dims, perm, elem)
+
+
+@pytest.mark.parametrize("dims,perm,elem", [([8000, 7500], [2, 1], 1), ([2, 7500, 8000], [1, 3, 2], 1),
+                                            ([7000, 3000], [2, 1], 4), ([3, 5000, 6001], [1, 3, 2], 2)])
+@pytest.mark.parametrize("factor", [0, 1])
+def test_factored_transposes_on_gpu(E, tuned, dims, perm, elem, factor):
+    """On-chip staging limited to single CTAs (no clusters, no groups):
+    transposes whose passes would stage through global scratch are split
+    along a factor of R or C (factor=1) or staged (factor=0)."""
+    tuned(max_cluster=1, col_form=1, factor=factor)
     run_case(E, dims, perm, elem)
 
 

@@ -108,3 +108,25 @@ def test_owner_maps_match_column_gathers(hostsim, dims, perm, elem):
                                  300000, ctypes.byref(visited))
     assert bad == 0
     assert visited.value >= 1
+
+
+@pytest.mark.parametrize("dims,perm,elem", [([8000, 7500], [2, 1], 1), ([2, 7500, 8000], [1, 3, 2], 1)])
+def test_factored_transposes(hostsim, dims, perm, elem):
+    """With on-chip staging limited to one CTA (no clusters, no groups), long
+    rows or columns would stage through global scratch; the lowering splits
+    such transposes along a factor of R or C.  The whole pass list, run with
+    the kernels' own maps, must still produce the oracle's permutation."""
+    import ctypes
+    hostsim.hs_tune.argtypes = [ctypes.c_char_p, ctypes.c_int]
+    describe = ctypes.create_string_buffer(1 << 14)
+    try:
+        assert hostsim.hs_tune(b"max_cluster", 1) == 0 and hostsim.hs_tune(b"col_form", 1) == 0
+        r = len(dims)
+        hostsim.hs_describe(describe, len(describe), r, (ctypes.c_int64 * r)(*dims), (ctypes.c_int * r)(*perm),
+                            elem, 1, ctypes.c_double(0.01), 0)
+        passes = describe.value.decode().splitlines()
+        assert len(passes) >= 3  # split into two transposes
+        assert run(hostsim, dims, perm, elem)
+    finally:
+        hostsim.hs_tune(b"max_cluster", 16)
+        hostsim.hs_tune(b"col_form", 0)
