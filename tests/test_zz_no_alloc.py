@@ -35,9 +35,10 @@ def _noalloc(E, t, cap, dims, perm, elem, nb, alpha, stream):
 
 
 @pytest.mark.parametrize("dims,perm,elem,nb,alpha", [
-    ([1100000, 20], [2, 1], 4, 1, 0.01),        # row strips beyond a cluster: grid-staged scratch
-    ([700000, 12], [2, 1], 8, 1, 0.01),
-    ([3301, 70, 5], [3, 1, 2], 4, 4, 0.01),     # padded sub-tensors: block moves through scratch
+    ([4, 20011, 819, 2], [1, 3, 2, 4], 4, 1, 0.01),  # group column passes: barrier counters in scratch
+    ([4, 20011, 819, 2], [1, 3, 2, 4], 4, 2, 0.01),  # and padded blocks moved through scratch in pieces
+    ([3301, 70, 5], [3, 1, 2], 4, 4, 0.01),          # padded sub-tensors: block moves through scratch
+    ([3, 1000003], [2, 1], 4, 1, 0.01),              # prime sides: a column tile staged in global scratch
 ])
 def test_noalloc_matches_allocating_entry_point(E, dims, perm, elem, nb, alpha):
     assert E.workspace_size(dims, perm, elem, nb, alpha) > 0  # the case does use scratch
@@ -68,9 +69,10 @@ def test_noalloc_matches_allocating_entry_point(E, dims, perm, elem, nb, alpha):
 
 
 def test_noalloc_rejects_scratch_beyond_its_limit(E):
-    """A transpose whose staged rows exceed the fixed array is refused with
-    EITHOT_EINVAL before any device work."""
-    dims, perm, elem = [9000000, 3], [2, 1], 4
+    """A transpose whose staged column tile exceeds the fixed array (two
+    prime sides: nothing to split it along) is refused with EITHOT_EINVAL
+    before any device work."""
+    dims, perm, elem = [3, 9000011], [2, 1], 4
     assert E.workspace_size(dims, perm, elem) > NOALLOC_SCRATCH
     dev = torch.device("cuda:0")
     n = math.prod(dims)
