@@ -1550,6 +1550,10 @@ int launch_col(uint8_t* data, const Pass& p, const FnOnChip& fn, const Fn64& fn6
     return 0;
 }
 
+// launch_col_group's answer when the device holds fewer co-resident CTAs
+// than the group form was planned for (the caller plans again without it).
+constexpr int kRetryWithoutGroups = -2;
+
 ColOwnArgs col_owner_args(uint8_t* data, const Pass& p, const Staging& st, int US) {
     ColOwnArgs a;
     a.base = data + p.offset;
@@ -1646,10 +1650,14 @@ int launch_col_group(uint8_t* data, const Pass& p, const Staging& st, const Own&
     gs.l2_prefetch = tuning().l2_prefetch != 0;
     const unsigned max_groups = static_cast<unsigned>(kGroupSyncBytes / sizeof(unsigned)) - 1;
     EI_CHECK(cudaMemsetAsync(ctx.scratch, 0, kGroupSyncBytes, ctx.stream));  // counters and abort flag
-    if (kThreads % a.RU != 0)
-        EI_CHECK(launch_groups(k_col_group<US, Own, false>, smem, a, own, gs, max_groups, ctx));
-    else
-        EI_CHECK(launch_groups(k_col_group<US, Own, true>, smem, a, own, gs, max_groups, ctx));
+    const cudaError_t e = kThreads % a.RU != 0
+                              ? launch_groups(k_col_group<US, Own, false>, smem, a, own, gs, max_groups, ctx)
+                              : launch_groups(k_col_group<US, Own, true>, smem, a, own, gs, max_groups, ctx);
+    if (e == cudaErrorCooperativeLaunchTooLarge) {  // fewer CTAs resident than planned: no group form
+        cudaGetLastError();
+        return kRetryWithoutGroups;
+    }
+    EI_CHECK(e);
     EI_CHECK(cudaGetLastError());
     ctx.launches++;
     return 0;
@@ -1752,8 +1760,13 @@ template <int US, template <typename> class FnT, typename Make32, typename Make6
 int run_col(uint8_t* data, const Pass& p, ExecContext& ctx, Make32 m32, Make64 m64, Own32 o32, Own64 o64) {
     const Staging st = plan_col_pass(p, ctx.caps);
     if (st.owner && st.group) {
-        if (fits32(p)) return launch_col_group<US>(data, p, st, o32(p), ctx);
-        return launch_col_group<US>(data, p, st, o64(p), ctx);
+        const int rc = fits32(p) ? launch_col_group<US>(data, p, st, o32(p), ctx)
+                                 : launch_col_group<US>(data, p, st, o64(p), ctx);
+        if (rc != kRetryWithoutGroups) return rc;
+        Tuning t = tuning();  // plan the pass again without groups
+        t.col_form = 1;
+        ScopedTuning scope(t);
+        return run_col<US, FnT>(data, p, ctx, m32, m64, o32, o64);
     }
     if (st.owner) {
         if (fits32(p)) return launch_col_owner<US>(data, p, st, o32(p), ctx);
