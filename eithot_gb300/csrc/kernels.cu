@@ -1608,8 +1608,11 @@ template <typename Own>
 cudaError_t launch_groups(void (*kernel)(ColOwnArgs, Own, GroupSync), size_t smem, const ColOwnArgs& a,
                           const Own& own, GroupSync gs, unsigned max_groups, ExecContext& ctx) {
     const void* kp = reinterpret_cast<const void*>(kernel);
-    cudaError_t e = prep_smem(kp, smem);
+    // the cooperative launch checks co-residency against the kernel's
+    // shared-memory limit, so the limit is this launch's size exactly
+    cudaError_t e = cudaFuncSetAttribute(kp, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
+    remember(LaunchKey{current_device(), kp, 0, 0, kQuerySmemSet}, static_cast<int>(smem));
     const LaunchKey key{current_device(), kp, smem, 1, kQueryBlocks};
     int per_sm = 0;
     if (!cached(key, &per_sm)) {
@@ -1763,9 +1766,15 @@ int run_col(uint8_t* data, const Pass& p, ExecContext& ctx, Make32 m32, Make64 m
         const int rc = fits32(p) ? launch_col_group<US>(data, p, st, o32(p), ctx)
                                  : launch_col_group<US>(data, p, st, o64(p), ctx);
         if (rc != kRetryWithoutGroups) return rc;
-        Tuning t = tuning();  // plan the pass again without groups
+        Tuning t = tuning();  // plan the pass again without groups, if its scratch fits
         t.col_form = 1;
         ScopedTuning scope(t);
+        const Staging alt = plan_col_pass(p, ctx.caps);
+        if (!alt.on_chip && ctx.scratch_bytes < p.rows * alt.tw * alt.w) {
+            ctx.err = "fewer CTAs co-resident than the group column pass needs, and too little workspace "
+                      "for the staged form";
+            return EITHOT_STATUS_CUDA;
+        }
         return run_col<US, FnT>(data, p, ctx, m32, m64, o32, o64);
     }
     if (st.owner) {
