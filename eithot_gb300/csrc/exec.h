@@ -29,6 +29,7 @@ struct ExecContext {
     uint8_t* scratch = nullptr;
     size_t scratch_bytes = 0;
     int launches = 0;
+    int group_per_sm_seen = 0;  // CTAs per SM the last group launch could have resident
     int passes = 0;
     std::string err;
     // When profiling, one event is recorded on `stream` before the first pass

@@ -1621,6 +1621,7 @@ cudaError_t launch_groups(void (*kernel)(ColOwnArgs, Own, GroupSync), size_t sme
         remember(key, per_sm);
     }
     const uint64_t resident = static_cast<uint64_t>(per_sm) * ctx.caps.sms;
+    ctx.group_per_sm_seen = per_sm;
     if (resident < gs.G) return cudaErrorCooperativeLaunchTooLarge;
     gs.nG = static_cast<unsigned>(std::min<uint64_t>({a.items, resident / gs.G, static_cast<uint64_t>(max_groups)}));
     cudaLaunchConfig_t cfg = {};
@@ -1766,6 +1767,16 @@ int run_col(uint8_t* data, const Pass& p, ExecContext& ctx, Make32 m32, Make64 m
         const int rc = fits32(p) ? launch_col_group<US>(data, p, st, o32(p), ctx)
                                  : launch_col_group<US>(data, p, st, o64(p), ctx);
         if (rc != kRetryWithoutGroups) return rc;
+        const int seen = ctx.group_per_sm_seen;
+        if (seen >= 1 && seen < 4 && tuning().group_per_sm != seen) {
+            // plan the groups again for the residency this kernel really has
+            Tuning t = tuning();
+            t.group_per_sm = seen;
+            t.col_form = 2;
+            ScopedTuning scope(t);
+            const Staging again = plan_col_pass(p, ctx.caps);
+            if (again.on_chip && again.group) return run_col<US, FnT>(data, p, ctx, m32, m64, o32, o64);
+        }
         Tuning t = tuning();  // plan the pass again without groups, if its scratch fits
         t.col_form = 1;
         ScopedTuning scope(t);
