@@ -117,7 +117,7 @@ struct SlabArgs {
     uint32_t nstrips;
 };
 
-template <int US>
+template <int US, int kPack>
 __global__ void __launch_bounds__(kThreads) k_slab(SlabArgs a) {
     using U = typename UnitOf<US>::T;
     extern __shared__ __align__(16) uint8_t smem[];
@@ -146,13 +146,36 @@ __global__ void __launch_bounds__(kThreads) k_slab(SlabArgs a) {
         }
         copy_in_wait<US>();
         __syncthreads();
-        for (uint32_t x = threadIdx.x; x < units; x += blockDim.x) {
-            uint32_t o, u, c, r;
-            a.div_upw.divmod(x, o, u);
-            if (u >= lim) continue;
-            a.div_R.divmod(o, c, r);  // output o = c*R + r holds input (r, c)
-            const U v = *reinterpret_cast<const U*>(smem + r * a.pitch + c * a.w + u * US);
-            *reinterpret_cast<U*>(mat + o * a.E + u * US) = v;
+        if constexpr (kPack > 1) {
+            // whole 1/2-byte elements: kPack consecutive outputs (across
+            // output rows) gathered into one 4-byte store, then the tail
+            const uint32_t groups = units / kPack;
+            for (uint32_t g = threadIdx.x; g < groups; g += blockDim.x) {
+                const uint32_t o0 = g * kPack;
+                uint32_t c, r;
+                a.div_R.divmod(o0, c, r);
+                uint32_t word = 0;
+#pragma unroll
+                for (int k = 0; k < kPack; ++k) {
+                    word |= static_cast<uint32_t>(*reinterpret_cast<const U*>(smem + r * a.pitch + c * US)) << (8 * US * k);
+                    if (++r == a.R) { r = 0; ++c; }
+                }
+                *reinterpret_cast<uint32_t*>(mat + static_cast<uint64_t>(o0) * US) = word;
+            }
+            for (uint32_t o = groups * kPack + threadIdx.x; o < units; o += blockDim.x) {
+                uint32_t c, r;
+                a.div_R.divmod(o, c, r);
+                *reinterpret_cast<U*>(mat + static_cast<uint64_t>(o) * US) = *reinterpret_cast<const U*>(smem + r * a.pitch + c * US);
+            }
+        } else {
+            for (uint32_t x = threadIdx.x; x < units; x += blockDim.x) {
+                uint32_t o, u, c, r;
+                a.div_upw.divmod(x, o, u);
+                if (u >= lim) continue;
+                a.div_R.divmod(o, c, r);  // output o = c*R + r holds input (r, c)
+                const U v = *reinterpret_cast<const U*>(smem + r * a.pitch + c * a.w + u * US);
+                *reinterpret_cast<U*>(mat + o * a.E + u * US) = v;
+            }
         }
         __syncthreads();
     }
@@ -275,8 +298,8 @@ __global__ void __launch_bounds__(kThreads) k_slab_pack(SlabPackArgs a) {
         block_copy_in<US>(smem, blk, units * US, a.vec16 && (units * US) % 16 == 0);
         __syncthreads();
         if constexpr (kPack > 1) {
-            // kPack consecutive outputs of one output row (R is a multiple
-            // of kPack) gathered into one 4-byte store
+            // kPack consecutive output elements (they may cross output rows
+            // and matrices) gathered into one 4-byte store
             const uint32_t groups = units / kPack;
             for (uint32_t g = threadIdx.x; g < groups; g += blockDim.x) {
                 const uint32_t x = g * kPack;
@@ -285,10 +308,22 @@ __global__ void __launch_bounds__(kThreads) k_slab_pack(SlabPackArgs a) {
                 a.div_R.divmod(o, c, r);
                 uint32_t word = 0;
 #pragma unroll
-                for (int k = 0; k < kPack; ++k)
-                    word |= static_cast<uint32_t>(*reinterpret_cast<const U*>(smem + (m * a.mat_units + (r + k) * a.C + c) * US))
+                for (int k = 0; k < kPack; ++k) {
+                    word |= static_cast<uint32_t>(*reinterpret_cast<const U*>(smem + (m * a.mat_units + r * a.C + c) * US))
                             << (8 * US * k);
+                    if (++r == a.R) {
+                        r = 0;
+                        if (++c == a.C) { c = 0; ++m; }
+                    }
+                }
                 *reinterpret_cast<uint32_t*>(blk + static_cast<uint64_t>(x) * US) = word;
+            }
+            for (uint32_t x = groups * kPack + threadIdx.x; x < units; x += blockDim.x) {  // the tail
+                uint32_t m, o, c, r;
+                a.div_mat_units.divmod(x, m, o);
+                a.div_R.divmod(o, c, r);
+                *reinterpret_cast<U*>(blk + static_cast<uint64_t>(x) * US) =
+                    *reinterpret_cast<const U*>(smem + (m * a.mat_units + r * a.C + c) * US);
             }
         } else {
             for (uint32_t x = threadIdx.x; x < units; x += blockDim.x) {
@@ -1279,11 +1314,16 @@ int launch_slab(uint8_t* data, const Pass& p, ExecContext& ctx) {
         const size_t smem = (static_cast<size_t>(b.k) * mat_bytes + 127) / 128 * 128;
         constexpr int kPack = US < 4 ? 4 / US : 1;
         const uint64_t addr = reinterpret_cast<uintptr_t>(b.base);
-        if (kPack > 1 && p.elem == US && p.rows % kPack == 0 && addr % 4 == 0 && mat_bytes % 4 == 0) {
+        if (kPack > 1 && p.elem == US && addr % 4 == 0) {
+            // items start on 4-byte boundaries: k * mat_bytes a multiple of 4
+            const uint32_t q = mat_bytes % 4 == 0 ? 1 : mat_bytes % 2 == 0 ? 2 : 4;
+            b.k = std::max<uint32_t>(q, b.k / q * q);
+            b.items = (p.batches + b.k - 1) / b.k;
+            const size_t smem4 = (static_cast<size_t>(b.k) * mat_bytes + 127) / 128 * 128;
             const void* k = reinterpret_cast<const void*>(&k_slab_pack<US, kPack>);
-            EI_CHECK(prep_smem(k, smem));
-            const int grid = grid_for(k, smem, b.items, ctx);
-            k_slab_pack<US, kPack><<<grid, kThreads, smem, ctx.stream>>>(b);
+            EI_CHECK(prep_smem(k, smem4));
+            const int grid = grid_for(k, smem4, b.items, ctx);
+            k_slab_pack<US, kPack><<<grid, kThreads, smem4, ctx.stream>>>(b);
         } else {
             const void* k = reinterpret_cast<const void*>(&k_slab_pack<US, 1>);
             EI_CHECK(prep_smem(k, smem));
@@ -1314,10 +1354,17 @@ int launch_slab(uint8_t* data, const Pass& p, ExecContext& ctx) {
     a.div_upw = FastDiv32::make(a.upw);
     a.div_rowunits = FastDiv32::make(a.rowunits);
     const size_t smem = slab_smem_bytes(p.rows, p.cols, p.strip);
-    const void* k = reinterpret_cast<const void*>(&k_slab<US>);
+    constexpr int kPack = US < 4 ? 4 / US : 1;
+    const bool pack = kPack > 1 && a.flat && p.elem == US && a.nstrips == 1 &&
+                      reinterpret_cast<uintptr_t>(a.base) % 4 == 0 && a.mat_bytes % 4 == 0;
+    const void* k = pack ? reinterpret_cast<const void*>(&k_slab<US, kPack>)
+                         : reinterpret_cast<const void*>(&k_slab<US, 1>);
     EI_CHECK(prep_smem(k, smem));
     const int grid = grid_for(k, smem, a.items, ctx);
-    k_slab<US><<<grid, kThreads, smem, ctx.stream>>>(a);
+    if (pack)
+        k_slab<US, kPack><<<grid, kThreads, smem, ctx.stream>>>(a);
+    else
+        k_slab<US, 1><<<grid, kThreads, smem, ctx.stream>>>(a);
     EI_CHECK(cudaGetLastError());
     ctx.launches++;
     return 0;
