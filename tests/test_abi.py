@@ -40,3 +40,14 @@ def test_workspace_sizes_host_only(E):
     assert E.workspace_size([3001, 4096], [2, 1], 4) <= 4096
     ws = E.workspace_size([4, 20011, 8192, 2], [1, 3, 2, 4], 4)
     assert 0 <= ws <= 0.0101 * 4 * 20011 * 8192 * 8
+
+
+def test_invalid_requests_are_refused(E):
+    import pytest
+    cases = [([0, 5], [2, 1], 4), ([4, 5], [1, 1], 4), ([4, 5], [2, 3], 4), ([4, 5], [2, 1], 0),
+             ([4, 5], [2, 1], 65), ([4, 5, 6], [2, 1], 4)]
+    for dims, perm, elem in cases:
+        with pytest.raises(E.EithotError) as ei:
+            E.workspace_size(dims, perm, elem)
+        assert ei.value.code == E.EINVAL, (dims, perm, elem)
+        assert E.lib.eithot_last_error()

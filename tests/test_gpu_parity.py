@@ -198,6 +198,16 @@ def test_factored_transposes_on_gpu(E, tuned, dims, perm, elem, factor):
     run_case(E, dims, perm, elem)
 
 
+@pytest.mark.parametrize("dims,perm,elem", [
+    ([5], [1], 4), ([1, 1, 1], [3, 2, 1], 2), ([7, 1, 5], [3, 2, 1], 1), ([1, 300000], [2, 1], 4),
+    ([300000, 1], [2, 1], 8), ([33, 17, 9], [1, 2, 3], 4), ([3, 2, 2, 3, 2, 2, 3, 2], [8, 6, 4, 2, 7, 5, 3, 1], 2),
+    ([9, 7, 5], [2, 3, 1], 33), ([4, 3, 5], [3, 1, 2], 64), ([2, 2], [2, 1], 1)])
+def test_edge_shapes(E, dims, perm, elem):
+    """Rank 1, size-1 axes, identity permutations, rank 8, element sizes of
+    33 and 64 bytes, the smallest matrix."""
+    run_case(E, dims, perm, elem)
+
+
 def test_bounded_wait_gives_up(E):
     """A group-barrier wait that nothing releases gives up after its bound,
     is counted, and leaves the context usable."""
