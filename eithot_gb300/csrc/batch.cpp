@@ -6,7 +6,9 @@
 // another.  Column passes use thread-block clusters only (no
 // group-synchronised passes, which rely on all their CTAs being resident
 // while other lanes' kernels occupy SMs).  Every lane has its own scratch
-// slice of the batch workspace.
+// slice of the batch workspace.  A tensor whose shape has recorded knobs
+// (eithot_tune_shape_set, e.g. from the autotuner) is planned and run with
+// them.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -29,6 +31,7 @@ struct eithot_batch {
     DeviceCaps caps;
     Tuning tuning;
     struct Item {
+        Tuning tuning;         // the batch's knobs, or the shape's (eithot_tune_shape_set)
         std::vector<Pass> passes;
         size_t need = 0;       // bytes the (padded) tensor occupies
         size_t scratch = 0;    // workspace its passes use
@@ -86,12 +89,18 @@ int eithot_batch_create(int count, const int* ranks, const int64_t* dims, const 
     }
     b->tuning = tuning();
     b->tuning.col_form = 1;  // clusters only: no pass relies on grid-wide residency
-    ScopedTuning scope(b->tuning);
     b->items.resize(count);
     size_t off = 0;
     for (int t = 0; t < count; ++t) {
         NdPlan plan;
         auto& it = b->items[t];
+        it.tuning = b->tuning;
+        if (ranks[t] >= 1 &&
+            shape_tuning(std::vector<int64_t>(dims + off, dims + off + ranks[t]),
+                         std::vector<int>(perms_1based + off, perms_1based + off + ranks[t]), elem_sizes[t],
+                         &it.tuning))
+            it.tuning.col_form = 1;  // a shape's knobs, still without group passes
+        ScopedTuning scope(it.tuning);
         const int rc = build(ranks[t], dims + off, perms_1based + off, elem_sizes[t], num_sub_tensors, alpha,
                              EITHOT_ORDER_MIXED, b->caps, &plan, &it.passes);
         if (rc) {
@@ -163,7 +172,6 @@ int eithot_batch_run(eithot_batch* b, void* const* d_data, const size_t* capacit
             owned = true;
         }
     }
-    ScopedTuning scope(b->tuning);
     cudaError_t e = cudaEventRecord(b->fork, st);
     int rc = EITHOT_OK;
     std::string err;
@@ -172,6 +180,7 @@ int eithot_batch_run(eithot_batch* b, void* const* d_data, const size_t* capacit
         e = cudaStreamWaitEvent(b->streams[l], b->fork, 0);
         for (int t : b->lane_items[l]) {
             if (e != cudaSuccess || rc != EITHOT_OK) break;
+            ScopedTuning scope(b->items[t].tuning);
             ExecContext ctx;
             ctx.caps = b->caps;
             ctx.stream = b->streams[l];

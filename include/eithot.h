@@ -259,9 +259,10 @@ int eithot_tune_get(const char* key, double* value);
 
 /* Knobs for one exact request (dims, 1-based perm, element size), for an
  * autotuner: the first call for a shape copies the process-wide knobs, then
- * sets `key`; eithot_transpose, eithot_transpose_ex and
- * eithot_workspace_size use the shape's knobs for that shape (the
- * allocation-free entry point and the batched form do not).  Clear drops
+ * sets `key`; eithot_transpose, eithot_transpose_ex, eithot_workspace_size
+ * and eithot_batch_create use the shape's knobs for that shape (the batched
+ * form without group-synchronised column passes; the allocation-free entry
+ * point not at all).  Clear drops
  * every shape's entry. */
 int eithot_tune_shape_set(int rank, const int64_t* dims, const int* perm_1based, size_t elem_size,
                           const char* key, double value);

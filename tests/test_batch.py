@@ -84,3 +84,19 @@ def test_batch_with_large_and_staged_tensors_caller_workspace(E):
 def test_batch_of_one_and_identity(E):
     run_batch(E, [([37, 64, 5, 3], [3, 1, 4, 2], 4)], seed=3)
     run_batch(E, [([37, 64], [1, 2], 2), ([5, 6, 7], [3, 2, 1], 8)], seed=4)
+
+
+@gpu
+def test_batch_uses_shape_knobs(E):
+    """Tensors whose shapes carry recorded knobs are planned and run with them;
+    the results stay bit-exact."""
+    tensors = random_tensors(30, 8) + [([3001, 4096], [2, 1], 4), ([2, 300000], [2, 1], 1), ([60, 40, 3401], [3, 1, 2], 2)]
+    try:
+        E.tune_shape_set([3001, 4096], [2, 1], 4, "variant", 1)
+        E.tune_shape_set([3001, 4096], [2, 1], 4, "dbuf", 0)
+        E.tune_shape_set([2, 300000], [2, 1], 1, "factor", 0)
+        E.tune_shape_set([60, 40, 3401], [3, 1, 2], 2, "col_form", 2)  # groups are still left out
+        E.tune_shape_set([60, 40, 3401], [3, 1, 2], 2, "max_cluster", 2)
+        run_batch(E, tensors, seed=31)
+    finally:
+        E.tune_shape_clear()
