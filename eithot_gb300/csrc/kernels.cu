@@ -868,6 +868,61 @@ __global__ void __launch_bounds__(kThreads) k_col_owner(ColOwnArgs a, Own own) {
     }
 }
 
+// Row tables of the group form.  A CTA's staged slots hold the same source
+// rows for every item (stage_of depends on the slot alone), so they are
+// computed once per CTA; the output rows of its owned slots depend on the
+// item's first column and are computed once per item, by one thread per row
+// instead of by every lane of the row.
+template <typename Own>
+__device__ __forceinline__ void own_fill_stage_rows(const ColOwnArgs& a, const Own& own,
+                                                    typename Own::index_type* srow, uint32_t x0, uint32_t nstage) {
+    using I = typename Own::index_type;
+    const uint32_t tbase = x0 + a.hbase;
+    for (uint32_t ii = threadIdx.x; ii < nstage; ii += blockDim.x)
+        srow[ii] = own.stage_of(static_cast<I>(a.div_m.mod(tbase + ii)));
+}
+
+template <typename Own>
+__device__ __forceinline__ void own_fill_write_rows(const Own& own, typename Own::index_type* wrow, uint32_t x0,
+                                                    uint32_t myrows, uint32_t col0) {
+    using I = typename Own::index_type;
+    for (uint32_t ii = threadIdx.x; ii < myrows; ii += blockDim.x)
+        wrow[ii] = own.row_of(static_cast<I>(x0 + ii), static_cast<I>(col0));
+}
+
+// own_stage_in with the source rows read from the CTA's table.
+template <int US, typename I, bool kLanes>
+__device__ __forceinline__ void own_stage_in_tab(const ColOwnArgs& a, const I* srow, uint8_t* buf, uint64_t it,
+                                                 uint32_t nstage, uint32_t lc, uint32_t lu, uint32_t ii0,
+                                                 uint32_t step) {
+    using U = typename UnitOf<US>::T;
+    const OwnItem ci = own_item(a, it);
+    if constexpr (kLanes) {
+        if (lc < ci.tcols && lu < ci.lim) {
+            const uint8_t* src = ci.mat + static_cast<uint64_t>(lc) * a.E + lu * US;
+            uint8_t* dst = buf + lc * a.w + lu * US;
+            for (uint32_t ii = ii0; ii < nstage; ii += step) {
+                const I gr = srow[ii];
+                if (!in_range(gr, a.rows)) continue;
+                copy_in<US, U>(dst + ii * a.pitch, src + static_cast<uint64_t>(gr) * a.row_bytes);
+            }
+        }
+    } else {
+        const uint32_t units = nstage * a.RU;
+        for (uint32_t x = threadIdx.x; x < units; x += blockDim.x) {
+            uint32_t ii, r, c, u;
+            a.div_RU.divmod(x, ii, r);
+            a.div_upw.divmod(r, c, u);
+            if (c >= ci.tcols || u >= ci.lim) continue;
+            const I gr = srow[ii];
+            if (!in_range(gr, a.rows)) continue;
+            copy_in<US, U>(buf + ii * a.pitch + c * a.w + u * US,
+                           ci.mat + static_cast<uint64_t>(gr) * a.row_bytes + static_cast<uint64_t>(c) * a.E + u * US);
+        }
+    }
+    if constexpr (US >= 4) asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
 // ---------------------------------------------------------------------------
 // Owner-computed column pass over groups of G co-resident CTAs (a
 // cooperative launch guarantees co-residency), for tiles larger than a
@@ -953,6 +1008,9 @@ __global__ void __launch_bounds__(kThreads) k_col_group(ColOwnArgs a, Own own, G
     const uint32_t x0 = r * a.Q;
     const uint32_t myrows = x0 < a.rows ? min(a.Q, a.rows - x0) : 0;
     const uint32_t nstage = myrows ? myrows + a.Hlo + a.Hhi : 0;
+    // row tables behind the slot buffer(s): Q + Hlo + Hhi source rows, Q output rows
+    I* srow = reinterpret_cast<I*>(smem + (a.dbuf ? 2 : 1) * a.buf_bytes);
+    I* wrow = srow + (a.Q + a.Hlo + a.Hhi);
     uint32_t lc = 0, lu = 0, ii0 = 0, step = 1;
     if constexpr (kLanes) {
         uint32_t lr;
@@ -960,35 +1018,38 @@ __global__ void __launch_bounds__(kThreads) k_col_group(ColOwnArgs a, Own own, G
         a.div_upw.divmod(lr, lc, lu);
         step = blockDim.x / a.RU;
     }
-    if (a.dbuf && grp < a.items) own_stage_in<US, Own, kLanes>(a, own, smem, grp, x0, nstage, lc, lu, ii0, step);
+    own_fill_stage_rows(a, own, srow, x0, nstage);
+    __syncthreads();
+    if (a.dbuf && grp < a.items) own_stage_in_tab<US, I, kLanes>(a, srow, smem, grp, nstage, lc, lu, ii0, step);
     uint32_t k = 0;
     for (uint64_t it = grp; it < a.items; it += gs.nG, ++k) {
         const uint32_t boff = a.dbuf ? (k & 1) * a.buf_bytes : 0;
-        if (!a.dbuf) own_stage_in<US, Own, kLanes>(a, own, smem, it, x0, nstage, lc, lu, ii0, step);
+        if (!a.dbuf) own_stage_in_tab<US, I, kLanes>(a, srow, smem, it, nstage, lc, lu, ii0, step);
         if constexpr (US >= 4) asm volatile("cp.async.wait_group 0;\n" ::: "memory");
         __syncthreads();  // this CTA's slots of the item are in shared memory
         if (threadIdx.x == 0 && gs.G > 1) group_arrive(ctr, gs.relaxed);
         const uint64_t nxt = it + gs.nG;
         if (a.dbuf && nxt < a.items)
-            own_stage_in<US, Own, kLanes>(a, own, smem + (boff ^ a.buf_bytes), nxt, x0, nstage, lc, lu, ii0, step);
+            own_stage_in_tab<US, I, kLanes>(a, srow, smem + (boff ^ a.buf_bytes), nxt, nstage, lc, lu, ii0, step);
         if (!a.dbuf && gs.l2_prefetch && nxt < a.items)  // the next item's rows head for L2 during the wait
             own_prefetch_l2(a, own, nxt, x0, nstage);
+        const OwnItem ci = own_item(a, it);
+        own_fill_write_rows(own, wrow, x0, myrows, ci.col0);  // while thread 0 waits
         if (threadIdx.x == 0) s_ok = gs.G <= 1 || group_wait(ctr, (k + 1) * gs.G, abort_flag, gs.sleep_ns);
         __syncthreads();  // every CTA of the group holds its slots: writes may start
         if (!s_ok) break;
-        const OwnItem ci = own_item(a, it);
         const uint8_t* buf = smem + boff;
         if constexpr (kLanes) {
             if (lc < ci.tcols && lu < ci.lim) {
                 const int64_t d = own.delta(static_cast<I>(ci.col0 + lc)) - own.delta(static_cast<I>(ci.col0));
-                const uint32_t soff = lc * a.w + lu * US;
-                const uint64_t lane_off = static_cast<uint64_t>(lc) * a.E + lu * US;
+                const uint8_t* src = buf + lc * a.w + lu * US;
+                uint8_t* dst = ci.mat + static_cast<uint64_t>(lc) * a.E + lu * US;
                 for (uint32_t ii = ii0; ii < myrows; ii += step) {
-                    const I i = own.row_of(static_cast<I>(x0 + ii), static_cast<I>(ci.col0));
+                    const I i = wrow[ii];
                     const int64_t local = own_local(a, ii, d);
                     if (!in_range(i, a.rows) || !in_range(static_cast<uint64_t>(local), nstage)) continue;
-                    *reinterpret_cast<U*>(ci.mat + static_cast<uint64_t>(i) * a.row_bytes + lane_off) =
-                        *reinterpret_cast<const U*>(buf + static_cast<uint32_t>(local) * a.pitch + soff);
+                    *reinterpret_cast<U*>(dst + static_cast<uint64_t>(i) * a.row_bytes) =
+                        *reinterpret_cast<const U*>(src + static_cast<uint32_t>(local) * a.pitch);
                 }
             }
         } else {
@@ -999,14 +1060,14 @@ __global__ void __launch_bounds__(kThreads) k_col_group(ColOwnArgs a, Own own, G
                 a.div_upw.divmod(rr, c, u);
                 if (c >= ci.tcols || u >= ci.lim) continue;
                 const int64_t d = own.delta(static_cast<I>(ci.col0 + c)) - own.delta(static_cast<I>(ci.col0));
-                const I i = own.row_of(static_cast<I>(x0 + ii), static_cast<I>(ci.col0));
+                const I i = wrow[ii];
                 const int64_t local = own_local(a, ii, d);
                 if (!in_range(i, a.rows) || !in_range(static_cast<uint64_t>(local), nstage)) continue;
                 *reinterpret_cast<U*>(ci.mat + static_cast<uint64_t>(i) * a.row_bytes + static_cast<uint64_t>(c) * a.E + u * US) =
                     *reinterpret_cast<const U*>(buf + static_cast<uint32_t>(local) * a.pitch + c * a.w + u * US);
             }
         }
-        __syncthreads();  // this CTA's threads are done with the buffer before it is restaged
+        __syncthreads();  // this CTA's threads are done with the buffer and the output rows
     }
     if constexpr (US >= 4) asm volatile("cp.async.wait_group 0;\n" ::: "memory");  // no copy outlives the CTA
 }
@@ -1687,7 +1748,8 @@ cudaError_t launch_groups(void (*kernel)(ColOwnArgs, Own, GroupSync), size_t sme
 template <int US, typename Own>
 int launch_col_group(uint8_t* data, const Pass& p, const Staging& st, const Own& own, ExecContext& ctx) {
     const ColOwnArgs a = col_owner_args(data, p, st, US);
-    const size_t smem = (st.dbuf ? 2 : 1) * static_cast<size_t>(a.buf_bytes);
+    const size_t tables = (2 * static_cast<size_t>(a.Q) + a.Hlo + a.Hhi) * sizeof(typename Own::index_type);
+    const size_t smem = (st.dbuf ? 2 : 1) * static_cast<size_t>(a.buf_bytes) + (tables + 15) / 16 * 16;
     if (ctx.scratch == nullptr || ctx.scratch_bytes < kGroupSyncBytes) {
         ctx.err = "workspace too small for a group-synchronised column pass";
         return EITHOT_STATUS_NOMEM;

@@ -335,9 +335,15 @@ Staging plan_col_owner(uint64_t rows, uint64_t cols, uint64_t batches, uint64_t 
                 const uint64_t per_cta_cap = std::min<uint64_t>(cap, sm_share - 3072);
                 for (bool db : {false, true}) {
                     if (db && !tuning().dbuf) continue;
-                    const uint64_t budget = per_cta_cap / (db ? 2 : 1);
-                    if (budget / pitch <= lo + hi) continue;
-                    const uint64_t qmax = budget / pitch - lo - hi;
+                    // the slot buffer(s) (128-byte rounded) and the CTA's row
+                    // tables: Q + lo + hi source rows and Q output rows of the
+                    // pass's index type (32-bit when m*n + m + n < 2^31)
+                    const uint64_t nbuf = db ? 2 : 1;
+                    const uint64_t idx = rows * cols + rows + cols < (uint64_t(1) << 31) ? 4 : 8;
+                    const uint64_t fixed = 16 + nbuf * 127 + (lo + hi) * (nbuf * pitch + idx);
+                    if (per_cta_cap <= fixed) continue;
+                    const uint64_t qmax = (per_cta_cap - fixed) / (nbuf * pitch + 2 * idx);
+                    if (qmax == 0) continue;
                     const uint64_t slots = static_cast<uint64_t>(per_sm) * caps.sms;
                     const uint64_t gmin = (rows + qmax - 1) / qmax;
                     if (gmin > slots) continue;
