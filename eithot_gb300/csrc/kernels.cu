@@ -769,106 +769,7 @@ __device__ __forceinline__ OwnItem own_item(const ColOwnArgs& a, uint64_t it) {
     return c;
 }
 
-// Stages slots x0 - Hlo .. x0 - Hlo + nstage - 1 (modulo m); slot t holds
-// source row own.stage_of(t).
-template <int US, typename Own, bool kLanes>
-__device__ __forceinline__ void own_stage_in(const ColOwnArgs& a, const Own& own, uint8_t* buf, uint64_t it,
-                                             uint32_t x0, uint32_t nstage, uint32_t lc, uint32_t lu,
-                                             uint32_t ii0, uint32_t step) {
-    using U = typename UnitOf<US>::T;
-    using I = typename Own::index_type;
-    const OwnItem ci = own_item(a, it);
-    const uint32_t tbase = x0 + a.hbase;  // reduced modulo m per slot
-    if constexpr (kLanes) {
-        if (lc < ci.tcols && lu < ci.lim) {
-            const uint64_t lane_off = static_cast<uint64_t>(lc) * a.E + lu * US;
-            for (uint32_t ii = ii0; ii < nstage; ii += step) {
-                const I gr = own.stage_of(static_cast<I>(a.div_m.mod(tbase + ii)));
-                if (!in_range(gr, a.rows)) continue;
-                copy_in<US, U>(buf + ii * a.pitch + lc * a.w + lu * US,
-                               ci.mat + static_cast<uint64_t>(gr) * a.row_bytes + lane_off);
-            }
-        }
-    } else {
-        const uint32_t units = nstage * a.RU;
-        for (uint32_t x = threadIdx.x; x < units; x += blockDim.x) {
-            uint32_t ii, r, c, u;
-            a.div_RU.divmod(x, ii, r);
-            a.div_upw.divmod(r, c, u);
-            if (c >= ci.tcols || u >= ci.lim) continue;
-            const I gr = own.stage_of(static_cast<I>(a.div_m.mod(tbase + ii)));
-            if (!in_range(gr, a.rows)) continue;
-            copy_in<US, U>(buf + ii * a.pitch + c * a.w + u * US,
-                           ci.mat + static_cast<uint64_t>(gr) * a.row_bytes + static_cast<uint64_t>(c) * a.E + u * US);
-        }
-    }
-    if constexpr (US >= 4) asm volatile("cp.async.commit_group;\n" ::: "memory");
-}
-
-template <int US, typename Own, bool kLanes>
-__global__ void __launch_bounds__(kThreads) k_col_owner(ColOwnArgs a, Own own) {
-    using U = typename UnitOf<US>::T;
-    using I = typename Own::index_type;
-    extern __shared__ __align__(16) uint8_t smem[];
-    cg::cluster_group cl = cg::this_cluster();
-    const unsigned K = cl.num_blocks();
-    const unsigned kr = cl.block_rank();
-    const uint64_t cid = blockIdx.x / K, ncl = gridDim.x / K;
-    const uint32_t x0 = kr * a.Q;
-    const uint32_t myrows = x0 < a.rows ? min(a.Q, a.rows - x0) : 0;
-    const uint32_t nstage = myrows ? myrows + a.Hlo + a.Hhi : 0;
-    uint32_t lc = 0, lu = 0, ii0 = 0, step = 1;
-    if constexpr (kLanes) {
-        uint32_t lr;
-        a.div_RU.divmod(threadIdx.x, ii0, lr);
-        a.div_upw.divmod(lr, lc, lu);
-        step = blockDim.x / a.RU;
-    }
-    if (a.dbuf && cid < a.items) own_stage_in<US, Own, kLanes>(a, own, smem, cid, x0, nstage, lc, lu, ii0, step);
-    uint32_t k = 0;
-    for (uint64_t it = cid; it < a.items; it += ncl, ++k) {
-        const uint32_t boff = a.dbuf ? (k & 1) * a.buf_bytes : 0;
-        if (!a.dbuf) own_stage_in<US, Own, kLanes>(a, own, smem, it, x0, nstage, lc, lu, ii0, step);
-        if constexpr (US >= 4) asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-        cluster_sync_reuse();  // every CTA holds its rows of this tile: writes may start
-        const uint64_t nxt = it + ncl;
-        if (a.dbuf && nxt < a.items)
-            own_stage_in<US, Own, kLanes>(a, own, smem + (boff ^ a.buf_bytes), nxt, x0, nstage, lc, lu, ii0, step);
-        const OwnItem ci = own_item(a, it);
-        const uint8_t* buf = smem + boff;
-        if constexpr (kLanes) {
-            if (lc < ci.tcols && lu < ci.lim) {
-                const int64_t d = own.delta(static_cast<I>(ci.col0 + lc)) - own.delta(static_cast<I>(ci.col0));
-                const uint32_t soff = lc * a.w + lu * US;
-                const uint64_t lane_off = static_cast<uint64_t>(lc) * a.E + lu * US;
-                for (uint32_t ii = ii0; ii < myrows; ii += step) {
-                    const I i = own.row_of(static_cast<I>(x0 + ii), static_cast<I>(ci.col0));
-                    const int64_t local = own_local(a, ii, d);
-                    if (!in_range(i, a.rows) || !in_range(static_cast<uint64_t>(local), nstage)) continue;
-                    *reinterpret_cast<U*>(ci.mat + static_cast<uint64_t>(i) * a.row_bytes + lane_off) =
-                        *reinterpret_cast<const U*>(buf + static_cast<uint32_t>(local) * a.pitch + soff);
-                }
-            }
-        } else {
-            const uint32_t units = myrows * a.RU;
-            for (uint32_t x = threadIdx.x; x < units; x += blockDim.x) {
-                uint32_t ii, r, c, u;
-                a.div_RU.divmod(x, ii, r);
-                a.div_upw.divmod(r, c, u);
-                if (c >= ci.tcols || u >= ci.lim) continue;
-                const int64_t d = own.delta(static_cast<I>(ci.col0 + c)) - own.delta(static_cast<I>(ci.col0));
-                const I i = own.row_of(static_cast<I>(x0 + ii), static_cast<I>(ci.col0));
-                const int64_t local = own_local(a, ii, d);
-                if (!in_range(i, a.rows) || !in_range(static_cast<uint64_t>(local), nstage)) continue;
-                *reinterpret_cast<U*>(ci.mat + static_cast<uint64_t>(i) * a.row_bytes + static_cast<uint64_t>(c) * a.E + u * US) =
-                    *reinterpret_cast<const U*>(buf + static_cast<uint32_t>(local) * a.pitch + c * a.w + u * US);
-            }
-        }
-        __syncthreads();  // this CTA's threads are done with the buffer before it is restaged
-    }
-}
-
-// Row tables of the group form.  A CTA's staged slots hold the same source
+// Row tables of the owner-computed forms.  A CTA's staged slots hold the same source
 // rows for every item (stage_of depends on the slot alone), so they are
 // computed once per CTA; the output rows of its owned slots depend on the
 // item's first column and are computed once per item, by one thread per row
@@ -923,6 +824,88 @@ __device__ __forceinline__ void own_stage_in_tab(const ColOwnArgs& a, const I* s
     if constexpr (US >= 4) asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
 
+// Writes the CTA's output rows of item ci from its staged slots, the output
+// rows read from the CTA's table: output row ii is wrow[ii], its element at
+// column offset c comes from local ii + Hlo + delta(col0 + c) - delta(col0).
+template <int US, typename Own, bool kLanes>
+__device__ __forceinline__ void own_write_rows_tab(const ColOwnArgs& a, const Own& own, const uint8_t* buf,
+                                                   const OwnItem& ci, const typename Own::index_type* wrow,
+                                                   uint32_t myrows, uint32_t nstage, uint32_t lc, uint32_t lu,
+                                                   uint32_t ii0, uint32_t step) {
+    using U = typename UnitOf<US>::T;
+    using I = typename Own::index_type;
+    if constexpr (kLanes) {
+        if (lc < ci.tcols && lu < ci.lim) {
+            const int64_t d = own.delta(static_cast<I>(ci.col0 + lc)) - own.delta(static_cast<I>(ci.col0));
+            const uint8_t* src = buf + lc * a.w + lu * US;
+            uint8_t* dst = ci.mat + static_cast<uint64_t>(lc) * a.E + lu * US;
+            for (uint32_t ii = ii0; ii < myrows; ii += step) {
+                const I i = wrow[ii];
+                const int64_t local = own_local(a, ii, d);
+                if (!in_range(i, a.rows) || !in_range(static_cast<uint64_t>(local), nstage)) continue;
+                *reinterpret_cast<U*>(dst + static_cast<uint64_t>(i) * a.row_bytes) =
+                    *reinterpret_cast<const U*>(src + static_cast<uint32_t>(local) * a.pitch);
+            }
+        }
+    } else {
+        const uint32_t units = myrows * a.RU;
+        for (uint32_t x = threadIdx.x; x < units; x += blockDim.x) {
+            uint32_t ii, rr, c, u;
+            a.div_RU.divmod(x, ii, rr);
+            a.div_upw.divmod(rr, c, u);
+            if (c >= ci.tcols || u >= ci.lim) continue;
+            const int64_t d = own.delta(static_cast<I>(ci.col0 + c)) - own.delta(static_cast<I>(ci.col0));
+            const I i = wrow[ii];
+            const int64_t local = own_local(a, ii, d);
+            if (!in_range(i, a.rows) || !in_range(static_cast<uint64_t>(local), nstage)) continue;
+            *reinterpret_cast<U*>(ci.mat + static_cast<uint64_t>(i) * a.row_bytes + static_cast<uint64_t>(c) * a.E + u * US) =
+                *reinterpret_cast<const U*>(buf + static_cast<uint32_t>(local) * a.pitch + c * a.w + u * US);
+        }
+    }
+}
+
+template <int US, typename Own, bool kLanes>
+__global__ void __launch_bounds__(kThreads) k_col_owner(ColOwnArgs a, Own own) {
+    using I = typename Own::index_type;
+    extern __shared__ __align__(16) uint8_t smem[];
+    cg::cluster_group cl = cg::this_cluster();
+    const unsigned K = cl.num_blocks();
+    const unsigned kr = cl.block_rank();
+    const uint64_t cid = blockIdx.x / K, ncl = gridDim.x / K;
+    const uint32_t x0 = kr * a.Q;
+    const uint32_t myrows = x0 < a.rows ? min(a.Q, a.rows - x0) : 0;
+    const uint32_t nstage = myrows ? myrows + a.Hlo + a.Hhi : 0;
+    // row tables behind the slot buffer(s): Q + Hlo + Hhi source rows, Q output rows
+    I* srow = reinterpret_cast<I*>(smem + (a.dbuf ? 2 : 1) * a.buf_bytes);
+    I* wrow = srow + (a.Q + a.Hlo + a.Hhi);
+    uint32_t lc = 0, lu = 0, ii0 = 0, step = 1;
+    if constexpr (kLanes) {
+        uint32_t lr;
+        a.div_RU.divmod(threadIdx.x, ii0, lr);
+        a.div_upw.divmod(lr, lc, lu);
+        step = blockDim.x / a.RU;
+    }
+    own_fill_stage_rows(a, own, srow, x0, nstage);
+    __syncthreads();
+    if (a.dbuf && cid < a.items) own_stage_in_tab<US, I, kLanes>(a, srow, smem, cid, nstage, lc, lu, ii0, step);
+    uint32_t k = 0;
+    for (uint64_t it = cid; it < a.items; it += ncl, ++k) {
+        const uint32_t boff = a.dbuf ? (k & 1) * a.buf_bytes : 0;
+        if (!a.dbuf) own_stage_in_tab<US, I, kLanes>(a, srow, smem, it, nstage, lc, lu, ii0, step);
+        const OwnItem ci = own_item(a, it);
+        own_fill_write_rows(own, wrow, x0, myrows, ci.col0);
+        if constexpr (US >= 4) asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        __syncthreads();       // the CTA's slots and output rows are visible to all its threads
+        cluster_sync_reuse();  // every CTA holds its rows of this tile: writes may start
+        const uint64_t nxt = it + ncl;
+        if (a.dbuf && nxt < a.items)
+            own_stage_in_tab<US, I, kLanes>(a, srow, smem + (boff ^ a.buf_bytes), nxt, nstage, lc, lu, ii0, step);
+        own_write_rows_tab<US, Own, kLanes>(a, own, smem + boff, ci, wrow, myrows, nstage, lc, lu, ii0, step);
+        __syncthreads();  // this CTA's threads are done with the buffer and the output rows
+    }
+    if constexpr (US >= 4) asm volatile("cp.async.wait_group 0;\n" ::: "memory");  // no copy outlives the CTA
+}
+
 // ---------------------------------------------------------------------------
 // Owner-computed column pass over groups of G co-resident CTAs (a
 // cooperative launch guarantees co-residency), for tiles larger than a
@@ -930,8 +913,10 @@ __device__ __forceinline__ void own_stage_in_tab(const ColOwnArgs& a, const I* s
 // owns slots [r*Q, (r+1)*Q).  The barrier between the group's loads and its
 // writes is a monotonic arrival counter per group in global memory (zeroed
 // before the launch): after its loads of the group's k-th item have landed
-// in shared memory a CTA adds 1 with release semantics, and it writes once
-// the counter has reached (k+1)*G (acquire).  Every wait is bounded: a CTA
+// in shared memory a CTA adds 1, and it writes once the counter has reached
+// (k+1)*G (acquire).  The only hazard is write-after-read, and a read whose
+// value has landed in shared memory cannot see a later write, so the add
+// needs no release semantics (a knob restores them).  Every wait is bounded: a CTA
 // that gives up (or sees another give up) counts a sync timeout, raises the
 // launch's abort flag and returns after its own copies have landed.
 // ---------------------------------------------------------------------------
@@ -1038,35 +1023,7 @@ __global__ void __launch_bounds__(kThreads) k_col_group(ColOwnArgs a, Own own, G
         if (threadIdx.x == 0) s_ok = gs.G <= 1 || group_wait(ctr, (k + 1) * gs.G, abort_flag, gs.sleep_ns);
         __syncthreads();  // every CTA of the group holds its slots: writes may start
         if (!s_ok) break;
-        const uint8_t* buf = smem + boff;
-        if constexpr (kLanes) {
-            if (lc < ci.tcols && lu < ci.lim) {
-                const int64_t d = own.delta(static_cast<I>(ci.col0 + lc)) - own.delta(static_cast<I>(ci.col0));
-                const uint8_t* src = buf + lc * a.w + lu * US;
-                uint8_t* dst = ci.mat + static_cast<uint64_t>(lc) * a.E + lu * US;
-                for (uint32_t ii = ii0; ii < myrows; ii += step) {
-                    const I i = wrow[ii];
-                    const int64_t local = own_local(a, ii, d);
-                    if (!in_range(i, a.rows) || !in_range(static_cast<uint64_t>(local), nstage)) continue;
-                    *reinterpret_cast<U*>(dst + static_cast<uint64_t>(i) * a.row_bytes) =
-                        *reinterpret_cast<const U*>(src + static_cast<uint32_t>(local) * a.pitch);
-                }
-            }
-        } else {
-            const uint32_t units = myrows * a.RU;
-            for (uint32_t x = threadIdx.x; x < units; x += blockDim.x) {
-                uint32_t ii, rr, c, u;
-                a.div_RU.divmod(x, ii, rr);
-                a.div_upw.divmod(rr, c, u);
-                if (c >= ci.tcols || u >= ci.lim) continue;
-                const int64_t d = own.delta(static_cast<I>(ci.col0 + c)) - own.delta(static_cast<I>(ci.col0));
-                const I i = wrow[ii];
-                const int64_t local = own_local(a, ii, d);
-                if (!in_range(i, a.rows) || !in_range(static_cast<uint64_t>(local), nstage)) continue;
-                *reinterpret_cast<U*>(ci.mat + static_cast<uint64_t>(i) * a.row_bytes + static_cast<uint64_t>(c) * a.E + u * US) =
-                    *reinterpret_cast<const U*>(buf + static_cast<uint32_t>(local) * a.pitch + c * a.w + u * US);
-            }
-        }
+        own_write_rows_tab<US, Own, kLanes>(a, own, smem + boff, ci, wrow, myrows, nstage, lc, lu, ii0, step);
         __syncthreads();  // this CTA's threads are done with the buffer and the output rows
     }
     if constexpr (US >= 4) asm volatile("cp.async.wait_group 0;\n" ::: "memory");  // no copy outlives the CTA
@@ -1697,10 +1654,18 @@ ColOwnArgs col_owner_args(uint8_t* data, const Pass& p, const Staging& st, int U
     return a;
 }
 
+// Shared memory of the row tables behind an owner-computed pass's slot
+// buffer(s): Q + Hlo + Hhi source rows and Q output rows.
+template <typename Own>
+size_t owner_table_bytes(const ColOwnArgs& a) {
+    const size_t bytes = (2 * static_cast<size_t>(a.Q) + a.Hlo + a.Hhi) * sizeof(typename Own::index_type);
+    return (bytes + 15) / 16 * 16;
+}
+
 template <int US, typename Own>
 int launch_col_owner(uint8_t* data, const Pass& p, const Staging& st, const Own& own, ExecContext& ctx) {
     const ColOwnArgs a = col_owner_args(data, p, st, US);
-    const size_t smem = (st.dbuf ? 2 : 1) * static_cast<size_t>(a.buf_bytes);
+    const size_t smem = (st.dbuf ? 2 : 1) * static_cast<size_t>(a.buf_bytes) + owner_table_bytes<Own>(a);
     if (kThreads % a.RU != 0)
         EI_CHECK(launch_clusters(k_col_owner<US, Own, false>, st.K, smem, a.items, ctx, a, own));
     else
@@ -1748,8 +1713,7 @@ cudaError_t launch_groups(void (*kernel)(ColOwnArgs, Own, GroupSync), size_t sme
 template <int US, typename Own>
 int launch_col_group(uint8_t* data, const Pass& p, const Staging& st, const Own& own, ExecContext& ctx) {
     const ColOwnArgs a = col_owner_args(data, p, st, US);
-    const size_t tables = (2 * static_cast<size_t>(a.Q) + a.Hlo + a.Hhi) * sizeof(typename Own::index_type);
-    const size_t smem = (st.dbuf ? 2 : 1) * static_cast<size_t>(a.buf_bytes) + (tables + 15) / 16 * 16;
+    const size_t smem = (st.dbuf ? 2 : 1) * static_cast<size_t>(a.buf_bytes) + owner_table_bytes<Own>(a);
     if (ctx.scratch == nullptr || ctx.scratch_bytes < kGroupSyncBytes) {
         ctx.err = "workspace too small for a group-synchronised column pass";
         return EITHOT_STATUS_NOMEM;

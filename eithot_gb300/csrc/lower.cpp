@@ -263,6 +263,9 @@ Staging plan_col_owner(uint64_t rows, uint64_t cols, uint64_t batches, uint64_t 
                        const DeviceCaps& caps) {
     const size_t cap = smem_cap_of(caps);
     const int form = tuning().col_form;
+    // bytes of one row-table entry: the pass's index type (32-bit when
+    // m*n + m + n < 2^31, as the kernels choose it)
+    const uint64_t idx = rows * cols + rows + cols < (uint64_t(1) << 31) ? 4 : 8;
     Staging best;
     best.on_chip = false;
     best.cost = 1e30;
@@ -275,7 +278,9 @@ Staging plan_col_owner(uint64_t rows, uint64_t cols, uint64_t batches, uint64_t 
     if (form != 2 && E <= 128 && !tuning().col_chunk) {
         for (bool db : {true, false}) {
             if (db && !tuning().dbuf) continue;
-            const uint64_t budget = kTwoPerSm / (db ? 2 : 1);
+            const uint64_t tables = 2 * rows * idx + 16;  // source and output row tables
+            if (kTwoPerSm <= tables + 256) continue;
+            const uint64_t budget = (kTwoPerSm - tables) / (db ? 2 : 1) - 127;
             const uint64_t tw_cap = std::min<uint64_t>(cols, budget / (rows * E));
             if (tw_cap < 1 || tw_cap * E < 128) continue;
             const uint64_t want_tiles = 4 * static_cast<uint64_t>(caps.sms);
@@ -309,7 +314,8 @@ Staging plan_col_owner(uint64_t rows, uint64_t cols, uint64_t batches, uint64_t 
                 const uint64_t per = (Q + lo + hi) * pitch;
                 for (bool db : {true, false}) {
                     if (db && !tuning().dbuf) continue;
-                    const uint64_t foot = per * (db ? 2 : 1);
+                    // slot buffer(s), 128-byte rounded, and the row tables
+                    const uint64_t foot = (per + 127) / 128 * 128 * (db ? 2 : 1) + (2 * Q + lo + hi) * idx + 16;
                     if (foot > cap) continue;
                     Staging s;
                     s.w = w; s.tw = tw; s.pitch = pitch; s.K = K; s.per_cta = per;
@@ -339,7 +345,6 @@ Staging plan_col_owner(uint64_t rows, uint64_t cols, uint64_t batches, uint64_t 
                     // tables: Q + lo + hi source rows and Q output rows of the
                     // pass's index type (32-bit when m*n + m + n < 2^31)
                     const uint64_t nbuf = db ? 2 : 1;
-                    const uint64_t idx = rows * cols + rows + cols < (uint64_t(1) << 31) ? 4 : 8;
                     const uint64_t fixed = 16 + nbuf * 127 + (lo + hi) * (nbuf * pitch + idx);
                     if (per_cta_cap <= fixed) continue;
                     const uint64_t qmax = (per_cta_cap - fixed) / (nbuf * pitch + 2 * idx);

@@ -81,7 +81,8 @@ struct Tuning {
     int slab_cluster = 1;  // matrices beyond one CTA's share: one owner-computed pass over a cluster
     int factor = 1;        // split a transpose along a factor of R or C when a pass would stage globally
     int sync_sleep_ns = 64;  // group barriers: back-off between polls
-    int sync_relaxed = 0;    // group barriers: arrive without release semantics
+    int sync_relaxed = 1;    // group barriers: arrive without release semantics (every load of the
+                             // arriving CTA has landed in shared memory before it arrives)
     int group_per_sm = 0;    // group form: 0 cost model, 1 or 2 CTAs per SM
     int l2_prefetch = 0;     // group form, single-buffered: prefetch the next item into L2 (slower on GB300)
 };

@@ -251,6 +251,8 @@ int eithot_estimate_report(int rank, const int64_t* dims, const int* perm_1based
  *                 into two on-chip transposes when that is cheaper, 0 not
  *   "sync_sleep_ns" back-off between polls of a group barrier (0..100000)
  *   "sync_relaxed" 1 group-barrier arrivals without release semantics
+ *                 (default: the arriving CTA's loads have all landed in
+ *                 shared memory), 0 release arrivals
  *   "group_per_sm" group form: 0 cost model, 1..4 resident CTAs per SM
  *   "l2_prefetch" 1 single-buffered group passes prefetch the next item into
  *                 L2 while they wait at the barrier, 0 not (default; slower) */
