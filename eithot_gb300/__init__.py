@@ -382,7 +382,7 @@ def selftest_wait() -> int:
 def tune_set(key: str, value: float) -> None:
     """Process-wide lowering knob ("dbuf", "max_cluster", "variant", "col_batch", "col_chunk",
     "col_owner", "col_form", "row_prefetch", "row_block", "slab_pack", "slab_cluster", "factor", "sync_sleep_ns", "sync_relaxed",
-    "group_per_sm", "l2_prefetch")."""
+    "group_per_sm", "l2_prefetch", "batch_graph")."""
     _check(lib.eithot_tune_set(key.encode(), float(value)))
 
 

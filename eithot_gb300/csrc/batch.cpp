@@ -8,7 +8,9 @@
 // while other lanes' kernels occupy SMs).  Every lane has its own scratch
 // slice of the batch workspace.  A tensor whose shape has recorded knobs
 // (eithot_tune_shape_set, e.g. from the autotuner) is planned and run with
-// them.
+// them.  Work is issued round-robin over the lanes so that every lane has
+// work queued from the start; a run that repeats the previous run's buffers
+// is captured once into a CUDA graph and replayed from then on.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -46,6 +48,15 @@ struct eithot_batch {
     std::vector<cudaEvent_t> done;
     cudaEvent_t fork = nullptr;
     int last_launches = 0;
+    // the graph form: the previous run's buffers, and the capture of a run on them
+    std::vector<void*> prev_data;
+    std::vector<size_t> prev_caps;
+    void* prev_ws = nullptr;
+    bool have_prev = false;
+    cudaStream_t origin = nullptr;  // capture stream
+    cudaGraphExec_t exec = nullptr;
+    bool graph_failed = false;      // the capture on these buffers did not succeed: issue directly
+    int graph_launches = 0;
 };
 
 namespace {
@@ -66,6 +77,79 @@ int make_streams(eithot_batch* b) {
     }
     if (e != cudaSuccess) return fail(EITHOT_ECUDA, std::string("batch streams: ") + cudaGetErrorString(e));
     return EITHOT_OK;
+}
+
+// Forks the lanes from `from`, issues every tensor's passes on its lane
+// (round-robin over the lanes) and joins every forked lane back into `from`,
+// whatever happened.
+int enqueue(eithot_batch* b, void* const* d_data, uint8_t* ws, cudaStream_t from) {
+    cudaError_t e = cudaEventRecord(b->fork, from);
+    const size_t lanes = b->streams.size();
+    std::vector<bool> forked(lanes, false);
+    for (size_t l = 0; l < lanes && e == cudaSuccess; ++l) {
+        e = cudaStreamWaitEvent(b->streams[l], b->fork, 0);
+        forked[l] = e == cudaSuccess;
+    }
+    int rc = EITHOT_OK;
+    std::string err;
+    b->last_launches = 0;
+    size_t rounds = 0;
+    for (const auto& li : b->lane_items) rounds = std::max(rounds, li.size());
+    for (size_t r = 0; r < rounds && e == cudaSuccess && rc == EITHOT_OK; ++r) {
+        for (size_t l = 0; l < lanes && rc == EITHOT_OK; ++l) {
+            if (r >= b->lane_items[l].size()) continue;
+            const int t = b->lane_items[l][r];
+            ScopedTuning scope(b->items[t].tuning);
+            ExecContext ctx;
+            ctx.caps = b->caps;
+            ctx.stream = b->streams[l];
+            ctx.scratch = ws ? ws + b->lane_offset[l] : nullptr;
+            ctx.scratch_bytes = ws ? b->lane_bytes[l] : 0;
+            rc = run_passes(static_cast<uint8_t*>(d_data[t]), b->items[t].passes, ctx);
+            if (rc) err = "tensor " + std::to_string(t) + ": " + ctx.err;
+            b->last_launches += ctx.launches;
+        }
+    }
+    for (size_t l = 0; l < lanes; ++l) {
+        if (!forked[l]) continue;
+        const cudaError_t j = cudaEventRecord(b->done[l], b->streams[l]);
+        if (j == cudaSuccess) cudaStreamWaitEvent(from, b->done[l], 0);
+        if (e == cudaSuccess) e = j;
+    }
+    if (rc) return fail(rc, err);
+    if (e != cudaSuccess) return fail(EITHOT_ECUDA, std::string("batch: ") + cudaGetErrorString(e));
+    return EITHOT_OK;
+}
+
+void drop_graph(eithot_batch* b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+}
+
+// Captures one run on the remembered buffers into b->exec; false (and no
+// graph) when the capture or instantiation did not succeed.
+bool capture(eithot_batch* b, void* const* d_data, uint8_t* ws) {
+    if (!b->origin && cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        b->origin = nullptr;
+        return false;
+    }
+    if (cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    const int rc = enqueue(b, d_data, ws, b->origin);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(b->origin, &g);
+    if (rc == EITHOT_OK && e == cudaSuccess && g) e = cudaGraphInstantiate(&b->exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (rc != EITHOT_OK || e != cudaSuccess || !b->exec) {
+        cudaGetLastError();
+        b->exec = nullptr;
+        return false;
+    }
+    b->graph_launches = b->last_launches;
+    return true;
 }
 
 }  // namespace
@@ -172,32 +256,30 @@ int eithot_batch_run(eithot_batch* b, void* const* d_data, const size_t* capacit
             owned = true;
         }
     }
-    cudaError_t e = cudaEventRecord(b->fork, st);
-    int rc = EITHOT_OK;
-    std::string err;
-    b->last_launches = 0;
-    for (size_t l = 0; l < b->streams.size() && e == cudaSuccess && rc == EITHOT_OK; ++l) {
-        e = cudaStreamWaitEvent(b->streams[l], b->fork, 0);
-        for (int t : b->lane_items[l]) {
-            if (e != cudaSuccess || rc != EITHOT_OK) break;
-            ScopedTuning scope(b->items[t].tuning);
-            ExecContext ctx;
-            ctx.caps = b->caps;
-            ctx.stream = b->streams[l];
-            ctx.scratch = ws ? ws + b->lane_offset[l] : nullptr;
-            ctx.scratch_bytes = ws ? b->lane_bytes[l] : 0;
-            rc = run_passes(static_cast<uint8_t*>(d_data[t]), b->items[t].passes, ctx);
-            if (rc) err = "tensor " + std::to_string(t) + ": " + ctx.err;
-            b->last_launches += ctx.launches;
+    const bool same = b->have_prev && b->prev_ws == ws &&
+                      std::equal(b->prev_data.begin(), b->prev_data.end(), d_data) &&
+                      std::equal(b->prev_caps.begin(), b->prev_caps.end(), capacities);
+    // a graph replays only caller-provided workspace (or none)
+    if (same && !owned && b->tuning.batch_graph && !b->graph_failed) {
+        if (!b->exec) b->graph_failed = !capture(b, d_data, ws);
+        if (b->exec) {
+            const cudaError_t e = cudaGraphLaunch(b->exec, st);
+            if (e != cudaSuccess) return fail(EITHOT_ECUDA, std::string("batch graph: ") + cudaGetErrorString(e));
+            b->last_launches = b->graph_launches;
+            return EITHOT_OK;
         }
-        if (e == cudaSuccess) e = cudaEventRecord(b->done[l], b->streams[l]);
     }
-    // join every lane that was forked, whatever happened
-    for (size_t l = 0; l < b->streams.size(); ++l) cudaStreamWaitEvent(st, b->done[l], 0);
+    if (!same) {
+        drop_graph(b);
+        b->graph_failed = false;
+        b->prev_data.assign(d_data, d_data + b->items.size());
+        b->prev_caps.assign(capacities, capacities + b->items.size());
+        b->prev_ws = ws;
+        b->have_prev = true;
+    }
+    const int rc = enqueue(b, d_data, ws, st);
     if (owned) cudaFreeAsync(ws, st);
-    if (rc) return fail(rc, err);
-    if (e != cudaSuccess) return fail(EITHOT_ECUDA, std::string("batch: ") + cudaGetErrorString(e));
-    return EITHOT_OK;
+    return rc;
 }
 
 int eithot_batch_launches(const eithot_batch* b, int* launches) {
@@ -208,6 +290,8 @@ int eithot_batch_launches(const eithot_batch* b, int* launches) {
 
 int eithot_batch_destroy(eithot_batch* b) {
     if (!b) return EITHOT_OK;
+    drop_graph(b);
+    if (b->origin) cudaStreamDestroy(b->origin);
     for (auto s : b->streams) cudaStreamDestroy(s);
     for (auto ev : b->done) cudaEventDestroy(ev);
     if (b->fork) cudaEventDestroy(b->fork);

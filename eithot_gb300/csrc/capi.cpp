@@ -138,6 +138,8 @@ int apply_knob(eithot::Tuning& t, const char* key, double value) {
         if (v != 0 && v != 32 && v != 64 && v != 128 && v != 256 && v != 512)
             return fail(EITHOT_EINVAL, "col_chunk must be 0, 32, 64, 128, 256 or 512");
         t.col_chunk = v;
+    } else if (k == "batch_graph") {
+        t.batch_graph = value != 0 ? 1 : 0;
     } else if (k == "max_cluster") {
         const int v = static_cast<int>(value);
         if (v != 1 && v != 2 && v != 4 && v != 8 && v != 16) return fail(EITHOT_EINVAL, "max_cluster must be 1, 2, 4, 8 or 16");
@@ -196,6 +198,7 @@ int eithot_tune_get(const char* key, double* value) {
     else if (k == "sync_relaxed") *value = t.sync_relaxed;
     else if (k == "group_per_sm") *value = t.group_per_sm;
     else if (k == "l2_prefetch") *value = t.l2_prefetch;
+    else if (k == "batch_graph") *value = t.batch_graph;
     else if (k == "col_chunk") *value = t.col_chunk;
     else if (k == "max_cluster") *value = t.max_cluster;
     else if (k == "variant") *value = t.variant;

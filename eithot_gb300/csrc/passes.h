@@ -85,6 +85,7 @@ struct Tuning {
                              // arriving CTA has landed in shared memory before it arrives)
     int group_per_sm = 0;    // group form: 0 cost model, 1 or 2 CTAs per SM
     int l2_prefetch = 0;     // group form, single-buffered: prefetch the next item into L2 (slower on GB300)
+    int batch_graph = 1;     // batched form: a run repeating the previous run's buffers replays a CUDA graph
 };
 Tuning& tuning();
 

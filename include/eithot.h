@@ -155,8 +155,12 @@ int eithot_workspace_size(int rank, const int64_t* dims, const int* perm_1based,
  * it from cudaMallocAsync on `stream`) must hold
  * eithot_batch_workspace_size() bytes.  A batch may be run any number of
  * times, on any buffers of the planned shapes, on the device it was planned
- * on; runs of one batch must not overlap.  eithot_batch_launches reports the
- * kernel launches of the last run. */
+ * on; runs of one batch must not overlap.  A run whose buffers, capacities
+ * and (caller-provided) workspace repeat the previous run's is replayed from
+ * a CUDA graph of that work, captured on the first repeat: one graph launch
+ * instead of thousands of kernel launches from the host.  eithot_batch_launches
+ * reports the kernel launches of the last run (the graph's kernel nodes when
+ * it was replayed). */
 typedef struct eithot_batch eithot_batch;
 
 int eithot_batch_create(int count, const int* ranks, const int64_t* dims, const int* perms_1based,
@@ -255,7 +259,10 @@ int eithot_estimate_report(int rank, const int64_t* dims, const int* perm_1based
  *                 shared memory), 0 release arrivals
  *   "group_per_sm" group form: 0 cost model, 1..4 resident CTAs per SM
  *   "l2_prefetch" 1 single-buffered group passes prefetch the next item into
- *                 L2 while they wait at the barrier, 0 not (default; slower) */
+ *                 L2 while they wait at the barrier, 0 not (default; slower)
+ *   "batch_graph" 1 a batch run on the same buffers and workspace as the
+ *                 batch's previous run replays the work as a CUDA graph
+ *                 (captured on the first repeat), 0 always issue directly */
 int eithot_tune_set(const char* key, double value);
 int eithot_tune_get(const char* key, double* value);
 

@@ -100,3 +100,19 @@ def test_batch_uses_shape_knobs(E):
         run_batch(E, tensors, seed=31)
     finally:
         E.tune_shape_clear()
+
+
+@gpu
+@pytest.mark.parametrize("graph", [1, 0])
+def test_batch_repeated_runs_replay_a_graph(E, graph):
+    """Runs on the same buffers and workspace: the first issues directly, the
+    second captures a CUDA graph and every later one replays it (with the
+    knob off, every run issues directly); new contents every run, each
+    bit-exact."""
+    saved = E.tune_get("batch_graph")
+    try:
+        E.tune_set("batch_graph", graph)
+        tensors = random_tensors(60, 9) + [([3001, 4096], [2, 1], 4), ([2, 300000], [2, 1], 1), ([60, 40, 3401], [3, 1, 2], 2)]
+        run_batch(E, tensors, seed=41, caller_workspace=True, runs=4)
+    finally:
+        E.tune_set("batch_graph", saved)
