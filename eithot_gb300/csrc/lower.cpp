@@ -28,8 +28,8 @@ void gcd_inverse(uint64_t a, uint64_t b, uint64_t* g, uint64_t* inv) {
 }
 
 size_t smem_cap_of(const DeviceCaps& caps) {
-    // Leave room for the block's static shared memory and the driver's
-    // per-block reservation.
+    // Leave room for the block's static shared memory and the CUDA
+    // runtime's per-block reservation.
     return caps.smem_optin > 2048 ? caps.smem_optin - 2048 : caps.smem_optin;
 }
 

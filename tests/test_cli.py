@@ -65,7 +65,7 @@ def test_cli_usage_errors(E, tmp_path):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("args", [
-    [3001, 4096, 2, 1, 4, 1, 0.01],                   # first BASELINE config
+    [3001, 4096, 2, 1, 4, 1, 0.01],                   # 3001x4096 int32, one sub-tensor
     [7249, 50, 2, 1, 4, 4, 0.02],                      # sub-tensors with padding
     [33, 17, 9, 2, 3, 1, 8, 1, 0.01],                  # 64-bit elements
     [16, 3001, 64, 3, 1, 2, 2, 1, 0.05],               # 16-bit elements (beyond the reference)

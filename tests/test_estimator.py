@@ -37,7 +37,8 @@ def test_reference_crash_case_is_handled(E):
         assert nb >= 1 and alpha > 0
 
 
-def test_baseline_configs(E):
+def test_benchmark_shapes(E):
+    """3001x4096 int32 and (4,20011,8192,2) int32 perm (1 3 2 4) at alpha 0.01."""
     assert E.estimate([3001, 4096], [2, 1], 4, 1, 0.01, 49152, 304)[:2] == (1, 0.01)
     nb, alpha, extra = E.estimate([4, 20011, 8192, 2], [1, 3, 2, 4], 4, 1, 0.01, 49152, 304)
     assert (nb, alpha) == (1, 0.01) and extra == 4 * 256 * 8192

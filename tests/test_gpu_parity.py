@@ -41,7 +41,7 @@ def run_case(E, dims, perm, elem, nb=1, alpha=0.01, order=0, slack=1.0, seed=1, 
     return E.last_stats()
 
 
-def test_config1_iota_2d(E):
+def test_iota_3001x4096_int32(E):
     """3001 x 4096 int32 iota, perm (2 1), nb 1, alpha 0.01: byte-exact vs the
     oracle and the reference's verify_inplace known answer."""
     dims, perm = [3001, 4096], [2, 1]
@@ -297,7 +297,7 @@ def test_reference_signature_shim(E):
 
 
 @pytest.mark.slow
-def test_config2_full_size(E):
+def test_4x20011x8192x2_int32_full_size(E):
     """(4, 20011, 8192, 2) int32, perm (1 3 2 4), nb/alpha from the
     estimator, extra device memory within alpha * bytes."""
     dims, perm = [4, 20011, 8192, 2], [1, 3, 2, 4]
@@ -336,7 +336,7 @@ def test_device_hash_fill_and_check(E):
 
 
 @pytest.mark.slow
-def test_config3_full_size_uint16(E):
+def test_16x3001x1024x256x4_uint16_full_size(E):
     """(16, 3001, 1024, 256, 4) uint16 (100.7 GB), perm (5 3 1 4 2), nb/alpha
     from the estimator at alpha 0.05: the tensor no 32-bit planner can
     describe.  Every output element is checked on the device against the
