@@ -87,7 +87,7 @@ def test_catanzaro_2d(E, R, C, elem):
 @pytest.fixture
 def tuned(E):
     keys = ("variant", "col_owner", "col_chunk", "max_cluster", "dbuf", "col_form", "row_prefetch", "row_block",
-            "slab_pack", "slab_cluster", "factor")
+            "slab_pack", "slab_cluster", "factor", "sync_relaxed", "group_per_sm")
     saved = {k: E.tune_get(k) for k in keys}
 
     def set_(**kw):
@@ -125,6 +125,22 @@ def test_column_tilings(E, tuned, chunk, max_cluster, dbuf, form):
         run_case(E, [4096, 3001], [2, 1], 4)
         run_case(E, [4, 20011, 819, 2], [1, 3, 2, 4], 4)
         run_case(E, [4000, 6000], [2, 1], 2)
+
+
+@pytest.mark.parametrize("relaxed", [0, 1])
+@pytest.mark.parametrize("per_sm", [1, 2, 3])
+def test_group_arrivals_and_residency(E, tuned, relaxed, per_sm):
+    """Group column passes with release and with relaxed arrivals, at one to
+    three CTAs per SM (row tables in shared memory sized for each), c2r and
+    r2c, gcd 1 and gcd > 1, 1- to 32-byte and 3-byte elements."""
+    tuned(col_form=2, dbuf=0, sync_relaxed=relaxed, group_per_sm=per_sm)
+    for variant in (1, 2):
+        E.tune_set("variant", variant)
+        run_case(E, [4096, 3001], [2, 1], 4)
+        run_case(E, [4, 20011, 819, 2], [1, 3, 2, 4], 4)
+        run_case(E, [6000, 4000], [2, 1], 1)
+        run_case(E, [2048, 1536], [2, 1], 32)
+        run_case(E, [999, 5003], [2, 1], 3)
 
 
 @pytest.mark.parametrize("dims,perm,elem", [([4, 3001, 8192, 1], [1, 3, 2, 4], 4), ([2, 3001, 16384, 1], [1, 3, 2, 4], 4),
