@@ -14,6 +14,15 @@
 // (8- and 16-bit elements, whose iota wraps) are accepted too.  Dims are
 // 64-bit: there is no 22 GB limit.  Errors print a message and exit 1
 // instead of the reference's exit(-1).
+//
+// EITHOT_MEMORY_TYPE=2 in the environment selects the reference's managed
+// path, which it selects at compile time (MEMORY_TYPE 2,
+// padding_managed_transpose, ITNT/src/test_inplace.cpp:91-136): the tensor
+// lives in cudaMallocManaged memory with 3 % slack (host-filled, transposed
+// where it lies, checked in place by the host), its own output lines, and
+// the throughput 2 * slack-padded bytes / time.  The reference never
+// records its start event there, so its elapsed-time call fails; this
+// program records it before the transpose.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -159,6 +168,63 @@ int run(const std::vector<int64_t>& dims, const std::vector<int>& perm, int nb, 
     return ok ? 0 : 3;
 }
 
+template <typename T>
+int run_managed(const std::vector<int64_t>& dims, const std::vector<int>& perm, int nb, double alpha) {
+    const int rank = static_cast<int>(dims.size());
+    int64_t vol = 1;
+    for (auto d : dims) vol *= d;
+    const size_t gpu_size =
+        static_cast<size_t>((1.0 + kPaddingSlack) * static_cast<double>(vol) * static_cast<double>(sizeof(T)));
+    T* m = nullptr;
+    CLI_CHECK(cudaMallocManaged(&m, std::max(gpu_size, sizeof(T))));
+    init_iota(m, vol);
+
+    long long perm_int = 0, pow10 = 1;
+    for (int i = 0; i < rank; ++i, pow10 *= 10) perm_int += pow10 * perm[rank - i - 1];
+    std::printf("%dD Inplace %lld transpose", rank, perm_int);
+    std::printf(", Data size = %.5f GB\n", static_cast<double>(gpu_size) / 1e9);
+    std::printf("number of sub_tensors = %d\n", nb);
+
+    cudaEvent_t start, stop;
+    CLI_CHECK(cudaEventCreate(&start));
+    CLI_CHECK(cudaEventCreate(&stop));
+    CLI_CHECK(cudaEventRecord(start, 0));
+    if (eithot_transpose(m, gpu_size, rank, dims.data(), perm.data(), sizeof(T), nb, alpha, nullptr) != EITHOT_OK) {
+        std::fprintf(stderr, "test_inplace: %s\n", eithot_last_error());
+        return 1;
+    }
+    CLI_CHECK(cudaDeviceSynchronize());
+    CLI_CHECK(cudaEventRecord(stop, 0));
+    CLI_CHECK(cudaEventSynchronize(stop));
+    float t = 0;
+    CLI_CHECK(cudaEventElapsedTime(&t, start, stop));
+
+    std::printf("Inplace transpose verify_inplace\n");
+    unsigned faults = 0, timeouts = 0;
+    eithot_index_faults(&faults);
+    eithot_sync_timeouts(&timeouts);
+    const bool ok = verify_inplace(m, dims, perm) && faults == 0 && timeouts == 0;
+    std::printf(ok ? "Correct transpose\n" : "Incorrect transpose\n");
+
+    const double throughput = static_cast<double>(gpu_size) * 2 / 1e6 / t;
+    std::printf("Execution Time: %.5fms\n", t);
+    if (FILE* f = std::fopen("inplace_bench.txt", "a+")) {
+        std::fprintf(f, "%.5f\n", t);
+        std::fclose(f);
+    }
+    if (FILE* f = std::fopen("inplace_bench_throughput.txt", "a+")) {
+        std::fprintf(f, "%.5f\n", throughput);
+        std::fclose(f);
+    }
+    CLI_CHECK(cudaFree(m));
+    return ok ? 0 : 3;
+}
+
+template <typename T>
+int run_mode(bool managed, const std::vector<int64_t>& dims, const std::vector<int>& perm, int nb, double alpha) {
+    return managed ? run_managed<T>(dims, perm, nb, alpha) : run<T>(dims, perm, nb, alpha);
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -180,10 +246,12 @@ int main(int argc, char** argv) {
     }
     for (int i = 0; i < rank; ++i)
         if (dims[i] < 1) { std::printf("Invalid rank or type size\n"); return 0; }
-    if (type_size == 4) return run<int32_t>(dims, perm, nb, alpha);
-    if (type_size > 4) return run<int64_t>(dims, perm, nb, alpha);
-    if (type_size == 2) return run<uint16_t>(dims, perm, nb, alpha);
-    if (type_size == 1) return run<uint8_t>(dims, perm, nb, alpha);
+    const char* mt = std::getenv("EITHOT_MEMORY_TYPE");
+    const bool managed = mt && std::atoi(mt) == 2;
+    if (type_size == 4) return run_mode<int32_t>(managed, dims, perm, nb, alpha);
+    if (type_size > 4) return run_mode<int64_t>(managed, dims, perm, nb, alpha);
+    if (type_size == 2) return run_mode<uint16_t>(managed, dims, perm, nb, alpha);
+    if (type_size == 1) return run_mode<uint8_t>(managed, dims, perm, nb, alpha);
     std::printf("Invalid rank or type size\n");
     return 0;
 }

@@ -84,3 +84,27 @@ def test_test_inplace_runs_and_verifies(E, tmp_path, args):
     assert (tmp_path / "inplace_bench.txt").read_text() == "%.5f\n" % t
     thr = float((tmp_path / "inplace_bench_throughput.txt").read_text())
     assert thr > 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("args", [
+    [3001, 4096, 2, 1, 4, 1, 0.01],                   # 3001x4096 int32
+    [7249, 50, 2, 1, 4, 4, 0.02],                      # sub-tensors with padding
+    [33, 17, 9, 2, 3, 1, 8, 1, 0.01],                  # 64-bit elements
+    [6, 4, 3401, 3, 2, 1, 1, 2, 0.01]])                # 8-bit elements, sub-tensors
+def test_test_inplace_managed_memory(E, tmp_path, args):
+    """EITHOT_MEMORY_TYPE=2: the reference's managed path (tensor in
+    cudaMallocManaged memory with 3 % slack, transposed where it lies,
+    checked in place by the host), with its own output lines."""
+    env = dict(os.environ, EITHOT_MEMORY_TYPE="2")
+    p = run("test_inplace", args, tmp_path, env=env)
+    assert p.returncode == 0, p.stdout + p.stderr
+    lines = p.stdout.splitlines()
+    rank = (len(args) - 3) // 2
+    assert lines[0].startswith("%dD Inplace " % rank) and ", Data size = " in lines[0]
+    assert lines[1] == "number of sub_tensors = %d" % args[2 * rank + 1]
+    assert lines[2:4] == ["Inplace transpose verify_inplace", "Correct transpose"]
+    assert lines[4].startswith("Execution Time: ")
+    t = float(lines[4].split(": ")[1].rstrip("ms"))
+    assert (tmp_path / "inplace_bench.txt").read_text() == "%.5f\n" % t
+    assert float((tmp_path / "inplace_bench_throughput.txt").read_text()) > 0
