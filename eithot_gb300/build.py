@@ -6,7 +6,8 @@ Host C++ is compiled by g++, CUDA by nvcc (one -gencode, sm_103a), in
 parallel; the library links the CUDA runtime statically and carries no torch
 dependency.  Objects go to eithot_gb300/_build/.  The drop-in replacements of
 the reference's command-line programs (test_inplace, Nd_estimation) are
-linked against the library into eithot_gb300/bin/.
+linked against the library into eithot_gb300/bin/, beside a copy of
+Statistic.py (the summary script the reference's benchmark runs).
 """
 from __future__ import annotations
 
@@ -25,6 +26,7 @@ LIB = os.path.join(LIBDIR, "libeithot.so")
 CLIDIR = os.path.join(PKG, "cli")
 BINDIR = os.path.join(PKG, "bin")
 CLI_PROGRAMS = {"test_inplace": "test_inplace.cpp", "Nd_estimation": "nd_estimation.cpp"}
+CLI_SCRIPTS = ["Statistic.py"]  # run by the reference's benchmark script beside the programs
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["kernels.cu", "checks.cu"]
@@ -96,6 +98,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
         for out in ex.map(_run, cli_jobs):
             if verbose and out.strip():
                 print(out)
+    for name in CLI_SCRIPTS:
+        shutil.copyfile(os.path.join(CLIDIR, name), os.path.join(BINDIR, name))
     return LIB
 
 

@@ -108,3 +108,19 @@ def test_test_inplace_managed_memory(E, tmp_path, args):
     t = float(lines[4].split(": ")[1].rstrip("ms"))
     assert (tmp_path / "inplace_bench.txt").read_text() == "%.5f\n" % t
     assert float((tmp_path / "inplace_bench_throughput.txt").read_text()) > 0
+
+
+def test_statistic_summarises_the_bench_files(tmp_path):
+    """Statistic.py (copied beside the programs into eithot_gb300/bin): mean and
+    population standard deviation of inplace_bench.txt and
+    inplace_bench_throughput.txt, printed and written to Statistic.txt."""
+    import statistics
+    (tmp_path / "inplace_bench.txt").write_text("70.5\n72.25\n60.0\n")
+    (tmp_path / "inplace_bench_throughput.txt").write_text("6.5\n6.0\n")
+    p = subprocess.run(["python3", os.path.join(ROOT, "eithot_gb300", "cli", "Statistic.py")], cwd=tmp_path,
+                       capture_output=True, text=True, timeout=60)
+    assert p.returncode == 0, p.stderr
+    want = ("Bench time:\n\tAvg:  %r\n\tStd:  %r\nThroughput:\n\tAvg:  %r\n\tStd:  %r\n"
+            % (statistics.fmean([70.5, 72.25, 60.0]), statistics.pstdev([70.5, 72.25, 60.0]), 6.25, 0.25))
+    assert p.stdout == want
+    assert (tmp_path / "Statistic.txt").read_text() == want
