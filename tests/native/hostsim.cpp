@@ -151,6 +151,45 @@ int hs_describe_staging(char* buf, size_t len, int rank, const int64_t* dims, co
     return static_cast<int>(passes.size());
 }
 
+// Shared memory every owner-computed column pass of the plan launches with,
+// computed as the executor computes it (the slot buffer(s), 128-byte
+// rounded, then the row tables: Q + Hlo + Hhi source rows and Q output rows
+// of the pass's index type, 16-byte rounded), against what the planner may
+// use: at most the per-block opt-in limit, and for group passes at most the
+// SM's share for the planned CTAs per SM less the 1 KB the hardware
+// reserves per block.  Returns the number of passes over budget (or -1).
+long hs_check_owner_smem(int rank, const int64_t* dims, const int* perm, size_t elem, int nb, double alpha,
+                         int order, int* owner_passes) {
+    NdPlan plan;
+    if (!make_nd_plan(rank, dims, perm, nb, alpha, order, &plan, &g_err)) return -1;
+    std::vector<Pass> passes;
+    DeviceCaps caps;
+    if (!lower_plan(plan, elem, caps, &passes, &g_err)) return -1;
+    long bad = 0;
+    int owners = 0;
+    for (const Pass& p : passes) {
+        if (p.type != kColGather) continue;
+        const Staging st = plan_col_pass(p, caps);
+        if (!st.on_chip || !st.owner) continue;
+        ++owners;
+        const uint64_t parts = st.group ? static_cast<uint64_t>(st.G) : static_cast<uint64_t>(st.K);
+        const uint64_t Q = (p.rows + parts - 1) / parts;
+        const uint64_t slots = Q + st.hlo + st.hhi;
+        const uint64_t buf = (slots * st.pitch + 127) / 128 * 128;
+        const uint64_t idx = fits32(p) ? 4 : 8;
+        const uint64_t tables = ((2 * Q + st.hlo + st.hhi) * idx + 15) / 16 * 16;
+        const uint64_t smem = (st.dbuf ? 2 : 1) * buf + tables;
+        bool over = smem > caps.smem_optin;
+        if (st.group) over = over || smem + 1024 > caps.smem_per_sm / static_cast<uint64_t>(st.per_sm);
+        if (over) {
+            ++bad;
+            g_err = p.what + ": " + std::to_string(smem) + " bytes of shared memory";
+        }
+    }
+    if (owner_passes) *owner_passes = owners;
+    return bad;
+}
+
 // Compares the 32-bit flavour of every Catanzaro map the plan uses with the
 // 64-bit flavour over all (i, j) when m*n <= max_full, else a strided
 // sample.  Returns the number of disagreements (or -1 on error).
@@ -304,6 +343,8 @@ int hs_tune(const char* key, int value) {
     Tuning& t = tuning();
     if (k == "max_cluster") t.max_cluster = value;
     else if (k == "col_form") t.col_form = value;
+    else if (k == "group_per_sm") t.group_per_sm = value;
+    else if (k == "dbuf") t.dbuf = value;
     else if (k == "factor") t.factor = value;
     else if (k == "slab_cluster") t.slab_cluster = value;
     else return -1;

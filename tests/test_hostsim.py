@@ -130,3 +130,40 @@ def test_factored_transposes(hostsim, dims, perm, elem):
     finally:
         hostsim.hs_tune(b"max_cluster", 16)
         hostsim.hs_tune(b"col_form", 0)
+
+
+OWNER_SHAPES = [([4, 20011, 8192, 2], [1, 3, 2, 4], 4), ([3001, 4096], [2, 1], 4), ([4096, 3001], [2, 1], 4),
+                ([20011, 819, 8], [2, 1, 3], 4), ([4000, 6000], [2, 1], 2), ([6000, 4000], [2, 1], 1),
+                ([2048, 1536], [2, 1], 32), ([999, 5003], [2, 1], 3), ([60, 40, 3401], [3, 1, 2], 2),
+                ([5, 70000], [2, 1], 8), ([70000, 5], [2, 1], 8), ([16, 3001, 1024, 256, 4], [5, 3, 1, 4, 2], 2),
+                ([2, 300000], [2, 1], 1), ([777, 14000], [2, 1], 8), ([1000003, 3], [2, 1], 4)]
+
+
+@pytest.mark.parametrize("form,per_sm,dbuf", [(0, 0, 1), (1, 0, 1), (1, 0, 0), (2, 1, 1), (2, 2, 0), (2, 3, 0),
+                                              (2, 4, 0), (2, 2, 1)])
+def test_owner_passes_fit_their_shared_memory(hostsim, form, per_sm, dbuf):
+    """Every owner-computed column pass, with its row tables, fits the
+    per-block limit, and a group pass fits the SM share it was planned for
+    (else the cooperative launch would find fewer co-resident CTAs)."""
+    import ctypes
+    hostsim.hs_tune.argtypes = [ctypes.c_char_p, ctypes.c_int]
+    hostsim.hs_check_owner_smem.restype = ctypes.c_long
+    hostsim.hs_check_owner_smem.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int),
+                                            ctypes.c_size_t, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                            ctypes.POINTER(ctypes.c_int)]
+    owners = 0
+    try:
+        for key, value in (("col_form", form), ("group_per_sm", per_sm), ("dbuf", dbuf)):
+            assert hostsim.hs_tune(key.encode(), value) == 0
+        for dims, perm, elem in OWNER_SHAPES:
+            r = len(dims)
+            n = ctypes.c_int(0)
+            bad = hostsim.hs_check_owner_smem(r, (ctypes.c_int64 * r)(*dims), (ctypes.c_int * r)(*perm), elem, 1,
+                                              ctypes.c_double(0.05), 0, ctypes.byref(n))
+            assert bad == 0, (dims, perm, elem, hostsim.hs_last_error().decode())
+            owners += n.value
+    finally:
+        hostsim.hs_tune(b"col_form", 0)
+        hostsim.hs_tune(b"group_per_sm", 0)
+        hostsim.hs_tune(b"dbuf", 1)
+    assert owners > 0
