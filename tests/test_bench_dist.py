@@ -68,3 +68,21 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch, capsys):
     ns = argparse.Namespace(gpus=2, steps=1, warmup=0, impl="reference")
     assert bench.run_reference(ns) == 0
     assert capsys.readouterr().out == ""
+
+
+def test_reference_arm_line_on_rank_zero():
+    """`bench.py --impl reference` on the host: one JSON line with the arm's
+    own metric, a cpu_baseline describing the run and an e2e with no host
+    copies."""
+    import json
+    import subprocess
+    import sys
+    p = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "3"], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert p.returncode == 0, p.stderr
+    line = json.loads(p.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "GB/s" and line["higher_is_better"] is True
+    assert line["value"] > 0 and line["steps"] == 1 and line["warmup"] == 3
+    cb = line["cpu_baseline"]
+    assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"] and cb["value"] == line["value"]
+    assert line["e2e"] == {"value": line["value"], "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
