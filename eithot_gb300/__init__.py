@@ -19,7 +19,7 @@ from typing import List, Optional, Sequence
 _PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_PKG, "_lib", "libeithot.so")
 
-OK, EINVAL, ENOMEM, ETIMEOUT, ECUDA, EUNSUPPORTED, EBUSY = range(7)
+OK, EINVAL, ENOMEM, ETIMEOUT, ECUDA, EUNSUPPORTED, EBUSY, EFAULT = range(8)
 ORDER_MIXED, ORDER_PRE, ORDER_POST = 0, 1, 2
 STEP_ROUND, STEP_PARTITION, STEP_JOIN, STEP_PAD_PRE, STEP_PAD_POST = range(5)
 
@@ -88,6 +88,10 @@ def _load():
                                          ctypes.c_size_t, ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_uint64)]
     lib.eithot_server_poll.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64), ctypes.c_int,
                                        ctypes.POINTER(ctypes.c_int)]
+    lib.eithot_server_poll_status.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64),
+                                              ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+    lib.eithot_server_memory.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t),
+                                         ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]
     lib.eithot_server_pending.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
     lib.eithot_server_launches.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
     lib.eithot_server_destroy.argtypes = [ctypes.c_void_p]
@@ -95,6 +99,8 @@ def _load():
     lib.eithot_tune_get.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double)]
     lib.eithot_tune_shape_set.argtypes = [ctypes.c_int, I64P, IP, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_double]
     lib.eithot_tune_shape_count.argtypes = [ctypes.POINTER(ctypes.c_int)]
+    lib.eithot_last_call.argtypes = [ctypes.POINTER(ctypes.c_uint64)]
+    lib.eithot_call_status.argtypes = [ctypes.c_uint64, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
     return lib
 
 
@@ -200,6 +206,22 @@ def transpose(tensor, dims, perm, num_sub_tensors: int = 1, alpha: float = 0.01,
     with torch.cuda.device(tensor.device):
         transpose_ptr(tensor.data_ptr(), cap, dims, perm, es, num_sub_tensors, alpha, order, sptr)
     return tensor
+
+
+def last_call() -> int:
+    """Id of this thread's most recent transpose call (eithot_last_call)."""
+    v = ctypes.c_uint64()
+    _check(lib.eithot_last_call(ctypes.byref(v)))
+    return v.value
+
+
+def call_status(call_id: int, stream: Optional[int] = None) -> int:
+    """Synchronises `stream` and returns the device-side outcome of call
+    `call_id`: OK, ETIMEOUT (a bounded group-barrier wait gave up) or EFAULT
+    (an index-map result fell outside its row or column)."""
+    v = ctypes.c_int()
+    _check(lib.eithot_call_status(call_id, ctypes.c_void_p(stream) if stream else None, ctypes.byref(v)))
+    return v.value
 
 
 def last_stats() -> dict:
@@ -322,6 +344,7 @@ class Server:
         _check(lib.eithot_server_create(workspace_bytes, streams, ctypes.byref(h)))
         self._h = h
         self._done = (ctypes.c_uint64 * 4096)()
+        self._status = (ctypes.c_int * 4096)()
 
     def submit(self, ptr: int, capacity_bytes: int, dims, perm, elem_size: int, num_sub_tensors: int = 1,
                alpha: float = 0.01) -> int:
@@ -332,13 +355,24 @@ class Server:
         return t.value
 
     def poll(self) -> List[int]:
+        return [t for t, _ in self.poll_status()]
+
+    def poll_status(self):
+        """Finished tickets with their device status (OK, ETIMEOUT, EFAULT)."""
         out = []
         while True:
             n = ctypes.c_int()
-            _check(lib.eithot_server_poll(self._h, self._done, len(self._done), ctypes.byref(n)))
-            out += list(self._done[: n.value])
+            _check(lib.eithot_server_poll_status(self._h, self._done, self._status, len(self._done),
+                                                 ctypes.byref(n)))
+            out += list(zip(self._done[: n.value], self._status[: n.value]))
             if n.value < len(self._done):
                 return out
+
+    def memory(self):
+        """(resident tensor bytes, pool bytes, scratch held in free HBM)."""
+        r, p, h = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_size_t()
+        _check(lib.eithot_server_memory(self._h, ctypes.byref(r), ctypes.byref(p), ctypes.byref(h)))
+        return r.value, p.value, h.value
 
     def pending(self):
         q, r = ctypes.c_int(), ctypes.c_int()
@@ -381,7 +415,8 @@ def selftest_wait() -> int:
 
 def tune_set(key: str, value: float) -> None:
     """Process-wide lowering knob ("dbuf", "max_cluster", "variant", "col_batch", "col_chunk",
-    "col_owner", "col_form", "row_prefetch", "row_block", "slab_pack", "slab_cluster", "factor", "sync_sleep_ns", "sync_relaxed",
+    "col_owner", "col_form", "row_prefetch", "row_block", "slab_pack", "slab_cluster", "factor", "sync_sleep_ns",
+    "sync_spin_limit", "sync_relaxed",
     "group_per_sm", "l2_prefetch", "batch_graph")."""
     _check(lib.eithot_tune_set(key.encode(), float(value)))
 

@@ -26,6 +26,7 @@ thread_local size_t g_events_used = 0;
 thread_local std::vector<std::pair<size_t, size_t>> g_spans;
 thread_local std::vector<std::string> g_pass_names;
 thread_local std::vector<double> g_pass_bytes;
+thread_local uint64_t g_last_call = 0;
 
 }  // namespace
 
@@ -111,12 +112,17 @@ int apply_knob(eithot::Tuning& t, const char* key, double value) {
     } else if (k == "sync_sleep_ns") {
         if (value < 0 || value > 100000) return fail(EITHOT_EINVAL, "sync_sleep_ns must be 0..100000");
         t.sync_sleep_ns = static_cast<int>(value);
+    } else if (k == "col_bulk") {
+        t.col_bulk = value != 0.0 ? 1 : 0;
     } else if (k == "l2_prefetch") {
         t.l2_prefetch = value != 0.0 ? 1 : 0;
     } else if (k == "group_per_sm") {
         const int v = static_cast<int>(value);
         if (v < 0 || v > 4) return fail(EITHOT_EINVAL, "group_per_sm must be 0..4");
         t.group_per_sm = v;
+    } else if (k == "sync_spin_limit") {
+        if (value < 0 || value > static_cast<double>(1 << 26)) return fail(EITHOT_EINVAL, "sync_spin_limit must be 0..2^26");
+        t.sync_spin_limit = static_cast<int>(value);
     } else if (k == "sync_relaxed") {
         t.sync_relaxed = value != 0.0 ? 1 : 0;
     } else if (k == "factor") {
@@ -196,8 +202,10 @@ int eithot_tune_get(const char* key, double* value) {
     else if (k == "factor") *value = t.factor;
     else if (k == "sync_sleep_ns") *value = t.sync_sleep_ns;
     else if (k == "sync_relaxed") *value = t.sync_relaxed;
+    else if (k == "sync_spin_limit") *value = t.sync_spin_limit;
     else if (k == "group_per_sm") *value = t.group_per_sm;
     else if (k == "l2_prefetch") *value = t.l2_prefetch;
+    else if (k == "col_bulk") *value = t.col_bulk;
     else if (k == "batch_graph") *value = t.batch_graph;
     else if (k == "col_chunk") *value = t.col_chunk;
     else if (k == "max_cluster") *value = t.max_cluster;
@@ -276,6 +284,25 @@ int eithot_selftest_wait(unsigned int* timeouts) {
     if (!timeouts) return fail(EITHOT_EINVAL, "null count");
     std::string err;
     if (eithot::run_wait_selftest(timeouts, &err)) return fail(EITHOT_ECUDA, err);
+    return EITHOT_OK;
+}
+
+int eithot_last_call(uint64_t* call_id) {
+    if (!call_id) return fail(EITHOT_EINVAL, "null call_id");
+    if (g_last_call == 0) return fail(EITHOT_EINVAL, "no transpose has been issued on this thread");
+    *call_id = g_last_call;
+    return EITHOT_OK;
+}
+
+int eithot_call_status(uint64_t call_id, void* stream, int* status) {
+    if (!status) return fail(EITHOT_EINVAL, "null status");
+    unsigned bits = 0;
+    std::string err;
+    if (int rc = eithot::read_call_status(call_id, static_cast<cudaStream_t>(stream), &bits, &err))
+        return fail(rc, err);
+    if (bits & eithot::kCallSyncTimeout) *status = EITHOT_ETIMEOUT;
+    else if (bits & eithot::kCallIndexFault) *status = EITHOT_EFAULT;
+    else *status = EITHOT_OK;
     return EITHOT_OK;
 }
 
@@ -426,6 +453,13 @@ int eithot_transpose_ex(void* d_data, size_t capacity_bytes, int rank, const int
         g_stats.free_after_alloc = fb;
     }
     g_stats.workspace_bytes = ctx.scratch_bytes;
+    {
+        std::string err;
+        if ((rc = eithot::begin_call(st, &g_last_call, &ctx.status, &err))) {
+            if (owned) cudaFreeAsync(ctx.scratch, st);
+            return fail(rc, err);
+        }
+    }
     rc = eithot::run_passes(static_cast<uint8_t*>(d_data), passes, ctx);
     g_events_used = ctx.events_used;
     if (owned) cudaFreeAsync(ctx.scratch, st);
@@ -487,6 +521,10 @@ int eithot_transpose_noalloc(void* d_data, size_t capacity_bytes, int rank, cons
     }
     g_stats.algorithmic_bytes = 2.0 * static_cast<double>(plan.volume) * static_cast<double>(elem_size);
     g_stats.workspace_bytes = ctx.scratch_bytes;
+    {
+        std::string err;
+        if ((rc = eithot::begin_call(ctx.stream, &g_last_call, &ctx.status, &err))) return fail(rc, err);
+    }
     rc = eithot::run_passes(static_cast<uint8_t*>(d_data), passes, ctx);
     g_stats.n_passes = ctx.passes;
     g_stats.n_launches = ctx.launches;
@@ -582,10 +620,13 @@ void transpose(void* data, int source, int rank, void* dim, void* permutation, s
             std::fprintf(stderr, "inplace::transpose: %s\n", cudaGetErrorString(e));
             return;
         }
-        unsigned int timeouts = 0;
-        if (eithot_sync_timeouts(&timeouts) == EITHOT_OK && timeouts)
-            std::fprintf(stderr, "inplace::transpose: %u bounded device waits gave up; the output is invalid\n",
-                         timeouts);
+        uint64_t id = 0;
+        int status = EITHOT_OK;
+        if (eithot_last_call(&id) == EITHOT_OK && eithot_call_status(id, nullptr, &status) == EITHOT_OK &&
+            status != EITHOT_OK)
+            std::fprintf(stderr, "inplace::transpose: %s; the output is invalid\n",
+                         status == EITHOT_ETIMEOUT ? "a bounded device wait gave up"
+                                                   : "an index map left its row or column");
     } else {
         std::fprintf(stderr, "inplace::transpose: %s\n", eithot_last_error());
     }

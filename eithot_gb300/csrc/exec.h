@@ -23,9 +23,16 @@ enum Status {
     EITHOT_STATUS_BUSY = 6,
 };
 
+// Per-call device status: a ring of status words in device memory, one per
+// call id (id mod kStatusRing); kernels OR these bits into their call's word.
+constexpr unsigned kStatusRing = 1u << 16;
+constexpr unsigned kCallIndexFault = 1u;   // an index-map result fell outside its row or column
+constexpr unsigned kCallSyncTimeout = 2u;  // a bounded group-barrier wait gave up
+
 struct ExecContext {
     DeviceCaps caps;
     cudaStream_t stream = nullptr;
+    unsigned* status = nullptr;  // this call's device status word (may be null)
     uint8_t* scratch = nullptr;
     size_t scratch_bytes = 0;
     int launches = 0;
@@ -67,6 +74,18 @@ int read_index_faults(unsigned int* out);
 int fill_hash(void* d, int64_t n, size_t elem, uint64_t seed, int64_t first, cudaStream_t s, std::string* err);
 int check_hash(const void* d, int rank, const int64_t* dims, const int* perm1, size_t elem, uint64_t seed,
                cudaStream_t s, uint64_t* mismatches, int64_t* first_bad, std::string* err);
+
+// Starts a call: takes the next call id, points *status at its device status
+// word on the current device and zeroes that word on `stream`.
+int begin_call(cudaStream_t stream, uint64_t* id, unsigned** status, std::string* err);
+
+// The call ids handed out so far (the next id to be issued).
+uint64_t next_call_id();
+
+// Reads call `id`'s status word on `stream` (stream-ordered, then
+// synchronises the stream).  False when the id is unknown or its word has
+// been reused by a later call.
+int read_call_status(uint64_t id, cudaStream_t stream, unsigned* bits, std::string* err);
 
 // Returns and clears the number of bounded group-barrier waits that gave up
 // (their launch aborted its writes); synchronises the device.

@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -38,9 +39,19 @@ constexpr int kThreads = 512;
 // eithot_index_faults().
 __device__ unsigned int g_index_faults = 0;
 
-__device__ __forceinline__ bool in_range(uint64_t v, uint64_t n) {
+// Per-call device status words: call id k owns word k mod kStatusRing.  A
+// call zeroes its word on its stream before its first pass; its kernels OR
+// kCallIndexFault / kCallSyncTimeout into it.
+__device__ unsigned int g_call_status[kStatusRing];
+
+__device__ __forceinline__ void raise_status(unsigned* status, unsigned bit) {
+    if (status) atomicOr(status, bit);
+}
+
+__device__ __forceinline__ bool in_range(uint64_t v, uint64_t n, unsigned* status) {
     if (v < n) return true;
     atomicAdd(&g_index_faults, 1u);
+    raise_status(status, kCallIndexFault);
     return false;
 }
 
@@ -351,6 +362,7 @@ __global__ void __launch_bounds__(kThreads) k_slab_pack(SlabPackArgs a) {
 // ---------------------------------------------------------------------------
 struct RowArgs {
     uint8_t* base;
+    unsigned* status;  // the call's status word
     uint64_t items, E, row_bytes;
     uint32_t rows, cols, P, w, upw, last_upw, nstrips, buf_bytes;
     bool flat;  // w == E: a CTA's pieces are contiguous bytes
@@ -393,7 +405,7 @@ __device__ __forceinline__ void row_stage_in(const RowArgs& a, const Fn& fn, uin
             for (int q = 0; q < kLoadBatch; ++q) {
                 if (!ok[q]) continue;
                 const I dst = fn(i, static_cast<I>(jq[q]));
-                if (!in_range(dst, a.cols)) continue;
+                if (!in_range(dst, a.cols, a.status)) continue;
                 uint32_t owner, off;
                 a.div_P.divmod(static_cast<uint32_t>(dst), owner, off);
                 *reinterpret_cast<U*>(peers[owner] + boff + off * a.w + uq[q] * US) = v[q];
@@ -460,7 +472,7 @@ __global__ void __launch_bounds__(kThreads) k_row_cluster(RowArgs a, Fn fn) {
                     v[q] = *reinterpret_cast<const U*>(smem + boff + jj * a.w + u * US);
                 } else {
                     const I src = fn(i, static_cast<I>(j));
-                    if (!in_range(src, a.cols)) continue;
+                    if (!in_range(src, a.cols, a.status)) continue;
                     uint32_t owner, off;
                     a.div_P.divmod(static_cast<uint32_t>(src), owner, off);
                     v[q] = *reinterpret_cast<const U*>(peers[owner] + boff + off * a.w + u * US);
@@ -484,6 +496,7 @@ __global__ void __launch_bounds__(kThreads) k_row_cluster(RowArgs a, Fn fn) {
 // ---------------------------------------------------------------------------
 struct RowBlockArgs {
     uint8_t* base;
+    unsigned* status;  // the call's status word
     uint64_t total_rows, items, row_bytes, E;
     uint32_t k, cols, upw, units_per_row;
     bool vec16;                // base and row size are 16-byte multiples
@@ -518,7 +531,7 @@ __global__ void __launch_bounds__(kThreads) k_row_block(RowBlockArgs a, Fn fn) {
                 a.div_upw.divmod(jx, j, u);
                 const I i = static_cast<I>(a.div_rows.mod(r0 + rr));
                 const I src = fn(i, static_cast<I>(j));
-                if (!in_range(src, a.cols)) continue;
+                if (!in_range(src, a.cols, a.status)) continue;
                 v[q] = *reinterpret_cast<const U*>(smem + rr * a.row_bytes + static_cast<uint32_t>(src) * a.E + u * US);
                 dst[q] = x;
             }
@@ -574,7 +587,7 @@ __global__ void __launch_bounds__(kThreads) k_row_solo(RowArgs a, Fn fn) {
                 uint32_t j, u;
                 a.div_upw.divmod(x, j, u);
                 const I src = fn(i, static_cast<I>(j));
-                if (!in_range(src, a.cols)) continue;
+                if (!in_range(src, a.cols, a.status)) continue;
                 w[q] = sm[static_cast<uint32_t>(src) * a.upw + u];
                 dst[q] = x;
             }
@@ -595,6 +608,7 @@ __global__ void __launch_bounds__(kThreads) k_row_solo(RowArgs a, Fn fn) {
 // ---------------------------------------------------------------------------
 struct ColArgs {
     uint8_t* base;
+    unsigned* status;  // the call's status word
     uint64_t items, E, row_bytes, mat_bytes;
     uint32_t rows, cols, tw, ntiles, pitch, Q, w, upw, last_upw, nstrips, RU, buf_bytes;  // RU = tw*upw
     bool dbuf;
@@ -693,7 +707,7 @@ __global__ void __launch_bounds__(kThreads) k_col_cluster(ColArgs a, Fn fn) {
                         ok[q] = false;
                         if (iq >= myrows) continue;
                         const I src = fn(static_cast<I>(r0 + iq), col);
-                        if (!in_range(src, a.rows)) continue;
+                        if (!in_range(src, a.rows, a.status)) continue;
                         uint32_t owner, off;
                         a.div_Q.divmod(static_cast<uint32_t>(src), owner, off);
                         v[q] = *reinterpret_cast<const U*>(peers[owner] + off * a.pitch + soff);
@@ -712,7 +726,7 @@ __global__ void __launch_bounds__(kThreads) k_col_cluster(ColArgs a, Fn fn) {
                 a.div_upw.divmod(r, c, u);
                 if (c >= ci.tcols || u >= ci.lim) continue;
                 const I src = fn(static_cast<I>(r0 + ii), static_cast<I>(ci.col0 + c));
-                if (!in_range(src, a.rows)) continue;
+                if (!in_range(src, a.rows, a.status)) continue;
                 uint32_t owner, off;
                 a.div_Q.divmod(static_cast<uint32_t>(src), owner, off);
                 *reinterpret_cast<U*>(ci.mat + static_cast<uint64_t>(r0 + ii) * a.row_bytes + static_cast<uint64_t>(c) * a.E + u * US) =
@@ -735,6 +749,7 @@ __global__ void __launch_bounds__(kThreads) k_col_cluster(ColArgs a, Fn fn) {
 // ---------------------------------------------------------------------------
 struct ColOwnArgs {
     uint8_t* base;
+    unsigned* status;  // the call's status word
     uint64_t items, E, row_bytes, mat_bytes;
     uint32_t rows, cols, tw, ntiles, pitch, Q, Hlo, Hhi, w, upw, last_upw, nstrips, RU, buf_bytes;
     uint32_t hbase;  // (-Hlo) mod m: slot x0 - Hlo is slot (x0 + hbase) mod m, also when Hlo > m
@@ -804,7 +819,7 @@ __device__ __forceinline__ void own_stage_in_tab(const ColOwnArgs& a, const I* s
             uint8_t* dst = buf + lc * a.w + lu * US;
             for (uint32_t ii = ii0; ii < nstage; ii += step) {
                 const I gr = srow[ii];
-                if (!in_range(gr, a.rows)) continue;
+                if (!in_range(gr, a.rows, a.status)) continue;
                 copy_in<US, U>(dst + ii * a.pitch, src + static_cast<uint64_t>(gr) * a.row_bytes);
             }
         }
@@ -816,7 +831,7 @@ __device__ __forceinline__ void own_stage_in_tab(const ColOwnArgs& a, const I* s
             a.div_upw.divmod(r, c, u);
             if (c >= ci.tcols || u >= ci.lim) continue;
             const I gr = srow[ii];
-            if (!in_range(gr, a.rows)) continue;
+            if (!in_range(gr, a.rows, a.status)) continue;
             copy_in<US, U>(buf + ii * a.pitch + c * a.w + u * US,
                            ci.mat + static_cast<uint64_t>(gr) * a.row_bytes + static_cast<uint64_t>(c) * a.E + u * US);
         }
@@ -842,7 +857,7 @@ __device__ __forceinline__ void own_write_rows_tab(const ColOwnArgs& a, const Ow
             for (uint32_t ii = ii0; ii < myrows; ii += step) {
                 const I i = wrow[ii];
                 const int64_t local = own_local(a, ii, d);
-                if (!in_range(i, a.rows) || !in_range(static_cast<uint64_t>(local), nstage)) continue;
+                if (!in_range(i, a.rows, a.status) || !in_range(static_cast<uint64_t>(local), nstage, a.status)) continue;
                 *reinterpret_cast<U*>(dst + static_cast<uint64_t>(i) * a.row_bytes) =
                     *reinterpret_cast<const U*>(src + static_cast<uint32_t>(local) * a.pitch);
             }
@@ -857,7 +872,7 @@ __device__ __forceinline__ void own_write_rows_tab(const ColOwnArgs& a, const Ow
             const int64_t d = own.delta(static_cast<I>(ci.col0 + c)) - own.delta(static_cast<I>(ci.col0));
             const I i = wrow[ii];
             const int64_t local = own_local(a, ii, d);
-            if (!in_range(i, a.rows) || !in_range(static_cast<uint64_t>(local), nstage)) continue;
+            if (!in_range(i, a.rows, a.status) || !in_range(static_cast<uint64_t>(local), nstage, a.status)) continue;
             *reinterpret_cast<U*>(ci.mat + static_cast<uint64_t>(i) * a.row_bytes + static_cast<uint64_t>(c) * a.E + u * US) =
                 *reinterpret_cast<const U*>(buf + static_cast<uint32_t>(local) * a.pitch + c * a.w + u * US);
         }
@@ -922,7 +937,9 @@ __global__ void __launch_bounds__(kThreads) k_col_owner(ColOwnArgs a, Own own) {
 // ---------------------------------------------------------------------------
 struct GroupSync {
     unsigned* counters;  // nG arrival counters, then the abort flag
+    unsigned* status;    // the call's status word (kCallSyncTimeout on a give-up)
     unsigned G, nG;
+    unsigned spin_limit; // polls before a wait gives up
     unsigned sleep_ns;   // back-off between polls
     bool relaxed;        // arrive without release semantics (the arriving CTA's loads have completed)
     bool l2_prefetch;    // single-buffered: prefetch the next item into L2 while waiting
@@ -930,7 +947,6 @@ struct GroupSync {
 
 __device__ unsigned g_sync_timeouts;
 
-constexpr uint32_t kSpinLimit = 1u << 20;  // at least ~0.5 s of polling (each poll is an L2 round trip)
 
 __device__ __forceinline__ void group_arrive(unsigned* ctr, bool relaxed) {
     if (relaxed)
@@ -945,16 +961,20 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
     return v;
 }
 
-// Thread 0 waits until *ctr >= target; false when it gave up or the launch
-// was aborted.  (A fence after relaxed polls would also wait for the CTA's
-// own prefetches in flight; acquire loads do not.)
-__device__ bool group_wait(const unsigned* ctr, unsigned target, unsigned* abort_flag, unsigned sleep_ns) {
-    for (uint32_t it = 0; it < kSpinLimit; ++it) {
+// Thread 0 waits until *ctr >= target, polling at most spin_limit times;
+// false when it gave up or the launch was aborted.  A give-up is counted
+// (g_sync_timeouts) and recorded in the call's status word.  (A fence after
+// relaxed polls would also wait for the CTA's own prefetches in flight;
+// acquire loads do not.)
+__device__ bool group_wait(const unsigned* ctr, unsigned target, unsigned* abort_flag, unsigned sleep_ns,
+                           unsigned spin_limit, unsigned* status) {
+    for (uint32_t it = 0; it < spin_limit; ++it) {
         if (ld_acquire(ctr) >= target) return true;
         if ((it & 31) == 31 && ld_acquire(abort_flag) != 0) return false;
         if (sleep_ns) __nanosleep(sleep_ns);
     }
     atomicAdd(&g_sync_timeouts, 1u);
+    raise_status(status, kCallSyncTimeout);
     atomicExch(abort_flag, 1u);
     return false;
 }
@@ -972,7 +992,7 @@ __device__ __forceinline__ void own_prefetch_l2(const ColOwnArgs& a, const Own& 
     for (uint32_t x = threadIdx.x; x < nstage * lines; x += blockDim.x) {
         const uint32_t ii = x / lines, l = x - ii * lines;
         const I gr = own.stage_of(static_cast<I>(a.div_m.mod(tbase + ii)));
-        if (!in_range(gr, a.rows)) continue;
+        if (!in_range(gr, a.rows, a.status)) continue;
         // an address inside the piece on every line it touches (the last one
         // is the piece's last byte)
         const uint8_t* p = ci.mat + static_cast<uint64_t>(gr) * a.row_bytes + min(l * 128, piece - 1);
@@ -1020,7 +1040,8 @@ __global__ void __launch_bounds__(kThreads) k_col_group(ColOwnArgs a, Own own, G
             own_prefetch_l2(a, own, nxt, x0, nstage);
         const OwnItem ci = own_item(a, it);
         own_fill_write_rows(own, wrow, x0, myrows, ci.col0);  // while thread 0 waits
-        if (threadIdx.x == 0) s_ok = gs.G <= 1 || group_wait(ctr, (k + 1) * gs.G, abort_flag, gs.sleep_ns);
+        if (threadIdx.x == 0)
+            s_ok = gs.G <= 1 || group_wait(ctr, (k + 1) * gs.G, abort_flag, gs.sleep_ns, gs.spin_limit, gs.status);
         __syncthreads();  // every CTA of the group holds its slots: writes may start
         if (!s_ok) break;
         own_write_rows_tab<US, Own, kLanes>(a, own, smem + boff, ci, wrow, myrows, nstage, lc, lu, ii0, step);
@@ -1029,10 +1050,159 @@ __global__ void __launch_bounds__(kThreads) k_col_group(ColOwnArgs a, Own own, G
     if constexpr (US >= 4) asm volatile("cp.async.wait_group 0;\n" ::: "memory");  // no copy outlives the CTA
 }
 
+// ---------------------------------------------------------------------------
+// The group column pass with its slots staged by the bulk-copy engine: one
+// cp.async.bulk per staged row piece (a row piece of a tile is contiguous
+// when elements are whole, w == E), issued by the lanes of warp 0 and
+// completed on an mbarrier per slot buffer.  Two slot buffers: the copies of
+// the group's next item are issued as soon as this CTA has arrived at the
+// group barrier, so they land while the CTA waits for the group and writes
+// the current item; no thread spends registers or issue slots on staging.
+// Preconditions (checked by the launcher): the tile's row pieces are whole
+// elements, 16-byte aligned and multiples of 16 bytes, and so is the pitch.
+// Every mbarrier wait is bounded; a CTA that gives up marks the call's
+// status, raises the abort flag and returns once its copies have landed.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile(
+        "{\n.reg .b64 st;\nmbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(smem_addr(bar))
+        : "memory");
+}
+
+// Waits for phase `parity` of the barrier to complete, at most `limit`
+// probes; false when it gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, uint32_t limit) {
+    const uint32_t a = smem_addr(bar);
+    for (uint32_t i = 0; i < limit; ++i) {
+        uint32_t done = 0;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void bulk_load(void* sdst, const void* gsrc, unsigned bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+            smem_addr(sdst)),
+        "l"(gsrc), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+constexpr uint32_t kMbarWaitLimit = 1u << 22;  // try_wait probes before a slot-buffer wait gives up
+
+// Warp 0 issues the bulk copies of item `it`'s slots into `buf`: slot ii
+// holds the row piece of source row srow[ii].  Each lane announces the bytes
+// of its own copies before issuing them; lane 0 arrives once every lane has.
+template <typename I>
+__device__ __forceinline__ void own_stage_bulk(const ColOwnArgs& a, const I* srow, uint8_t* buf, uint64_t it,
+                                               uint32_t nstage, uint64_t* bar) {
+    const unsigned lane = threadIdx.x & 31;
+    const OwnItem ci = own_item(a, it);
+    const unsigned piece = ci.tcols * a.w;
+    unsigned mine = 0;
+    for (uint32_t ii = lane; ii < nstage; ii += 32)
+        if (srow[ii] < static_cast<I>(a.rows)) mine += piece;
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // earlier generic reads of buf come first
+    if (mine) mbar_expect_tx(bar, mine);
+    for (uint32_t ii = lane; ii < nstage; ii += 32) {
+        const I gr = srow[ii];
+        if (!in_range(gr, a.rows, a.status)) continue;
+        bulk_load(buf + ii * a.pitch, ci.mat + static_cast<uint64_t>(gr) * a.row_bytes, piece, bar);
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(bar);
+}
+
+template <int US, typename Own, bool kLanes>
+__global__ void __launch_bounds__(kThreads) k_col_group_bulk(ColOwnArgs a, Own own, GroupSync gs) {
+    using I = typename Own::index_type;
+    extern __shared__ __align__(128) uint8_t smem[];
+    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ int s_ok;
+    const unsigned grp = blockIdx.x / gs.G, r = blockIdx.x - grp * gs.G;
+    if (grp >= gs.nG) return;  // never launched: the grid is nG * G CTAs
+    unsigned* ctr = gs.counters + grp;
+    unsigned* abort_flag = gs.counters + gs.nG;
+    const uint32_t x0 = r * a.Q;
+    const uint32_t myrows = x0 < a.rows ? min(a.Q, a.rows - x0) : 0;
+    const uint32_t nstage = myrows ? myrows + a.Hlo + a.Hhi : 0;
+    I* srow = reinterpret_cast<I*>(smem + 2 * a.buf_bytes);
+    I* wrow = srow + (a.Q + a.Hlo + a.Hhi);
+    uint32_t lc = 0, lu = 0, ii0 = 0, step = 1;
+    if constexpr (kLanes) {
+        uint32_t lr;
+        a.div_RU.divmod(threadIdx.x, ii0, lr);
+        a.div_upw.divmod(lr, lc, lu);
+        step = blockDim.x / a.RU;
+    }
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    own_fill_stage_rows(a, own, srow, x0, nstage);
+    __syncthreads();  // barriers initialised, source-row table filled
+    const bool warp0 = threadIdx.x < 32;
+    if (warp0 && grp < a.items) own_stage_bulk(a, srow, smem, grp, nstage, &bars[0]);
+    uint32_t k = 0;
+    int inflight = -1;  // buffer whose copies may still be in flight when the loop ends early
+    for (uint64_t it = grp; it < a.items; it += gs.nG, ++k) {
+        const uint32_t b = k & 1;
+        const bool landed = __syncthreads_and(mbar_wait(&bars[b], (k >> 1) & 1, kMbarWaitLimit));
+        if (!landed) {
+            if (threadIdx.x == 0) {
+                raise_status(gs.status, kCallSyncTimeout);
+                atomicExch(abort_flag, 1u);
+            }
+            inflight = static_cast<int>(b);
+            break;
+        }
+        if (threadIdx.x == 0 && gs.G > 1) group_arrive(ctr, gs.relaxed);
+        const uint64_t nxt = it + gs.nG;
+        // the other buffer was last read by the previous item's writes, which
+        // every thread finished before the loop's closing barrier
+        if (nxt < a.items && warp0) own_stage_bulk(a, srow, smem + (b ^ 1) * a.buf_bytes, nxt, nstage, &bars[b ^ 1]);
+        const OwnItem ci = own_item(a, it);
+        own_fill_write_rows(own, wrow, x0, myrows, ci.col0);  // while thread 0 waits
+        if (threadIdx.x == 0)
+            s_ok = gs.G <= 1 || group_wait(ctr, (k + 1) * gs.G, abort_flag, gs.sleep_ns, gs.spin_limit, gs.status);
+        __syncthreads();  // every CTA of the group holds its slots: writes may start
+        if (!s_ok) {
+            if (nxt < a.items) inflight = static_cast<int>(b ^ 1);
+            ++k;  // the in-flight buffer's use is item k + 1
+            break;
+        }
+        own_write_rows_tab<US, Own, kLanes>(a, own, smem + b * a.buf_bytes, ci, wrow, myrows, nstage, lc, lu, ii0,
+                                            step);
+        __syncthreads();  // this CTA's threads are done with the buffer and the output rows
+    }
+    // no copy outlives the CTA: copies issued before an early exit land
+    // before it returns (bounded); item k used buffer k & 1 at phase (k >> 1) & 1
+    if (inflight >= 0) mbar_wait(&bars[inflight], (k >> 1) & 1, kMbarWaitLimit);
+}
+
 // Launch-time self-test of the bounded wait: one CTA waits on a counter
 // that nothing increments and must give up, counting one sync timeout.
 __global__ void k_wait_selftest(unsigned* counters) {
-    if (threadIdx.x == 0) group_wait(counters, 1u, counters + 1, 256);
+    if (threadIdx.x == 0) group_wait(counters, 1u, counters + 1, 256, kDefaultSpinLimit, nullptr);
 }
 
 // ---------------------------------------------------------------------------
@@ -1043,6 +1213,7 @@ __global__ void k_wait_selftest(unsigned* counters) {
 // ---------------------------------------------------------------------------
 struct StageRowArgs {
     uint8_t* base;
+    unsigned* status;  // the call's status word
     uint8_t* scratch;
     uint64_t rows, cols, it0, n;
     StripGeom g;
@@ -1070,12 +1241,12 @@ __global__ void __launch_bounds__(kThreads) k_row_stage(StageRowArgs a, Fn fn) {
         uint8_t* st = a.scratch + gi * item_bytes;
         if (kIn) {
             const uint64_t slot = kScatter ? fn(i, j) : j;
-            if (!in_range(slot, a.cols)) continue;
+            if (!in_range(slot, a.cols, a.status)) continue;
             *reinterpret_cast<U*>(st + slot * a.g.w + u * US) =
                 *reinterpret_cast<const U*>(row + j * a.g.E + u * US);
         } else {
             const uint64_t slot = kScatter ? j : fn(i, j);
-            if (!in_range(slot, a.cols)) continue;
+            if (!in_range(slot, a.cols, a.status)) continue;
             *reinterpret_cast<U*>(row + j * a.g.E + u * US) =
                 *reinterpret_cast<const U*>(st + slot * a.g.w + u * US);
         }
@@ -1084,6 +1255,7 @@ __global__ void __launch_bounds__(kThreads) k_row_stage(StageRowArgs a, Fn fn) {
 
 struct StageColArgs {
     uint8_t* base;
+    unsigned* status;  // the call's status word
     uint8_t* scratch;
     uint64_t rows, cols, tw, ntiles, it0, n;
     StripGeom g;
@@ -1119,7 +1291,7 @@ __global__ void __launch_bounds__(kThreads) k_col_stage(StageColArgs a, Fn fn) {
                 *reinterpret_cast<const U*>(mat + i * row_bytes + c * a.g.E + u * US);
         } else {
             const uint64_t src = fn(i, col0 + c);
-            if (!in_range(src, a.rows)) continue;
+            if (!in_range(src, a.rows, a.status)) continue;
             *reinterpret_cast<U*>(mat + i * row_bytes + c * a.g.E + u * US) =
                 *reinterpret_cast<const U*>(st + src * spitch + c * a.g.w + u * US);
         }
@@ -1447,6 +1619,7 @@ int launch_row(uint8_t* data, const Pass& p, const FnOnChip& fn, const Fn64& fn6
         const uint64_t row_bytes = p.cols * p.elem;
         if (row_bytes * kRowBlockMinRows <= kRowBlockBytes && tuning().row_block) {  // whole rows: any strip
             RowBlockArgs b;
+            b.status = ctx.status;
             b.base = data + p.offset;
             b.total_rows = p.batches * p.rows;
             b.row_bytes = row_bytes;
@@ -1471,6 +1644,7 @@ int launch_row(uint8_t* data, const Pass& p, const FnOnChip& fn, const Fn64& fn6
         }
     }
     RowArgs a;
+    a.status = ctx.status;
     a.base = data + p.offset;
     a.E = p.elem;
     a.row_bytes = p.cols * p.elem;
@@ -1522,6 +1696,7 @@ int launch_row_staged(uint8_t* data, const Pass& p, const Staging& st, ExecConte
     }
     const uint64_t per_group = std::max<uint64_t>(1, ctx.scratch_bytes / item_bytes);
     StageRowArgs a;
+    a.status = ctx.status;
     a.base = data + p.offset;
     a.scratch = ctx.scratch;
     a.rows = p.rows; a.cols = p.cols;
@@ -1554,6 +1729,7 @@ int launch_col_staged(uint8_t* data, const Pass& p, const Staging& st, ExecConte
     }
     const uint64_t per_group = std::max<uint64_t>(1, ctx.scratch_bytes / item_bytes);
     StageColArgs a;
+    a.status = ctx.status;
     a.base = data + p.offset;
     a.scratch = ctx.scratch;
     a.rows = p.rows; a.cols = p.cols; a.tw = st.tw; a.ntiles = ntiles;
@@ -1580,6 +1756,7 @@ int launch_col(uint8_t* data, const Pass& p, const FnOnChip& fn, const Fn64& fn6
     const Staging st = plan_col_staging(p.rows, p.elem, cap, p.cols);
     if (!st.on_chip) return launch_col_staged<US, Fn64>(data, p, st, ctx, fn64);
     ColArgs a;
+    a.status = ctx.status;
     a.base = data + p.offset;
     a.E = p.elem;
     a.row_bytes = p.cols * p.elem;
@@ -1619,8 +1796,9 @@ int launch_col(uint8_t* data, const Pass& p, const FnOnChip& fn, const Fn64& fn6
 // than the group form was planned for (the caller plans again without it).
 constexpr int kRetryWithoutGroups = -2;
 
-ColOwnArgs col_owner_args(uint8_t* data, const Pass& p, const Staging& st, int US) {
+ColOwnArgs col_owner_args(uint8_t* data, const Pass& p, const Staging& st, int US, unsigned* status) {
     ColOwnArgs a;
+    a.status = status;
     a.base = data + p.offset;
     a.E = p.elem;
     a.row_bytes = p.cols * p.elem;
@@ -1664,7 +1842,7 @@ size_t owner_table_bytes(const ColOwnArgs& a) {
 
 template <int US, typename Own>
 int launch_col_owner(uint8_t* data, const Pass& p, const Staging& st, const Own& own, ExecContext& ctx) {
-    const ColOwnArgs a = col_owner_args(data, p, st, US);
+    const ColOwnArgs a = col_owner_args(data, p, st, US, ctx.status);
     const size_t smem = (st.dbuf ? 2 : 1) * static_cast<size_t>(a.buf_bytes) + owner_table_bytes<Own>(a);
     if (kThreads % a.RU != 0)
         EI_CHECK(launch_clusters(k_col_owner<US, Own, false>, st.K, smem, a.items, ctx, a, own));
@@ -1710,9 +1888,76 @@ cudaError_t launch_groups(void (*kernel)(ColOwnArgs, Own, GroupSync), size_t sme
     return cudaLaunchKernelEx(&cfg, kernel, a, own, gs);
 }
 
+// Group-synchronised passes never overlap on the device, whichever streams
+// or threads issue them: each one waits for an event recorded after the
+// previous one on that device.  Two of them in flight at once could each hold
+// part of the SMs while waiting for CTAs of their own that cannot be placed;
+// ordered, each waits only for kernels that finish on their own.  (A stream
+// being captured into a graph is not ordered this way: the batched form,
+// which captures, never uses group passes.)
+std::mutex g_chain_mu;
+std::map<int, cudaEvent_t> g_chain;  // device -> event after its last group pass
+
+class GroupChain {
+public:
+    explicit GroupChain(cudaStream_t stream) : lock_(g_chain_mu), stream_(stream) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(stream, &cs) != cudaSuccess) {
+            cudaGetLastError();
+            cs = cudaStreamCaptureStatusNone;
+        }
+        capturing_ = cs != cudaStreamCaptureStatusNone;
+    }
+    // Makes the stream wait for the previous group pass on this device.
+    cudaError_t before() {
+        if (capturing_) return cudaSuccess;
+        dev_ = current_device();
+        auto it = g_chain.find(dev_);
+        if (it == g_chain.end()) return cudaSuccess;
+        cudaError_t e = cudaStreamWaitEvent(stream_, it->second, 0);
+        if (e == cudaErrorInvalidResourceHandle) {  // the device was reset since: start a new chain
+            cudaGetLastError();
+            g_chain.erase(it);
+            return cudaSuccess;
+        }
+        return e;
+    }
+    // Records the end of this group pass as the next one's predecessor.
+    cudaError_t after() {
+        if (capturing_) return cudaSuccess;
+        auto it = g_chain.find(dev_);
+        if (it == g_chain.end()) {
+            cudaEvent_t ev = nullptr;
+            const cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+            if (e != cudaSuccess) return e;
+            it = g_chain.emplace(dev_, ev).first;
+        }
+        return cudaEventRecord(it->second, stream_);
+    }
+
+private:
+    std::lock_guard<std::mutex> lock_;
+    cudaStream_t stream_;
+    bool capturing_ = false;
+    int dev_ = 0;
+};
+
+// A double-buffered group pass stages its slots with bulk copies when every
+// row piece is whole elements, 16-byte aligned and a multiple of 16 bytes
+// (so is the slot pitch) and the knob allows it.
+template <int US>
+bool bulk_ok(const ColOwnArgs& a, const Staging& st) {
+    if constexpr (US < 4) {
+        return false;
+    } else {
+        return st.dbuf && st.bulk && tuning().col_bulk && a.nstrips == 1 && a.w == a.E && a.pitch % 16 == 0 &&
+               a.row_bytes % 16 == 0 && reinterpret_cast<uintptr_t>(a.base) % 16 == 0;
+    }
+}
+
 template <int US, typename Own>
 int launch_col_group(uint8_t* data, const Pass& p, const Staging& st, const Own& own, ExecContext& ctx) {
-    const ColOwnArgs a = col_owner_args(data, p, st, US);
+    const ColOwnArgs a = col_owner_args(data, p, st, US, ctx.status);
     const size_t smem = (st.dbuf ? 2 : 1) * static_cast<size_t>(a.buf_bytes) + owner_table_bytes<Own>(a);
     if (ctx.scratch == nullptr || ctx.scratch_bytes < kGroupSyncBytes) {
         ctx.err = "workspace too small for a group-synchronised column pass";
@@ -1722,20 +1967,29 @@ int launch_col_group(uint8_t* data, const Pass& p, const Staging& st, const Own&
     gs.counters = reinterpret_cast<unsigned*>(ctx.scratch);
     gs.G = static_cast<unsigned>(st.G);
     gs.nG = 0;
+    gs.status = ctx.status;
+    gs.spin_limit = static_cast<unsigned>(tuning().sync_spin_limit);
     gs.sleep_ns = static_cast<unsigned>(tuning().sync_sleep_ns);
     gs.relaxed = tuning().sync_relaxed != 0;
     gs.l2_prefetch = tuning().l2_prefetch != 0;
     const unsigned max_groups = static_cast<unsigned>(kGroupSyncBytes / sizeof(unsigned)) - 1;
     EI_CHECK(cudaMemsetAsync(ctx.scratch, 0, kGroupSyncBytes, ctx.stream));  // counters and abort flag
-    const cudaError_t e = kThreads % a.RU != 0
-                              ? launch_groups(k_col_group<US, Own, false>, smem, a, own, gs, max_groups, ctx)
-                              : launch_groups(k_col_group<US, Own, true>, smem, a, own, gs, max_groups, ctx);
+    GroupChain chain(ctx.stream);
+    EI_CHECK(chain.before());
+    cudaError_t e;
+    if (bulk_ok<US>(a, st))
+        e = kThreads % a.RU != 0 ? launch_groups(k_col_group_bulk<US, Own, false>, smem, a, own, gs, max_groups, ctx)
+                                 : launch_groups(k_col_group_bulk<US, Own, true>, smem, a, own, gs, max_groups, ctx);
+    else
+        e = kThreads % a.RU != 0 ? launch_groups(k_col_group<US, Own, false>, smem, a, own, gs, max_groups, ctx)
+                                 : launch_groups(k_col_group<US, Own, true>, smem, a, own, gs, max_groups, ctx);
     if (e == cudaErrorCooperativeLaunchTooLarge) {  // fewer CTAs resident than planned: no group form
         cudaGetLastError();
         return kRetryWithoutGroups;
     }
     EI_CHECK(e);
     EI_CHECK(cudaGetLastError());
+    EI_CHECK(chain.after());
     ctx.launches++;
     return 0;
 }
@@ -2083,6 +2337,62 @@ int noalloc_scratch(uint8_t** ptr, std::string* err) {
     }
     cache.emplace_back(dev, static_cast<uint8_t*>(p));
     *ptr = static_cast<uint8_t*>(p);
+    return 0;
+}
+
+namespace {
+std::atomic<uint64_t> g_next_call{1};
+}  // namespace
+
+uint64_t next_call_id() { return g_next_call.load(); }
+
+int begin_call(cudaStream_t stream, uint64_t* id, unsigned** status, std::string* err) {
+    // The device address is looked up on every call (a host-side table
+    // lookup), so it follows the current device and survives a device reset.
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_call_status);
+    if (e != cudaSuccess || p == nullptr) {
+        *err = std::string("cudaGetSymbolAddress(call status): ") + cudaGetErrorString(e);
+        return EITHOT_STATUS_CUDA;
+    }
+    const uint64_t k = g_next_call.fetch_add(1);
+    unsigned* word = static_cast<unsigned*>(p) + (k % kStatusRing);
+    e = cudaMemsetAsync(word, 0, sizeof(unsigned), stream);
+    if (e != cudaSuccess) {
+        *err = std::string("cudaMemsetAsync(call status): ") + cudaGetErrorString(e);
+        return EITHOT_STATUS_CUDA;
+    }
+    *id = k;
+    *status = word;
+    return 0;
+}
+
+int read_call_status(uint64_t id, cudaStream_t stream, unsigned* bits, std::string* err) {
+    const uint64_t next = g_next_call.load();
+    if (id == 0 || id >= next) {
+        *err = "unknown call id";
+        return EITHOT_STATUS_INVALID;
+    }
+    if (next - id > kStatusRing) {
+        *err = "the call's status word has been reused by a later call";
+        return EITHOT_STATUS_INVALID;
+    }
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_call_status);
+    unsigned v = 0;
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&v, static_cast<unsigned*>(p) + (id % kStatusRing), sizeof(v), cudaMemcpyDeviceToHost,
+                            stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) {
+        *err = std::string("reading the call status: ") + cudaGetErrorString(e);
+        return EITHOT_STATUS_CUDA;
+    }
+    if (g_next_call.load() - id > kStatusRing) {  // reused while we read it
+        *err = "the call's status word has been reused by a later call";
+        return EITHOT_STATUS_INVALID;
+    }
+    *bits = v;
     return 0;
 }
 

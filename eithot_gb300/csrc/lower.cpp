@@ -339,6 +339,9 @@ Staging plan_col_owner(uint64_t rows, uint64_t cols, uint64_t batches, uint64_t 
                 const uint64_t sm_share = caps.smem_per_sm / per_sm;
                 if (sm_share < 4096) continue;
                 const uint64_t per_cta_cap = std::min<uint64_t>(cap, sm_share - 3072);
+                // bulk-copy staging: whole elements in 16-byte pieces at a
+                // 16-byte pitch, double-buffered
+                const bool bulk_able = tuning().col_bulk && E <= tb && pitch % 16 == 0 && (cols * E) % 16 == 0;
                 for (bool db : {false, true}) {
                     if (db && !tuning().dbuf) continue;
                     // the slot buffer(s) (128-byte rounded) and the CTA's row
@@ -367,8 +370,12 @@ Staging plan_col_owner(uint64_t rows, uint64_t cols, uint64_t batches, uint64_t 
                     const double residency = per_sm == 1 ? (db ? 0.17 : 0.4)
                                            : per_sm == 2 ? (db ? 0.05 : 0.02)
                                            : per_sm == 3 ? (db ? 0.04 : 0.0) : 0.03;
+                    s.bulk = db && bulk_able;
+                    // bulk-staged CTAs overlap their next item's loads with the
+                    // barrier wait and the writes without spending registers on them
+                    const double bulk_gain = s.bulk ? (per_sm <= 2 ? 0.06 : 0.0) : 0.0;
                     s.cost = 1.0 / (eff * util) + 0.5 * static_cast<double>((lo + hi) * G) / static_cast<double>(rows) +
-                             (G > 1 ? 0.08 : 0.0) + residency;
+                             (G > 1 ? 0.08 : 0.0) + (s.bulk ? residency - 0.05 - bulk_gain : residency);
                     consider(s);
                 }
             }

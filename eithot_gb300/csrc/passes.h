@@ -81,10 +81,12 @@ struct Tuning {
     int slab_cluster = 1;  // matrices beyond one CTA's share: one owner-computed pass over a cluster
     int factor = 1;        // split a transpose along a factor of R or C when a pass would stage globally
     int sync_sleep_ns = 64;  // group barriers: back-off between polls
+    int sync_spin_limit = 1 << 20;  // group barriers: polls before a wait gives up (>= ~0.5 s)
     int sync_relaxed = 1;    // group barriers: arrive without release semantics (every load of the
                              // arriving CTA has landed in shared memory before it arrives)
     int group_per_sm = 0;    // group form: 0 cost model, 1 or 2 CTAs per SM
     int l2_prefetch = 0;     // group form, single-buffered: prefetch the next item into L2 (slower on GB300)
+    int col_bulk = 1;        // group form: double-buffered CTAs staging their slots with bulk copies
     int batch_graph = 1;     // batched form: a run repeating the previous run's buffers replays a CUDA graph
 };
 Tuning& tuning();
@@ -126,6 +128,7 @@ struct Staging {
     bool on_chip = false;  // the item fits the cluster's distributed shared memory
     bool owner = false;    // column pass run owner-computed (each CTA writes from its own rows)
     uint64_t hlo = 0, hhi = 0;  // owner-computed: halo rows staged below / above the owned ones
+    bool bulk = false;     // group form staged by bulk copies (whole-element 16-byte pieces, double-buffered)
     bool group = false;    // owner-computed over a group of G co-resident CTAs (global-memory
     int G = 0;             //   barrier, any size) instead of a thread-block cluster
     int per_sm = 1;        // CTAs per SM the footprint was sized for
@@ -150,6 +153,9 @@ Staging plan_col_pass(const Pass& p, const DeviceCaps& caps);
 // Bytes at the start of the workspace that group-synchronised passes use
 // for their barrier counters.
 constexpr size_t kGroupSyncBytes = 4096;
+
+// Default number of polls before a group-barrier wait gives up.
+constexpr unsigned kDefaultSpinLimit = 1u << 20;
 
 // Lowers every step of `plan` for element size `elem` into passes.
 bool lower_plan(const NdPlan& plan, uint64_t elem, const DeviceCaps& caps,

@@ -34,6 +34,7 @@ extern "C" {
 #define EITHOT_ECUDA         4  /* a CUDA runtime call failed */
 #define EITHOT_EUNSUPPORTED  5  /* valid request outside what this build handles */
 #define EITHOT_EBUSY         6  /* admission refused (served form) */
+#define EITHOT_EFAULT        7  /* a kernel found an index-map result outside its row or column */
 
 /* ---- REORDER_TYPE (ITNT/src/Nd_transpose.cpp:22-28) ------------------- */
 #define EITHOT_ORDER_MIXED   0  /* reference default: fewer non-linearized rounds wins, tie -> post */
@@ -136,6 +137,24 @@ int eithot_transpose_noalloc(void* d_data, size_t capacity_bytes, int rank,
                              size_t elem_size, int num_sub_tensors, double alpha,
                              void* stream);
 
+/* ---- per-call device status --------------------------------------------
+ * No reference counterpart (the reference exits the process on any CUDA
+ * error, ITNT/src/cudacheck.cpp:4-10).  Every eithot_transpose,
+ * eithot_transpose_ex and eithot_transpose_noalloc call that reaches the
+ * device gets a call id and a device status word of its own, zeroed on the
+ * call's stream before its first pass.  A kernel of the call sets it when a
+ * bounded group-barrier wait gives up (the launch then skips its remaining
+ * writes, so the tensor is left partly permuted) or when an index-map
+ * result falls outside its row or column (skipped, never dereferenced).
+ * eithot_last_call returns the id of the calling thread's most recent such
+ * call.  eithot_call_status synchronises `stream` (the call's stream), reads
+ * the word and sets *status to EITHOT_OK, EITHOT_ETIMEOUT or EITHOT_EFAULT;
+ * the output of a call whose status is not EITHOT_OK is invalid.  The words
+ * form a ring of 65536: a call's status can be read until 65536 later calls
+ * have started (then EITHOT_EINVAL). */
+int eithot_last_call(uint64_t* call_id);
+int eithot_call_status(uint64_t call_id, void* stream, int* status);
+
 /* Device scratch bytes eithot_transpose_ex needs for this request. */
 int eithot_workspace_size(int rank, const int64_t* dims, const int* perm_1based,
                           size_t elem_size, int num_sub_tensors, double alpha,
@@ -176,11 +195,18 @@ int eithot_batch_destroy(eithot_batch* batch);
  * No reference counterpart.  A server takes requests for in-place
  * transposes of tensors already resident on the device and runs them on
  * `streams` executor streams (1..16) with scratch from a pool of
- * `workspace_bytes` device bytes that eithot_server_create allocates once
- * (admission: a request whose scratch can never fit the pool is refused
- * with EITHOT_EBUSY; one that does not fit now waits).  Requests run in
- * arrival order; consecutive requests under 64 MB at the head of the queue
- * are run together as one batch (continuous batching), larger ones alone.
+ * `workspace_bytes` device bytes that eithot_server_create allocates once.
+ * Admission: a request's scratch (at most alpha times its bytes, the same
+ * workspace eithot_transpose would take) is charged to the pool; one that
+ * does not fit now waits.  A request whose scratch exceeds the whole pool is
+ * admitted against the device's free HBM instead (cudaMemGetInfo, keeping
+ * 256 MB free): it runs alone with scratch allocated when it starts, and
+ * such requests wait for one another while free HBM cannot hold them all;
+ * it is refused with EITHOT_EBUSY only when free HBM cannot hold it at
+ * submission.  Requests run in arrival order; consecutive requests under
+ * 64 MB at the head of the queue are run together as one batch (continuous
+ * batching; a batch whose lane workspaces exceed the pool is halved until
+ * it fits), larger ones alone.
  * The server has no thread of its own: work is retired and dispatched
  * inside eithot_server_submit and eithot_server_poll, which never block.
  * eithot_server_poll hands back up to max_done tickets of finished
@@ -193,6 +219,14 @@ int eithot_server_submit(eithot_server* server, void* d_data, size_t capacity_by
                          const int64_t* dims, const int* perm_1based, size_t elem_size,
                          int num_sub_tensors, double alpha, uint64_t* ticket);
 int eithot_server_poll(eithot_server* server, uint64_t* done, int max_done, int* n_done);
+/* As eithot_server_poll, also giving each finished ticket's device status
+ * (statuses[i] for done[i]; EITHOT_OK, or EITHOT_ETIMEOUT / EITHOT_EFAULT as
+ * eithot_call_status reports them, whose result is invalid). */
+int eithot_server_poll_status(eithot_server* server, uint64_t* done, int* statuses, int max_done, int* n_done);
+/* Bytes of the tensors of queued and running requests, the pool's size, and
+ * the scratch that running requests admitted beyond the pool hold in HBM. */
+int eithot_server_memory(const eithot_server* server, size_t* resident_bytes, size_t* pool_bytes,
+                         size_t* hbm_scratch_bytes);
 int eithot_server_pending(const eithot_server* server, int* queued, int* running);
 int eithot_server_launches(const eithot_server* server, int* launches);
 int eithot_server_destroy(eithot_server* server);
@@ -254,6 +288,9 @@ int eithot_estimate_report(int rank, const int64_t* dims, const int* perm_1based
  *                 scratch is split along a factor of its rows or columns
  *                 into two on-chip transposes when that is cheaper, 0 not
  *   "sync_sleep_ns" back-off between polls of a group barrier (0..100000)
+ *   "sync_spin_limit" polls of a group barrier before a wait gives up
+ *                 (0..2^26; default 2^20, at least about half a second);
+ *                 a give-up is reported by eithot_call_status
  *   "sync_relaxed" 1 group-barrier arrivals without release semantics
  *                 (default: the arriving CTA's loads have all landed in
  *                 shared memory), 0 release arrivals
@@ -299,10 +336,16 @@ int eithot_profile_get(int i, char* name, size_t name_len, double* ms, double* b
 int eithot_index_faults(unsigned int* count);
 
 /* Column passes whose tiles exceed a thread-block cluster synchronise a
- * group of co-resident CTAs through a barrier in global memory.  Every wait
- * on it is bounded (about half a second); a CTA that gives up aborts the
- * launch's remaining writes and is counted here, and the call's output is
- * then invalid.  Returns and clears the count; synchronises the device. */
+ * group of co-resident CTAs through a barrier in global memory (a
+ * cooperative launch).  Such launches never overlap one another on a device,
+ * whichever streams or threads issue them: each waits for an event recorded
+ * after the previous one (except on a stream that is being captured into a
+ * graph).  Every wait on the barrier is bounded (about half a second by
+ * default, knob "sync_spin_limit"); a CTA that gives up aborts the launch's
+ * remaining writes, marks its call's status EITHOT_ETIMEOUT (see
+ * eithot_call_status) and is counted here.  A nonzero count means that some
+ * call's output is invalid.  Returns and clears the process-wide count;
+ * synchronises the device. */
 int eithot_sync_timeouts(unsigned int* count);
 
 /* Runs one bounded wait that nothing releases (a single 32-thread block

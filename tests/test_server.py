@@ -53,16 +53,20 @@ def test_server_mixed_requests(E):
         assert E.check_hash_ptr(buf.data_ptr() + int(o), d, p, e, 100 + t) == (0, -1), (t, d, p, e)
 
 
-def test_server_refuses_what_the_pool_cannot_hold(E):
+def test_server_refuses_what_neither_pool_nor_free_hbm_can_hold(E):
+    """A request whose scratch exceeds both the pool and the device's free
+    memory is refused at submission (no device work is issued for it)."""
     dev = torch.device("cuda:0")
-    dims, perm = [60000, 300], [2, 1]
-    need = E.workspace_size(dims, perm, 4)
-    assert need > 0
-    buf = torch.zeros(60000 * 300 * 4 + 256, dtype=torch.uint8, device=dev)
-    srv = E.Server(need - 256 if need > 256 else 0, streams=1)
+    dims, perm, alpha = [2097152, 1048576], [2, 1], 0.05  # an 8 TiB int32 matrix, described only
+    need = E.workspace_size(dims, perm, 4, alpha=alpha)
+    free, _ = torch.cuda.mem_get_info(dev)
+    assert need > free
+    buf = torch.zeros(256, dtype=torch.uint8, device=dev)
+    srv = E.Server(1 << 20, streams=1)
     with pytest.raises(E.EithotError) as ei:
-        srv.submit(buf.data_ptr(), buf.numel(), dims, perm, 4)
+        srv.submit(buf.data_ptr(), 4 * math.prod(dims), dims, perm, 4, alpha=alpha)
     assert ei.value.code == E.EBUSY
+    assert srv.pending() == (0, 0)
     srv.close()
 
 
