@@ -13,12 +13,19 @@ whatever they hold, so each step re-transposes the buffer as a fresh
 value: effective GB/s = 2 * bytes / device time per step (inputs resident).
 e2e:   the same metric through the C ABI with the tensor in pinned host
        memory: every step copies it to the device, transposes, and copies
-       the result back; consecutive steps are pipelined over two device
+       the result back; consecutive steps are pipelined over three device
        buffers (copies of one step overlap the transpose of another).
+Beside them: the 3001 x 4096 int32 matrix (perm (2 1)) timed the same way
+(device-resident and end to end), the reference's own CUDA build
+(test_inplace recompiled for sm_103a from baseline/_ref, when built) on both
+configurations, and the reference's own single-threaded host permutation
+next to the oracle's OpenMP restatement of it.
 With N > 1 (torchrun) every rank runs its own replica (the path does not
 shard); value sums the ranks' bytes over the max-over-ranks time.
---impl reference times the reference's CPU path (the oracle's restatement of
-TensorUtil::seq_tt) on the host cores on a bounded slice of the workload.
+--impl reference times the reference's CPU path on the host cores on a
+bounded slice of the workload: its own TensorUtil::seq_tt compiled from the
+reference's sources (single-threaded, as the reference runs it) when that
+build exists, else the oracle's restatement of it.
 """
 from __future__ import annotations
 
@@ -26,6 +33,8 @@ import argparse
 import json
 import math
 import os
+import platform
+import re
 import statistics
 import subprocess
 import sys
@@ -53,6 +62,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the 3001 x 4096 matrix and the reference's own GPU build")
     ap.add_argument("--dims", default=None,
                     help="comma-separated dims overriding the workload (small cases for ncu captures)")
     ap.add_argument("--workload", default="transpose", choices=["transpose", "batched", "served", "study"],
@@ -175,6 +186,119 @@ def cpu_baseline(threads=0, budget_s=10.0):
                       "(1/16 of the workload, 328 MB), median of %d runs" % len(times)}
 
 
+def ref_bin(name):
+    """A binary of the reference's own build (baseline/_ref, built by
+    `make -C oracle ref-gpu` for this machine), or None."""
+    path = os.path.join(ROOT, "baseline", "_ref", "ITNT", "bin-" + platform.machine(), name)
+    return path if os.path.exists(path) else None
+
+
+SLICE = [4, 20011, 512, 2]  # 1/16 of the workload, for the host permutation
+
+
+def ref_seqtt_baseline(runs=1):
+    """The reference's own host permutation TensorUtil::seq_tt (compiled from
+    its sources, single-threaded as the reference runs it) on the workload's
+    1/16 slice, iota data."""
+    exe = ref_bin("ref_seqtt_timer")
+    if not exe:
+        return None
+    r = subprocess.run([exe, str(ELEM), str(runs), "1"] + [str(d) for d in SLICE] + [str(p) for p in PERM],
+                       capture_output=True, text=True, timeout=600)
+    if r.returncode != 0 or not r.stdout.split():
+        return None
+    secs = float(r.stdout.split()[0])
+    n = math.prod(SLICE)
+    return {"value": 2.0 * n * ELEM / secs / 1e9, "unit": "GB/s", "cores": 1, "kind": "reference",
+            "ms_per_run": secs * 1e3,
+            "sample": "the reference's TensorUtil::seq_tt compiled from its sources, single-threaded, out-of-place "
+                      "on dims (4,20011,512,2) int32 (1/16 of the workload, 328 MB), median of %d runs" % runs}
+
+
+REF_CASES = {"4,20011,8192,2 perm 1 3 2 4": ([4, 20011, 8192, 2], [1, 3, 2, 4]),
+             "3001,4096 perm 2 1": ([3001, 4096], [2, 1])}
+
+
+def reference_gpu(timeout=900):
+    """The reference's own CUDA build (its test_inplace, recompiled for
+    sm_103a from its sources) on the bench workload and on the 3001 x 4096
+    int32 matrix: one run each, as the reference's driver runs (iota data,
+    H2D, inplace::transpose, D2H, verify_inplace on the host).  Reports its
+    own two timings: "Execution Time without h2d2h" (device part) and
+    "Execution Time" (with both copies), as effective GB/s."""
+    exe = ref_bin("test_inplace")
+    if not exe:
+        return {"unavailable": "the reference's GPU build is absent (baseline/_ref is made where the "
+                               "reference tree is mounted)"}
+    out = {}
+    for name, (dims, perm) in REF_CASES.items():
+        nb, alpha = 1, 0.01
+        args = [str(d) for d in dims] + [str(p) for p in perm] + [str(ELEM), str(nb), str(alpha)]
+        with tempfile.TemporaryDirectory() as tmp:
+            try:
+                r = subprocess.run([exe] + args, cwd=tmp, capture_output=True, text=True, timeout=timeout)
+            except subprocess.TimeoutExpired:
+                out[name] = {"unavailable": "timed out after %d s" % timeout}
+                continue
+        text = r.stdout
+        dev_ms = re.search(r"Execution Time without h2d2h: ([0-9.]+)ms", text)
+        all_ms = re.search(r"Execution Time: ([0-9.]+)ms", text)
+        if r.returncode != 0 or not dev_ms or not all_ms:
+            out[name] = {"unavailable": "exit %d: %s" % (r.returncode, (r.stdout + r.stderr).strip()[-300:])}
+            continue
+        nbytes = math.prod(dims) * ELEM
+        d, a = float(dev_ms.group(1)), float(all_ms.group(1))
+        out[name] = {"correct": "Correct transpose" in text, "nb": nb, "alpha": alpha,
+                     "device_ms": d, "device_gbs": 2.0 * nbytes / (d / 1e3) / 1e9,
+                     "e2e_ms": a, "e2e_gbs": 2.0 * nbytes / (a / 1e3) / 1e9,
+                     "command": "test_inplace " + " ".join(args)}
+    return out
+
+
+def time_c1(E, dev, steps=50):
+    """The 3001 x 4096 int32 matrix, perm (2 1), nb 1, alpha 0.01: device
+    time per transpose (resident, CUDA events) and end to end through the C
+    ABI (H2D from pinned memory, transpose, D2H, serialised like the
+    reference's driver)."""
+    import torch
+    dims, perm = [3001, 4096], [2, 1]
+    n = math.prod(dims)
+    nbytes = n * ELEM
+    buf = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    E.fill_hash_ptr(buf.data_ptr(), n, ELEM, SEED)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(5):
+        E.transpose_ptr(buf.data_ptr(), nbytes, dims, perm, ELEM, 1, 0.01, E.ORDER_MIXED, stream.cuda_stream)
+    # L2 (129 MB) would hold the 49 MB matrix: flush it between steps with a
+    # 256 MB write and time only the transposes
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    ms = []
+    for _ in range(steps):
+        flush.fill_(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        E.transpose_ptr(buf.data_ptr(), nbytes, dims, perm, ELEM, 1, 0.01, E.ORDER_MIXED, stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms.append(e0.elapsed_time(e1))
+    host = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    host.copy_(buf)
+    e2e = []
+    for _ in range(10):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        buf.copy_(host, non_blocking=True)
+        E.transpose_ptr(buf.data_ptr(), nbytes, dims, perm, ELEM, 1, 0.01, E.ORDER_MIXED, stream.cuda_stream)
+        host.copy_(buf, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        e2e.append(e0.elapsed_time(e1))
+    d, a = statistics.median(ms), statistics.median(e2e)
+    return {"dims": dims, "perm": perm, "elem_bytes": ELEM, "device_ms": d, "device_gbs": 2.0 * nbytes / (d / 1e3) / 1e9,
+            "e2e_ms": a, "e2e_gbs": 2.0 * nbytes / (a / 1e3) / 1e9,
+            "timing": "median of %d flushed device steps and %d serialised H2D+transpose+D2H steps" % (steps, 10)}
+
+
 def max_over_ranks(x: float, device) -> float:
     """The largest of every rank's x (identity without a process group)."""
     import torch
@@ -196,6 +320,30 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
+    exe = ref_bin("ref_seqtt_timer")
+    if exe:
+        # the reference's own host permutation, compiled from its sources:
+        # each step is one single-threaded seq_tt over the slice
+        n = math.prod(SLICE)
+        r = subprocess.run([exe, str(ELEM), str(max(1, args.steps)), str(max(0, args.warmup))] +
+                           [str(d) for d in SLICE] + [str(p) for p in PERM], capture_output=True, text=True,
+                           timeout=1800)
+        if r.returncode == 0 and r.stdout.split():
+            dt = float(r.stdout.split()[0])
+            value = 2.0 * n * ELEM / dt / 1e9
+            sample = ("the reference's TensorUtil::seq_tt compiled from its sources, single-threaded as the "
+                      "reference runs it, out-of-place on dims (4,20011,512,2) int32 (iota)")
+            line = {
+                "impl": "reference", "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "i32", "data": "synthetic (iota, the reference's init_data)",
+                "config": {"workload": WORKLOAD, "sample": "dims (4,20011,512,2), 1/16 of the workload", "dims": DIMS,
+                           "perm": PERM, "elem_bytes": ELEM},
+                "cpu_baseline": {"value": value, "unit": "GB/s", "cores": 1, "kind": "reference", "sample": sample},
+                "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            }
+            print(json.dumps(line), flush=True)
+            return 0
     import numpy as np
     import oracle
 
@@ -380,8 +528,11 @@ def run_eithot(args):
                     "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind if peak_kind == "measured"
                     else "fallback 6.8 TB/s",
                     "passes": {k: {"avg_ms": v["ms"] / v["n"], "gbs": v["bytes"] / (v["ms"] / v["n"] / 1e3) / 1e9}
-                               for k, v in per_pass.items()}}
+                               for k, v in per_pass.items()},
+                    # the whole transpose (every pass) against the same peak
+                    "transpose_frac": value / world / peak}
 
+    c1 = time_c1(E, dev) if (rank == 0 and not args.no_extras) else None
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
@@ -396,8 +547,20 @@ def run_eithot(args):
             "roofline": roofline,
             "clocks": clocks,
         }
+        if c1:
+            line["c1_3001x4096"] = c1
         if not args.no_cpu_baseline:
-            line["cpu_baseline"] = cpu_baseline()
+            port = cpu_baseline()
+            ref = ref_seqtt_baseline()
+            if ref:
+                ref["port_beside"] = port
+                line["cpu_baseline"] = ref
+            else:
+                line["cpu_baseline"] = port
+        if not args.no_extras:
+            del buf
+            torch.cuda.empty_cache()
+            line["reference_gpu"] = reference_gpu()
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist

@@ -20,7 +20,7 @@ _PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_PKG, "_lib", "libeithot.so")
 
 OK, EINVAL, ENOMEM, ETIMEOUT, ECUDA, EUNSUPPORTED, EBUSY, EFAULT = range(8)
-ORDER_MIXED, ORDER_PRE, ORDER_POST = 0, 1, 2
+ORDER_MIXED, ORDER_PRE, ORDER_POST, ORDER_FEWEST = 0, 1, 2, 3
 STEP_ROUND, STEP_PARTITION, STEP_JOIN, STEP_PAD_PRE, STEP_PAD_POST = range(5)
 
 

@@ -29,8 +29,8 @@ CLI_PROGRAMS = {"test_inplace": "test_inplace.cpp", "Nd_estimation": "nd_estimat
 CLI_SCRIPTS = ["Statistic.py"]  # run by the reference's benchmark script beside the programs
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["kernels.cu", "checks.cu"]
-CPP_SOURCES = ["plan.cpp", "lower.cpp", "estimator.cpp", "capi.cpp", "batch.cpp", "server.cpp"]
+CU_SOURCES = ["kernels.cu", "checks.cu", "perm.cu"]
+CPP_SOURCES = ["plan.cpp", "lower.cpp", "search.cpp", "estimator.cpp", "capi.cpp", "batch.cpp", "server.cpp"]
 
 
 def cuda_home() -> str:

@@ -15,6 +15,7 @@
 #include "exec.h"
 #include "passes.h"
 #include "plan.h"
+#include "search.h"
 
 namespace {
 
@@ -76,6 +77,14 @@ int build(int rank, const int64_t* dims, const int* perm, size_t elem, int nb, d
     if (static_cast<double>(plan->padded_volume) * static_cast<double>(elem) > 1.15e18)
         return fail(EITHOT_EINVAL, "tensor too large");
     if (!eithot::lower_plan(*plan, elem, caps, passes, &err)) return fail(EITHOT_EINVAL, err);
+    if (order == EITHOT_ORDER_FEWEST && plan->nb == 1 && !plan->padded) {
+        // the pass-minimising search, kept only for a clear modelled gain
+        std::vector<eithot::Pass> alt;
+        double cost = 0;
+        if (eithot::search_plan(plan->dims, plan->perm, elem, caps, &alt, &cost, nullptr) &&
+            cost < eithot::passes_model_cost(*passes, caps) - 0.2)
+            passes->swap(alt);
+    }
     return EITHOT_OK;
 }
 

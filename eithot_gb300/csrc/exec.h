@@ -54,6 +54,13 @@ struct ExecContext {
 size_t pass_workspace_bytes(const Pass& p, const DeviceCaps& caps);
 size_t pass_workspace_ideal(const Pass& p, const DeviceCaps& caps);
 
+// The planner's slab and block permutations (perm.cu); scratch of a block
+// permutation: its segment table and the saved blocks of its longest cycle
+// (ideal: of every cycle at once).
+int run_slab_perm(uint8_t* data, const Pass& p, ExecContext& ctx);
+int run_block_perm(uint8_t* data, const Pass& p, ExecContext& ctx);
+size_t block_perm_workspace(const Pass& p, bool ideal);
+
 // Launches every pass in order on ctx.stream.  Returns a Status.
 int run_passes(uint8_t* data, const std::vector<Pass>& passes, ExecContext& ctx);
 

@@ -2216,6 +2216,8 @@ uint64_t pass_unit(const uint8_t* data, const Pass& p, const DeviceCaps& caps) {
 size_t pass_workspace_bytes(const Pass& p, const DeviceCaps& caps) {
     const size_t cap = smem_cap_of(caps);
     switch (p.type) {
+        case kBlockPerm:
+            return block_perm_workspace(p, false);
         case kRowGather:
         case kRowScatter: {
             const Staging st = plan_row_staging(p.cols, p.elem, cap, p.type == kRowScatter);
@@ -2242,6 +2244,8 @@ size_t pass_workspace_bytes(const Pass& p, const DeviceCaps& caps) {
 size_t pass_workspace_ideal(const Pass& p, const DeviceCaps& caps) {
     const size_t cap = smem_cap_of(caps);
     switch (p.type) {
+        case kBlockPerm:
+            return block_perm_workspace(p, true);
         case kRowGather:
         case kRowScatter: {
             const Staging st = plan_row_staging(p.cols, p.elem, cap, p.type == kRowScatter);
@@ -2281,14 +2285,20 @@ int run_passes(uint8_t* data, const std::vector<Pass>& passes, ExecContext& ctx)
         if (int rc = record()) return rc;
     }
     for (const Pass& p : passes) {
-        const uint64_t U = pass_unit(data, p, ctx.caps);
         int rc;
-        switch (U) {
-            case 16: rc = run_pass_u<16>(data, p, ctx); break;
-            case 8: rc = run_pass_u<8>(data, p, ctx); break;
-            case 4: rc = run_pass_u<4>(data, p, ctx); break;
-            case 2: rc = run_pass_u<2>(data, p, ctx); break;
-            default: rc = run_pass_u<1>(data, p, ctx); break;
+        if (p.type == kSlabPerm) {
+            rc = run_slab_perm(data, p, ctx);
+        } else if (p.type == kBlockPerm) {
+            rc = run_block_perm(data, p, ctx);
+        } else {
+            const uint64_t U = pass_unit(data, p, ctx.caps);
+            switch (U) {
+                case 16: rc = run_pass_u<16>(data, p, ctx); break;
+                case 8: rc = run_pass_u<8>(data, p, ctx); break;
+                case 4: rc = run_pass_u<4>(data, p, ctx); break;
+                case 2: rc = run_pass_u<2>(data, p, ctx); break;
+                default: rc = run_pass_u<1>(data, p, ctx); break;
+            }
         }
         if (rc) return rc;
         ctx.passes++;

@@ -517,6 +517,18 @@ void lower_xpose(const Xpose& x, const DeviceCaps& caps, std::vector<Pass>* pass
     passes->insert(passes->end(), chosen.begin(), chosen.end());
 }
 
+double passes_cost_of(const std::vector<Pass>& ps, const DeviceCaps& caps) {
+    bool staged = false;
+    return passes_cost(ps, caps, &staged);
+}
+
+double xpose_cost(const Xpose& x, const DeviceCaps& caps) {
+    std::vector<Pass> ps;
+    lower_xpose(x, caps, &ps);
+    bool staged = false;
+    return passes_cost(ps, caps, &staged);
+}
+
 namespace {
 void lower_xpose_direct(const Xpose& x, const DeviceCaps& caps, std::vector<Pass>* passes) {
     if (x.B == 0 || x.R <= 1 || x.C <= 1) return;  // identity

@@ -24,6 +24,8 @@ enum PassType {
     kColGather = 3,      // out[i][j] = in[g(i,j)][j]
     kBlockMove = 4,      // n_blocks blocks of `block` bytes: s*src_pitch -> s*dst_pitch
     kSlabCluster = 5,    // each of B matrices (R x C) transposed by a K-CTA cluster, owner-computed
+    kSlabPerm = 6,       // each of B slabs (axes nd_dims, elements of `elem` bytes) permuted on chip by nd_perm
+    kBlockPerm = 7,      // blocks of `block` bytes, indexed by axes nd_dims, permuted by nd_perm along its cycles
 };
 
 enum FnType {
@@ -46,6 +48,10 @@ struct Pass {
     int cluster = 1;                     // kSlabCluster: CTAs per matrix
     // block moves
     uint64_t block = 0, n_blocks = 0, src_pitch = 0, dst_pitch = 0;
+    // slab and block permutations: the permuted axes (fastest first) and the
+    // output order (output axis j is input axis nd_perm[j])
+    std::vector<uint64_t> nd_dims;
+    std::vector<int> nd_perm;
     std::string what;
 };
 
@@ -86,7 +92,7 @@ struct Tuning {
                              // arriving CTA has landed in shared memory before it arrives)
     int group_per_sm = 0;    // group form: 0 cost model, 1 or 2 CTAs per SM
     int l2_prefetch = 0;     // group form, single-buffered: prefetch the next item into L2 (slower on GB300)
-    int col_bulk = 1;        // group form: double-buffered CTAs staging their slots with bulk copies
+    int col_bulk = 0;        // group form: double-buffered CTAs staging their slots with bulk copies (slower on GB300)
     int batch_graph = 1;     // batched form: a run repeating the previous run's buffers replays a CUDA graph
 };
 Tuning& tuning();
@@ -163,6 +169,13 @@ bool lower_plan(const NdPlan& plan, uint64_t elem, const DeviceCaps& caps,
 
 // Lowers one batched transpose (exposed for tests).
 void lower_xpose(const Xpose& x, const DeviceCaps& caps, std::vector<Pass>* passes);
+
+// Modelled time of the passes lower_xpose emits for x, in streaming passes.
+double xpose_cost(const Xpose& x, const DeviceCaps& caps);
+
+// Modelled time of a list of slab, row and column passes (the lowering's
+// own cost model), in streaming passes.
+double passes_cost_of(const std::vector<Pass>& passes, const DeviceCaps& caps);
 
 // Maps one low-order op acting on `n_sub` back-to-back sub-tensors onto a
 // batched transpose.

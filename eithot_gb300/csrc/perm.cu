@@ -1,0 +1,399 @@
+// sm_103a kernels of the pass-minimising planner's single-pass moves
+// (search.cpp): the slab permutation (leading axes of every slab permuted on
+// chip) and the block permutation (blocks of leading axes moved along the
+// permutation's cycles).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "exec.h"
+#include "index_math.cuh"
+#include "passes.h"
+#include "search.h"
+
+namespace eithot {
+
+namespace {
+
+constexpr int kMaxAxes = 8;
+
+template <int S> struct UnitT;
+template <> struct UnitT<1> { using T = uint8_t; };
+template <> struct UnitT<2> { using T = uint16_t; };
+template <> struct UnitT<4> { using T = uint32_t; };
+template <> struct UnitT<8> { using T = uint2; };
+template <> struct UnitT<16> { using T = uint4; };
+
+template <int US>
+__device__ __forceinline__ void stage_unit(uint8_t* sdst, const uint8_t* gsrc) {
+    using U = typename UnitT<US>::T;
+    if constexpr (US >= 4) {
+        const uint32_t sa = static_cast<uint32_t>(__cvta_generic_to_shared(sdst));
+        if constexpr (US == 16)
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gsrc) : "memory");
+        else
+            asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(sa), "l"(gsrc), "n"(US) : "memory");
+    } else {
+        *reinterpret_cast<U*>(sdst) = *reinterpret_cast<const U*>(gsrc);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Slab permutation: B slabs of `count` elements (E bytes each; an element is
+// moved in strips of w bytes when it is wider than 128 B), each staged whole
+// in one CTA's shared memory and written back in the output order of its q
+// axes.  Output element o (row-major in the output's axis order, fastest
+// first) holds input element sum_j c_j(o) * istr[j], c_j(o) the coordinate of
+// output axis j.  kPack > 1: whole 1- or 2-byte elements, kPack consecutive
+// outputs packed into one 4-byte store.
+// ---------------------------------------------------------------------------
+struct SlabPermArgs {
+    uint8_t* base;
+    uint64_t items, slab_bytes;
+    uint32_t count, E, w, upw, last_upw, nstrips, q;
+    FastDiv div_strips;
+    FastDiv32 div_upw;
+    FastDiv32 od[kMaxAxes];   // output dims, output order
+    uint32_t istr[kMaxAxes];  // input stride (elements) of output axis j
+};
+
+__device__ __forceinline__ uint32_t slab_src(const SlabPermArgs& a, uint32_t o) {
+    uint32_t idx = 0;
+#pragma unroll
+    for (int j = 0; j < kMaxAxes; ++j) {
+        if (j >= static_cast<int>(a.q)) break;
+        uint32_t qt, c;
+        a.od[j].divmod(o, qt, c);
+        idx += c * a.istr[j];
+        o = qt;
+    }
+    return idx;
+}
+
+template <int US, int kPack>
+__global__ void __launch_bounds__(512) k_slab_perm(SlabPermArgs a) {
+    using U = typename UnitT<US>::T;
+    extern __shared__ __align__(16) uint8_t smem[];
+    for (uint64_t it = blockIdx.x; it < a.items; it += gridDim.x) {
+        uint64_t b, s;
+        a.div_strips.divmod(it, b, s);
+        const uint32_t lim = (s + 1 == a.nstrips) ? a.last_upw : a.upw;
+        uint8_t* slab = a.base + b * a.slab_bytes + s * a.w;
+        const uint32_t units = a.count * a.upw;
+        if (a.w == a.E) {  // whole elements: the slab is contiguous
+            for (uint32_t x = threadIdx.x; x < units; x += blockDim.x)
+                stage_unit<US>(smem + x * US, slab + static_cast<uint64_t>(x) * US);
+        } else {
+            for (uint32_t x = threadIdx.x; x < units; x += blockDim.x) {
+                uint32_t e, u;
+                a.div_upw.divmod(x, e, u);
+                if (u >= lim) continue;
+                stage_unit<US>(smem + e * a.w + u * US, slab + static_cast<uint64_t>(e) * a.E + u * US);
+            }
+        }
+        if constexpr (US >= 4) asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+        __syncthreads();
+        if constexpr (kPack > 1) {
+            const uint32_t groups = a.count / kPack;
+            for (uint32_t g = threadIdx.x; g < groups; g += blockDim.x) {
+                const uint32_t o0 = g * kPack;
+                uint32_t word = 0;
+#pragma unroll
+                for (int k = 0; k < kPack; ++k)
+                    word |= static_cast<uint32_t>(*reinterpret_cast<const U*>(smem + slab_src(a, o0 + k) * US))
+                            << (8 * US * k);
+                *reinterpret_cast<uint32_t*>(slab + static_cast<uint64_t>(o0) * US) = word;
+            }
+            for (uint32_t o = groups * kPack + threadIdx.x; o < a.count; o += blockDim.x)
+                *reinterpret_cast<U*>(slab + static_cast<uint64_t>(o) * US) =
+                    *reinterpret_cast<const U*>(smem + slab_src(a, o) * US);
+        } else {
+            for (uint32_t x = threadIdx.x; x < units; x += blockDim.x) {
+                uint32_t o, u;
+                a.div_upw.divmod(x, o, u);
+                if (u >= lim) continue;
+                const uint32_t src = slab_src(a, o);
+                *reinterpret_cast<U*>(slab + static_cast<uint64_t>(o) * a.E + u * US) =
+                    *reinterpret_cast<const U*>(smem + src * a.w + u * US);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Block permutation along cycles.  Blocks of `blk` bytes are indexed by q
+// axes; the block at output index t comes from input index src(t).  The
+// cycles are cut into segments (host table): a first launch copies the block
+// at every segment's head to scratch; a second walks every segment backwards
+// from its tail: position t <- block at src(t), then t = src(t), the last step
+// taking the head's saved copy.  Every position is written once and read
+// before it is written, by the same thread for the same bytes (each thread
+// owns fixed byte lanes of every block), so no barrier is needed.  Segments
+// are processed in chunks of whole cycles (a cycle's segments depend only on
+// one another).
+// ---------------------------------------------------------------------------
+struct CycleArgs {
+    uint8_t* base;
+    uint8_t* saved;
+    const uint64_t* head;
+    const uint64_t* tail;
+    const uint64_t* len;
+    uint64_t seg0, nseg, blk, units;
+    uint32_t q;
+    FastDiv div_units;
+    FastDiv od[kMaxAxes];     // output dims, output order
+    uint64_t istr[kMaxAxes];  // input stride (blocks) of output axis j
+};
+
+__device__ __forceinline__ uint64_t cycle_src(const CycleArgs& a, uint64_t t) {
+    uint64_t idx = 0;
+#pragma unroll
+    for (int j = 0; j < kMaxAxes; ++j) {
+        if (j >= static_cast<int>(a.q)) break;
+        uint64_t qt, c;
+        a.od[j].divmod(t, qt, c);
+        idx += c * a.istr[j];
+        t = qt;
+    }
+    return idx;
+}
+
+template <int US>
+__global__ void __launch_bounds__(512) k_cycle_save(CycleArgs a) {
+    using U = typename UnitT<US>::T;
+    const uint64_t total = a.nseg * a.units;
+    for (uint64_t x = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; x < total;
+         x += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        uint64_t i, u;
+        a.div_units.divmod(x, i, u);
+        *reinterpret_cast<U*>(a.saved + i * a.blk + u * US) =
+            *reinterpret_cast<const U*>(a.base + a.head[a.seg0 + i] * a.blk + u * US);
+    }
+}
+
+constexpr int kFollowThreads = 256;
+constexpr int kFollowBatch = 4;  // units in flight per thread
+
+template <int US>
+__global__ void __launch_bounds__(kFollowThreads) k_cycle_follow(CycleArgs a) {
+    using U = typename UnitT<US>::T;
+    for (uint64_t sg = blockIdx.x; sg < a.nseg; sg += gridDim.x) {
+        uint64_t t = a.tail[a.seg0 + sg];
+        const uint64_t n = a.len[a.seg0 + sg];
+        for (uint64_t step = 0; step < n; ++step) {
+            const uint64_t p = cycle_src(a, t);
+            const uint8_t* from = (step + 1 == n) ? a.saved + sg * a.blk : a.base + p * a.blk;
+            uint8_t* to = a.base + t * a.blk;
+            for (uint64_t x0 = threadIdx.x; x0 < a.units; x0 += kFollowBatch * kFollowThreads) {
+                U v[kFollowBatch];
+#pragma unroll
+                for (int k = 0; k < kFollowBatch; ++k) {
+                    const uint64_t x = x0 + k * kFollowThreads;
+                    if (x < a.units) v[k] = *reinterpret_cast<const U*>(from + x * US);
+                }
+#pragma unroll
+                for (int k = 0; k < kFollowBatch; ++k) {
+                    const uint64_t x = x0 + k * kFollowThreads;
+                    if (x < a.units) *reinterpret_cast<U*>(to + x * US) = v[k];
+                }
+            }
+            t = p;
+        }
+    }
+}
+
+uint64_t pow2_unit(std::initializer_list<uint64_t> vals) {
+    uint64_t u = 16;
+    for (uint64_t v : vals)
+        while (u > 1 && v % u != 0) u /= 2;
+    return u;
+}
+
+#define PM_CHECK(expr)                                                    \
+    do {                                                                  \
+        cudaError_t e__ = (expr);                                         \
+        if (e__ != cudaSuccess) {                                         \
+            ctx.err = std::string(#expr) + ": " + cudaGetErrorString(e__); \
+            return EITHOT_STATUS_CUDA;                                    \
+        }                                                                 \
+    } while (0)
+
+int device_sms(const ExecContext& ctx) { return std::max(1, ctx.caps.sms); }
+
+template <int US, int kPack>
+int launch_slab_perm(const SlabPermArgs& a, size_t smem, ExecContext& ctx) {
+    auto kern = k_slab_perm<US, kPack>;
+    PM_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    int per_sm = 0;
+    PM_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 512, smem));
+    const uint64_t cap = static_cast<uint64_t>(std::max(per_sm, 1)) * device_sms(ctx);
+    const unsigned grid = static_cast<unsigned>(std::max<uint64_t>(1, std::min<uint64_t>(a.items, cap)));
+    kern<<<grid, 512, smem, ctx.stream>>>(a);
+    PM_CHECK(cudaGetLastError());
+    ctx.launches++;
+    return 0;
+}
+
+template <int US>
+int launch_cycles(const CycleArgs& a, ExecContext& ctx) {
+    const uint64_t total = a.nseg * a.units;
+    const unsigned g1 = static_cast<unsigned>(std::max<uint64_t>(
+        1, std::min<uint64_t>((total + 511) / 512, static_cast<uint64_t>(device_sms(ctx)) * 4)));
+    k_cycle_save<US><<<g1, 512, 0, ctx.stream>>>(a);
+    PM_CHECK(cudaGetLastError());
+    const unsigned g2 = static_cast<unsigned>(
+        std::max<uint64_t>(1, std::min<uint64_t>(a.nseg, static_cast<uint64_t>(device_sms(ctx)) * 8)));
+    k_cycle_follow<US><<<g2, kFollowThreads, 0, ctx.stream>>>(a);
+    PM_CHECK(cudaGetLastError());
+    ctx.launches += 2;
+    return 0;
+}
+
+// Output dims in output order and the input stride of each output axis.
+void out_geometry(const Pass& p, std::vector<uint64_t>* od, std::vector<uint64_t>* istr) {
+    const int q = static_cast<int>(p.nd_dims.size());
+    std::vector<uint64_t> in_stride(q);
+    uint64_t st = 1;
+    for (int i = 0; i < q; ++i) {
+        in_stride[i] = st;
+        st *= p.nd_dims[i];
+    }
+    od->resize(q);
+    istr->resize(q);
+    for (int j = 0; j < q; ++j) {
+        (*od)[j] = p.nd_dims[p.nd_perm[j]];
+        (*istr)[j] = in_stride[p.nd_perm[j]];
+    }
+}
+
+uint64_t table_bytes(uint64_t nseg) { return (3 * nseg * sizeof(uint64_t) + 255) / 256 * 256; }
+
+}  // namespace
+
+int run_slab_perm(uint8_t* data, const Pass& p, ExecContext& ctx) {
+    const int q = static_cast<int>(p.nd_dims.size());
+    if (q < 1 || q > kMaxAxes || static_cast<int>(p.nd_perm.size()) != q) {
+        ctx.err = "internal: slab permutation of more than 8 axes";
+        return EITHOT_STATUS_INVALID;
+    }
+    uint64_t count = 1;
+    for (auto d : p.nd_dims) count *= d;
+    const uint64_t w = p.strip ? p.strip : p.elem;
+    const size_t smem = count * w;
+    if (smem > smem_cap_of(ctx.caps) || count >= (uint64_t(1) << 31)) {
+        ctx.err = "internal: slab permutation beyond one CTA's shared memory";
+        return EITHOT_STATUS_INVALID;
+    }
+    SlabPermArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.base = data + p.offset;
+    a.slab_bytes = count * p.elem;
+    a.count = static_cast<uint32_t>(count);
+    a.E = static_cast<uint32_t>(p.elem);
+    a.w = static_cast<uint32_t>(w);
+    a.nstrips = static_cast<uint32_t>((p.elem + w - 1) / w);
+    a.items = p.batches * a.nstrips;
+    a.q = static_cast<uint32_t>(q);
+    a.div_strips = FastDiv::make(a.nstrips, a.items);
+    std::vector<uint64_t> od, istr;
+    out_geometry(p, &od, &istr);
+    for (int j = 0; j < q; ++j) {
+        a.od[j] = FastDiv32::make(od[j]);
+        a.istr[j] = static_cast<uint32_t>(istr[j]);
+    }
+    const uint64_t addr = reinterpret_cast<uintptr_t>(a.base);
+    const uint64_t last = p.elem - (a.nstrips - 1) * w;
+    const uint64_t US = pow2_unit({addr, p.elem, w, last, a.slab_bytes});
+    a.upw = static_cast<uint32_t>(w / US);
+    a.last_upw = static_cast<uint32_t>(last / US);
+    a.div_upw = FastDiv32::make(a.upw);
+    const bool whole = a.nstrips == 1;
+    switch (US) {
+        case 16: return launch_slab_perm<16, 1>(a, smem, ctx);
+        case 8: return launch_slab_perm<8, 1>(a, smem, ctx);
+        case 4: return launch_slab_perm<4, 1>(a, smem, ctx);
+        case 2:
+            if (whole && p.elem == 2 && addr % 4 == 0 && a.slab_bytes % 4 == 0) return launch_slab_perm<2, 2>(a, smem, ctx);
+            return launch_slab_perm<2, 1>(a, smem, ctx);
+        default:
+            if (whole && p.elem == 1 && addr % 4 == 0 && a.slab_bytes % 4 == 0) return launch_slab_perm<1, 4>(a, smem, ctx);
+            return launch_slab_perm<1, 1>(a, smem, ctx);
+    }
+}
+
+size_t block_perm_workspace(const Pass& p, bool ideal) {
+    const CycleTable& tab = cycle_table(p.nd_dims, p.nd_perm);
+    const uint64_t nseg = tab.head.size();
+    if (nseg == 0) return 0;
+    return table_bytes(nseg) + (ideal ? nseg : tab.max_cycle_segments) * p.block;
+}
+
+int run_block_perm(uint8_t* data, const Pass& p, ExecContext& ctx) {
+    const int q = static_cast<int>(p.nd_dims.size());
+    if (q < 1 || q > kMaxAxes || static_cast<int>(p.nd_perm.size()) != q) {
+        ctx.err = "internal: block permutation of more than 8 axes";
+        return EITHOT_STATUS_INVALID;
+    }
+    const CycleTable& tab = cycle_table(p.nd_dims, p.nd_perm);
+    const uint64_t nseg = tab.head.size();
+    if (nseg == 0) return 0;  // every block stays
+    const uint64_t tb = table_bytes(nseg);
+    if (ctx.scratch == nullptr || ctx.scratch_bytes < tb + tab.max_cycle_segments * p.block) {
+        ctx.err = "workspace too small for the block permutation's segment table and saved blocks";
+        return EITHOT_STATUS_NOMEM;
+    }
+    uint64_t* dev_tab = reinterpret_cast<uint64_t*>(ctx.scratch);
+    PM_CHECK(cudaMemcpyAsync(dev_tab, tab.head.data(), nseg * sizeof(uint64_t), cudaMemcpyHostToDevice, ctx.stream));
+    PM_CHECK(cudaMemcpyAsync(dev_tab + nseg, tab.tail.data(), nseg * sizeof(uint64_t), cudaMemcpyHostToDevice,
+                             ctx.stream));
+    PM_CHECK(cudaMemcpyAsync(dev_tab + 2 * nseg, tab.len.data(), nseg * sizeof(uint64_t), cudaMemcpyHostToDevice,
+                             ctx.stream));
+    CycleArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.base = data + p.offset;
+    a.saved = ctx.scratch + tb;
+    a.head = dev_tab;
+    a.tail = dev_tab + nseg;
+    a.len = dev_tab + 2 * nseg;
+    a.blk = p.block;
+    a.q = static_cast<uint32_t>(q);
+    std::vector<uint64_t> od, istr;
+    out_geometry(p, &od, &istr);
+    uint64_t nblocks = 1;
+    for (auto d : p.nd_dims) nblocks *= d;
+    for (int j = 0; j < q; ++j) {
+        a.od[j] = FastDiv::make(od[j], nblocks);
+        a.istr[j] = istr[j];
+    }
+    const uint64_t US = pow2_unit({reinterpret_cast<uintptr_t>(a.base), reinterpret_cast<uintptr_t>(a.saved), p.block});
+    a.units = p.block / US;
+    const uint64_t cap_seg = (ctx.scratch_bytes - tb) / p.block;  // saved blocks per chunk
+    // chunks of whole cycles
+    size_t c = 0;
+    const size_t ncyc = tab.cycle_first.size() - 1;
+    while (c < ncyc) {
+        const uint64_t s0 = tab.cycle_first[c];
+        size_t c1 = c + 1;
+        while (c1 < ncyc && tab.cycle_first[c1 + 1] - s0 <= cap_seg) ++c1;
+        a.seg0 = s0;
+        a.nseg = tab.cycle_first[c1] - s0;
+        a.div_units = FastDiv::make(a.units, a.nseg * a.units);
+        int rc = 0;
+        switch (US) {
+            case 16: rc = launch_cycles<16>(a, ctx); break;
+            case 8: rc = launch_cycles<8>(a, ctx); break;
+            case 4: rc = launch_cycles<4>(a, ctx); break;
+            case 2: rc = launch_cycles<2>(a, ctx); break;
+            default: rc = launch_cycles<1>(a, ctx); break;
+        }
+        if (rc) return rc;
+        c = c1;
+    }
+    return 0;
+}
+
+}  // namespace eithot

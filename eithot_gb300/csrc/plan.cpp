@@ -172,7 +172,8 @@ bool make_nd_plan(int rank, const int64_t* dims_in, const int* perm_1based,
                   int nb, double alpha, int order, NdPlan* plan, std::string* err) {
     if (rank < 1 || rank > 32) { *err = "rank must be in [1, 32]"; return false; }
     if (!dims_in || !perm_1based) { *err = "null dims or permutation"; return false; }
-    if (order < kOrderMixed || order > kOrderPost) { *err = "reorder_type must be 0, 1 or 2"; return false; }
+    if (order < kOrderMixed || order > kOrderFewest) { *err = "reorder_type must be 0, 1, 2 or 3"; return false; }
+    if (order == kOrderFewest) order = kOrderMixed;  // the plan's own steps follow the reference's series
     if (!(alpha > 0.0) || !std::isfinite(alpha)) { *err = "alpha must be a positive finite ratio"; return false; }
     if (nb < 1) { *err = "num_sub_tensors must be >= 1"; return false; }
     std::vector<int64_t> dims(dims_in, dims_in + rank);

@@ -9,7 +9,9 @@
 
 namespace eithot {
 
-enum Order { kOrderMixed = 0, kOrderPre = 1, kOrderPost = 2 };
+// kOrderFewest: the reference's mixed series for the plan's steps, and the
+// executor may replace its passes with a pass-minimising search's.
+enum Order { kOrderMixed = 0, kOrderPre = 1, kOrderPost = 2, kOrderFewest = 3 };
 
 // A low-order transpose: rank 2..4 tensor, 1-based permutation.
 struct LowOp {

@@ -40,6 +40,13 @@ extern "C" {
 #define EITHOT_ORDER_MIXED   0  /* reference default: fewer non-linearized rounds wins, tie -> post */
 #define EITHOT_ORDER_PRE     1
 #define EITHOT_ORDER_POST    2
+/* No reference counterpart: the plan with the fewest modelled device passes,
+ * searched over batched 2D transposes, on-chip slab permutations and
+ * cycle-following block permutations (the reference's unwired 4D/5D
+ * single-pass linearisations, generalised); the reference's mixed series
+ * when the search finds nothing clearly cheaper, and always for tensors
+ * split into sub-tensors. */
+#define EITHOT_ORDER_FEWEST  3
 
 /* ---- step roles in a plan --------------------------------------------- */
 #define EITHOT_STEP_ROUND     0  /* one low-order transpose of the series */
@@ -295,6 +302,11 @@ int eithot_estimate_report(int rank, const int64_t* dims, const int* perm_1based
  *                 (default: the arriving CTA's loads have all landed in
  *                 shared memory), 0 release arrivals
  *   "group_per_sm" group form: 0 cost model, 1..4 resident CTAs per SM
+ *   "col_bulk"    1 group passes may run double-buffered with their row pieces
+ *                 staged by bulk copies (cp.async.bulk, mbarrier completion)
+ *                 when every piece is whole 16-byte-aligned elements, 0 not
+ *                 (default; measured slower than three single-buffered CTAs
+ *                 per SM on GB300)
  *   "l2_prefetch" 1 single-buffered group passes prefetch the next item into
  *                 L2 while they wait at the barrier, 0 not (default; slower)
  *   "batch_graph" 1 a batch run on the same buffers and workspace as the

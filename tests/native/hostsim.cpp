@@ -12,6 +12,7 @@
 #include "fn_build.h"
 #include "passes.h"
 #include "plan.h"
+#include "search.h"
 
 using namespace eithot;
 
@@ -32,10 +33,59 @@ void col_gather(uint8_t* base, const Pass& p, const Fn& fn) {
     }
 }
 
+// Input index (in the pass's axes) of output index o: output axis j is
+// input axis perm[j].
+uint64_t nd_src(const std::vector<uint64_t>& dims, const std::vector<int>& perm, uint64_t o) {
+    const size_t q = dims.size();
+    std::vector<uint64_t> in_stride(q);
+    uint64_t st = 1;
+    for (size_t i = 0; i < q; ++i) {
+        in_stride[i] = st;
+        st *= dims[i];
+    }
+    uint64_t idx = 0;
+    for (size_t j = 0; j < q; ++j) {
+        const uint64_t d = dims[perm[j]];
+        idx += (o % d) * in_stride[perm[j]];
+        o /= d;
+    }
+    return idx;
+}
+
 void apply(uint8_t* data, const Pass& p) {
     uint8_t* base = data + p.offset;
     const uint64_t E = p.elem;
     switch (p.type) {
+        case kSlabPerm: {
+            uint64_t count = 1;
+            for (auto d : p.nd_dims) count *= d;
+            std::vector<uint8_t> tmp(count * E);
+            for (uint64_t b = 0; b < p.batches; ++b) {
+                uint8_t* m = base + b * count * E;
+                std::memcpy(tmp.data(), m, count * E);
+                for (uint64_t o = 0; o < count; ++o)
+                    std::memcpy(m + o * E, &tmp[nd_src(p.nd_dims, p.nd_perm, o) * E], E);
+            }
+            break;
+        }
+        case kBlockPerm: {
+            // the device algorithm, in place: save every segment's head,
+            // then walk every segment backwards from its tail
+            const CycleTable& tab = cycle_table(p.nd_dims, p.nd_perm);
+            const uint64_t blk = p.block, nseg = tab.head.size();
+            std::vector<uint8_t> saved(nseg * blk);
+            for (uint64_t k = 0; k < nseg; ++k) std::memcpy(&saved[k * blk], base + tab.head[k] * blk, blk);
+            for (uint64_t k = 0; k < nseg; ++k) {
+                uint64_t t = tab.tail[k];
+                for (uint64_t step = 0; step < tab.len[k]; ++step) {
+                    const uint64_t src = nd_src(p.nd_dims, p.nd_perm, t);
+                    const uint8_t* from = step + 1 == tab.len[k] ? &saved[k * blk] : base + src * blk;
+                    std::memmove(base + t * blk, from, blk);
+                    t = src;
+                }
+            }
+            break;
+        }
         case kSlabCluster:
         case kSlabTranspose: {
             const uint64_t R = p.rows, C = p.cols;
@@ -85,6 +135,23 @@ void apply(uint8_t* data, const Pass& p) {
     }
 }
 
+// The pass list the C ABI executes for this plan: the lowered reference
+// series, replaced by the pass-minimising search's when the request asks for
+// the fewest passes and the search finds a clearly cheaper plan (as
+// eithot_transpose_ex decides it).
+bool lower_plan_as_executed(const NdPlan& plan, size_t elem, int order, const DeviceCaps& caps,
+                            std::vector<Pass>* passes) {
+    if (!lower_plan(plan, elem, caps, passes, &g_err)) return false;
+    if (order == kOrderFewest && plan.nb == 1 && !plan.padded) {
+        std::vector<Pass> alt;
+        double cost = 0;
+        if (search_plan(plan.dims, plan.perm, elem, caps, &alt, &cost, nullptr) &&
+            cost < passes_model_cost(*passes, caps) - 0.2)
+            passes->swap(alt);
+    }
+    return true;
+}
+
 }  // namespace
 
 extern "C" {
@@ -102,7 +169,7 @@ int hs_transpose(void* data, size_t capacity, int rank, const int64_t* dims, con
     }
     std::vector<Pass> passes;
     DeviceCaps caps;
-    if (!lower_plan(plan, elem, caps, &passes, &g_err)) return -1;
+    if (!lower_plan_as_executed(plan, elem, order, caps, &passes)) return -1;
     for (const Pass& p : passes) apply(static_cast<uint8_t*>(data), p);
     return static_cast<int>(passes.size());
 }
@@ -114,7 +181,7 @@ int hs_describe(char* buf, size_t len, int rank, const int64_t* dims, const int*
     if (!make_nd_plan(rank, dims, perm, nb, alpha, order, &plan, &g_err)) return -1;
     std::vector<Pass> passes;
     DeviceCaps caps;
-    if (!lower_plan(plan, elem, caps, &passes, &g_err)) return -1;
+    if (!lower_plan_as_executed(plan, elem, order, caps, &passes)) return -1;
     std::string s;
     for (const Pass& p : passes) s += p.what + "\n";
     std::strncpy(buf, s.c_str(), len);
@@ -130,7 +197,7 @@ int hs_describe_staging(char* buf, size_t len, int rank, const int64_t* dims, co
     if (!make_nd_plan(rank, dims, perm, nb, alpha, order, &plan, &g_err)) return -1;
     std::vector<Pass> passes;
     DeviceCaps caps;
-    if (!lower_plan(plan, elem, caps, &passes, &g_err)) return -1;
+    if (!lower_plan_as_executed(plan, elem, order, caps, &passes)) return -1;
     std::string s;
     for (const Pass& p : passes) {
         s += p.what;

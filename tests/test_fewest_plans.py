@@ -1,0 +1,111 @@
+"""Parity of the pass-minimising plans (reorder type EITHOT_ORDER_FEWEST)
+with the oracle, through the C ABI on device memory: the searched series
+of batched 2D transposes, on-chip slab permutations (the reference's row
+linearisations _3214 / _43215, generalised) and cycle-following block
+permutations (its column linearisations _1432 / _14325 / _15432,
+generalised).  Bit-exact against the oracle's out-of-place permutation."""
+import itertools
+import math
+import random
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+FEWEST = 3
+
+
+def run_case(E, dims, perm, elem, alpha=0.01, seed=1, workspace=None, expect=None):
+    """expect: a pass kind ("cycle-perm", "slab-perm") the plan must use."""
+    n = math.prod(dims)
+    host = oracle.fill_hash(n, elem, seed)
+    buf = torch.from_numpy(host.copy()).cuda()
+    s = torch.cuda.current_stream()
+    wptr, wbytes = 0, 0
+    if workspace is not None:
+        ws = torch.empty(max(workspace, 256), dtype=torch.uint8, device="cuda")
+        wptr, wbytes = ws.data_ptr(), workspace
+    if expect:
+        E.set_profiling(True)
+        E.profile_reset()
+    try:
+        E.transpose_ptr(buf.data_ptr(), buf.numel(), dims, perm, elem, 1, alpha, FEWEST, s.cuda_stream, wptr, wbytes)
+    finally:
+        E.set_profiling(False)
+    cid = E.last_call()
+    assert E.call_status(cid, s.cuda_stream) == E.OK
+    if expect:
+        names = [p["name"] for p in E.profile()]
+        E.profile_reset()
+        assert any(nm.startswith(expect) for nm in names), names
+    got = buf.cpu().numpy()
+    want = oracle.permute(host, dims, perm, elem)
+    if not np.array_equal(got, want):
+        bad = np.nonzero(got != want)[0]
+        raise AssertionError("mismatch %s perm %s elem %d: %d bad bytes, first at %d" % (dims, perm, elem, bad.size, bad[0]))
+    return E.last_stats()
+
+
+@pytest.mark.parametrize("rank", [3, 4, 5])
+def test_every_permutation(E, rank):
+    rng = random.Random(7 + rank)
+    for perm in itertools.permutations(range(1, rank + 1)):
+        for elem in (1, 2, 4, 8):
+            dims = [rng.choice([2, 3, 5, 16, 33, 64, 96, 130]) for _ in range(rank)]
+            while math.prod(dims) * elem > (2 << 20):
+                dims[dims.index(max(dims))] //= 2
+            run_case(E, dims, list(perm), elem)
+
+
+@pytest.mark.parametrize("dims,perm,elem,expect", [
+    ([16, 301, 1024, 64, 4], [5, 3, 1, 4, 2], 2, "cycle-perm"),  # the 100 GB configuration's plan, 1/50 scale
+    ([64, 50, 60, 70], [1, 4, 3, 2], 4, "cycle-perm"),        # 15 KB blocks
+    ([1024, 7, 9, 11], [1, 4, 3, 2], 8, "cycle-perm"),        # 8 KB blocks, three permuted axes
+    ([4096, 3, 300, 200], [1, 4, 3, 2], 2, "cycle-perm"),     # 8 KB blocks of 2-byte elements
+    ([16, 31, 64, 8, 4], [5, 3, 1, 4, 2], 2, "slab-perm"),    # a four-axis slab permutation
+    ([20, 30, 40, 50, 6], [5, 4, 3, 2, 1], 2, None),
+    ([8, 7, 6, 5, 4, 3], [6, 4, 2, 1, 3, 5], 4, None),
+    ([2, 3, 5, 7, 11, 13, 2], [7, 1, 6, 2, 5, 3, 4], 1, None),
+    ([4096, 33, 65], [1, 3, 2], 1, None), ([3001, 4096], [2, 1], 4, None), ([4, 2001, 819, 2], [1, 3, 2, 4], 4, None)])
+def test_named_shapes(E, dims, perm, elem, expect):
+    run_case(E, dims, perm, elem, expect=expect)
+
+
+def test_cycle_permutation_in_chunks(E):
+    """A block permutation whose workspace (alpha 0.01) holds only a few
+    cycles' saved blocks at once: the segments run in several chunks of
+    whole cycles (two launches each)."""
+    dims, perm, elem = [1024, 7, 9, 11], [1, 4, 3, 2], 8
+    need = E.workspace_size(dims, perm, elem, 1, 0.01, FEWEST)
+    assert need < 0.02 * math.prod(dims) * elem
+    st = run_case(E, dims, perm, elem, workspace=need, expect="cycle-perm")
+    assert st["n_launches"] >= 4
+
+
+def test_16x3001x1024x256x4_uint16_fewest_passes(E):
+    """(16, 3001, 1024, 256, 4) uint16 (100.7 GB), perm (5 3 1 4 2), alpha
+    0.05, planned for the fewest passes: four passes (a Catanzaro transpose
+    of 1024 x 3001 matrices of 32-byte elements, a cycle-following
+    permutation of 32 KB blocks, a slab permutation of 128 KB slabs) where
+    the reference's series takes six.  Every output element is checked on
+    the device against the counter hash of its source index."""
+    dims, perm, elem, seed = [16, 3001, 1024, 256, 4], [5, 3, 1, 4, 2], 2, 0xC3
+    n = math.prod(dims)
+    cap = n * elem
+    free, _ = torch.cuda.mem_get_info()
+    if free < cap * 1.08:
+        pytest.skip("needs %.0f GB of free device memory" % (cap * 1.08 / 1e9))
+    buf = torch.empty(cap, dtype=torch.uint8, device="cuda")
+    E.fill_hash_ptr(buf.data_ptr(), n, elem, seed)
+    s = torch.cuda.current_stream()
+    E.transpose_ptr(buf.data_ptr(), cap, dims, perm, elem, 1, 0.05, FEWEST, s.cuda_stream)
+    cid = E.last_call()
+    assert E.call_status(cid, s.cuda_stream) == E.OK
+    st = E.last_stats()
+    assert st["n_passes"] <= 4
+    assert st["workspace_bytes"] <= 0.05 * n * elem
+    assert E.check_hash_ptr(buf.data_ptr(), dims, perm, elem, seed) == (0, -1)

@@ -87,7 +87,7 @@ def test_catanzaro_2d(E, R, C, elem):
 @pytest.fixture
 def tuned(E):
     keys = ("variant", "col_owner", "col_chunk", "max_cluster", "dbuf", "col_form", "row_prefetch", "row_block",
-            "slab_pack", "slab_cluster", "factor", "sync_relaxed", "group_per_sm")
+            "slab_pack", "slab_cluster", "factor", "sync_relaxed", "group_per_sm", "col_bulk")
     saved = {k: E.tune_get(k) for k in keys}
 
     def set_(**kw):
@@ -139,6 +139,21 @@ def test_group_arrivals_and_residency(E, tuned, relaxed, per_sm):
         run_case(E, [4096, 3001], [2, 1], 4)
         run_case(E, [4, 20011, 819, 2], [1, 3, 2, 4], 4)
         run_case(E, [6000, 4000], [2, 1], 1)
+        run_case(E, [2048, 1536], [2, 1], 32)
+        run_case(E, [999, 5003], [2, 1], 3)
+
+
+@pytest.mark.parametrize("per_sm", [1, 2])
+def test_group_pass_with_bulk_copies(E, tuned, per_sm):
+    """Double-buffered group column passes whose row pieces are staged by
+    bulk copies completing on mbarriers (whole 16-byte-aligned elements),
+    c2r and r2c, 16-, 4- and 32-byte elements; shapes whose pieces do not
+    qualify fall back to the cp.async form."""
+    tuned(col_form=2, dbuf=1, col_bulk=1, group_per_sm=per_sm)
+    for variant in (1, 2):
+        E.tune_set("variant", variant)
+        run_case(E, [4, 20011, 819, 2], [1, 3, 2, 4], 4)
+        run_case(E, [4096, 3001], [2, 1], 4)
         run_case(E, [2048, 1536], [2, 1], 32)
         run_case(E, [999, 5003], [2, 1], 3)
 

@@ -167,3 +167,27 @@ def test_owner_passes_fit_their_shared_memory(hostsim, form, per_sm, dbuf):
         hostsim.hs_tune(b"group_per_sm", 0)
         hostsim.hs_tune(b"dbuf", 1)
     assert owners > 0
+
+
+@pytest.mark.parametrize("rank", [3, 4, 5])
+def test_fewest_pass_plans_all_permutations(hostsim, rank):
+    """The pass-minimising search (order 3): every permutation of ranks 3-5
+    on shapes whose leading blocks reach the cycle-following and slab moves;
+    the block permutation is simulated with the device's segment algorithm
+    (heads saved, segments walked backwards)."""
+    rng = random.Random(100 + rank)
+    for perm in itertools.permutations(range(1, rank + 1)):
+        for elem in (1, 2, 4, 8):
+            dims = [rng.choice([2, 3, 5, 16, 33, 64, 96, 130]) for _ in range(rank)]
+            while math.prod(dims) * elem > (3 << 20):
+                dims[dims.index(max(dims))] //= 2
+            assert run(hostsim, dims, list(perm), elem, order=3), (dims, perm, elem)
+
+
+@pytest.mark.parametrize("dims,perm,elem", [
+    ([16, 31, 64, 8, 4], [5, 3, 1, 4, 2], 2), ([64, 50, 60, 70], [1, 4, 3, 2], 4), ([20, 30, 40, 50, 6], [5, 4, 3, 2, 1], 2),
+    ([8, 7, 6, 5, 4, 3], [6, 4, 2, 1, 3, 5], 4), ([512, 9, 11, 13], [1, 4, 2, 3], 8), ([2, 3, 5, 7, 11, 13, 2], [7, 1, 6, 2, 5, 3, 4], 1)])
+def test_fewest_pass_plans_named_shapes(hostsim, dims, perm, elem):
+    """Shapes whose searched plans use cycle-following block permutations
+    (4-32 KB blocks), slab permutations of 2-6 axes and factor splits."""
+    assert run(hostsim, dims, perm, elem, order=3)
