@@ -621,21 +621,29 @@ def run_batched(args):
         torch.cuda.synchronize(dev)
         return time.perf_counter() - t0
 
-    def plain():
+    def plain(order=E.ORDER_MIXED):
         for (d, p, e), q, c in zip(ts, ptrs, caps):
-            E.transpose_ptr(q, c, d, p, e, 1, 0.01, E.ORDER_MIXED, st.cuda_stream)
+            E.transpose_ptr(q, c, d, p, e, 1, 0.01, order, st.cuda_stream)
+
+    def plain_fewest():
+        plain(E.ORDER_FEWEST)
 
     def batched():
         batch.run(ptrs, caps, ws.data_ptr(), batch.workspace_size, st.cuda_stream)
 
     plain()
+    plain_fewest()
     batched()  # a repeat of the checked run's buffers: captured into a CUDA graph here, replayed below
     t_plain = statistics.median(timed(plain) for _ in range(max(3, args.steps // 4)))
+    t_plain_fewest = statistics.median(timed(plain_fewest) for _ in range(max(3, args.steps // 4)))
     t_batch = statistics.median(timed(batched) for _ in range(max(3, args.steps // 4)))
     total = sum(sizes)
     line = {"metric": "batched in-place GB/s (2*bytes/s), %d mixed tensors" % len(ts), "value": 2 * total / t_batch / 1e9,
             "unit": "GB/s", "higher_is_better": True, "n_gpus": 1, "ms_per_batch": t_batch * 1e3,
-            "one_at_a_time": {"value": 2 * total / t_plain / 1e9, "ms": t_plain * 1e3},
+            "one_at_a_time": {"value": 2 * total / t_plain / 1e9, "ms": t_plain * 1e3,
+                              "plan": "the reference's series (EITHOT_ORDER_MIXED, eithot_transpose's default)"},
+            "one_at_a_time_fewest": {"value": 2 * total / t_plain_fewest / 1e9, "ms": t_plain_fewest * 1e3,
+                                     "plan": "fewest modelled passes (EITHOT_ORDER_FEWEST), as the batch plans"},
             "speedup_vs_one_at_a_time": t_plain / t_batch, "launches_per_batch": batch.launches,
             "data": "synthetic (seeded counter hash per tensor, checked on the device after the first run)",
             "config": {"workload": "4096 tensors, rank U{3..6}, bytes log-uniform [4 KB, 64 MB], elem U{1,2,4,8}, "

@@ -1,6 +1,8 @@
 // The batched form: many independent in-place transposes planned once and
 // run together.  Each tensor's passes stay in order on one of up to 16
-// internal streams ("lanes"); tensors are spread over the lanes
+// internal streams ("lanes"); every tensor is planned for the fewest
+// modelled passes (without cycle-following moves, whose segment tables are
+// copied from the host); tensors are spread over the lanes
 // largest-first onto the least-loaded lane, so the small passes of
 // different tensors overlap on the GPU instead of queueing behind one
 // another.  Column passes use thread-block clusters only (no
@@ -30,6 +32,7 @@ using namespace eithot::api;
 
 struct eithot_batch {
     int device = -1;
+    int order = EITHOT_ORDER_FEWEST;  // plans with the fewest modelled passes
     DeviceCaps caps;
     Tuning tuning;
     struct Item {
@@ -172,7 +175,8 @@ int eithot_batch_create(int count, const int* ranks, const int64_t* dims, const 
         cudaGetLastError();
     }
     b->tuning = tuning();
-    b->tuning.col_form = 1;  // clusters only: no pass relies on grid-wide residency
+    b->tuning.col_form = 1;     // clusters only: no pass relies on grid-wide residency
+    b->tuning.cycle_moves = 0;  // every pass can be captured in a graph (no host-to-device table copies)
     b->items.resize(count);
     size_t off = 0;
     for (int t = 0; t < count; ++t) {
@@ -182,11 +186,13 @@ int eithot_batch_create(int count, const int* ranks, const int64_t* dims, const 
         if (ranks[t] >= 1 &&
             shape_tuning(std::vector<int64_t>(dims + off, dims + off + ranks[t]),
                          std::vector<int>(perms_1based + off, perms_1based + off + ranks[t]), elem_sizes[t],
-                         &it.tuning))
+                         &it.tuning)) {
             it.tuning.col_form = 1;  // a shape's knobs, still without group passes
+            it.tuning.cycle_moves = 0;
+        }
         ScopedTuning scope(it.tuning);
         const int rc = build(ranks[t], dims + off, perms_1based + off, elem_sizes[t], num_sub_tensors, alpha,
-                             EITHOT_ORDER_MIXED, b->caps, &plan, &it.passes);
+                             b->order, b->caps, &plan, &it.passes);
         if (rc) {
             delete b;
             return fail(rc, "tensor " + std::to_string(t) + ": " + eithot_last_error());

@@ -121,6 +121,16 @@ int apply_knob(eithot::Tuning& t, const char* key, double value) {
     } else if (k == "sync_sleep_ns") {
         if (value < 0 || value > 100000) return fail(EITHOT_EINVAL, "sync_sleep_ns must be 0..100000");
         t.sync_sleep_ns = static_cast<int>(value);
+    } else if (k == "cycle_moves") {
+        t.cycle_moves = value != 0.0 ? 1 : 0;
+    } else if (k == "slab_perm") {
+        const int v = static_cast<int>(value);
+        if (v < 0 || v > 2) return fail(EITHOT_EINVAL, "slab_perm must be 0, 1 or 2");
+        t.slab_perm = v;
+    } else if (k == "slab_runs") {
+        t.slab_runs = value != 0.0 ? 1 : 0;
+    } else if (k == "slab_prefetch") {
+        t.slab_prefetch = value != 0.0 ? 1 : 0;
     } else if (k == "col_bulk") {
         t.col_bulk = value != 0.0 ? 1 : 0;
     } else if (k == "l2_prefetch") {
@@ -215,6 +225,10 @@ int eithot_tune_get(const char* key, double* value) {
     else if (k == "group_per_sm") *value = t.group_per_sm;
     else if (k == "l2_prefetch") *value = t.l2_prefetch;
     else if (k == "col_bulk") *value = t.col_bulk;
+    else if (k == "cycle_moves") *value = t.cycle_moves;
+    else if (k == "slab_perm") *value = t.slab_perm;
+    else if (k == "slab_runs") *value = t.slab_runs;
+    else if (k == "slab_prefetch") *value = t.slab_prefetch;
     else if (k == "batch_graph") *value = t.batch_graph;
     else if (k == "col_chunk") *value = t.col_chunk;
     else if (k == "max_cluster") *value = t.max_cluster;
@@ -483,9 +497,10 @@ int eithot_transpose_ex(void* d_data, size_t capacity_bytes, int rank, const int
 // device memory during the call: their device memory is owned by another
 // allocator (a framework's caching pool that has reserved the free HBM, so an
 // extra allocation would fail or fragment it), or the call sits on a path
-// that must not pay for an allocation.  The first call on each device looks
-// up the array's device address (cudaGetSymbolAddress); make that first call
-// before any stream capture.  All calls share the array and it keeps the
+// that must not pay for an allocation.  Every call looks up the array's
+// device address on the current device (cudaGetSymbolAddress, no
+// allocation); make the first call on a device before any stream capture.
+// All calls share the array and it keeps the
 // last call's contents; nothing in it needs to start at zero.  Calls whose
 // device work overlaps (other streams, other host threads) race on it.
 int eithot_transpose_noalloc(void* d_data, size_t capacity_bytes, int rank, const int64_t* dims,

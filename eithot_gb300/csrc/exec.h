@@ -69,8 +69,8 @@ bool query_caps(int device, DeviceCaps* caps, std::string* err);
 // Size of the fixed device scratch behind eithot_transpose_noalloc.
 constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;
 
-// Device address of that scratch on the current device (looked up on the
-// first call per device).
+// Device address of that scratch on the current device (looked up on every
+// call: no allocation, and valid after a device reset).
 int noalloc_scratch(uint8_t** ptr, std::string* err);
 
 // Count of index-map results that fell outside their row/column since the

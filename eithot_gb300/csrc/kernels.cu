@@ -2323,29 +2323,15 @@ static __device__ __align__(256) uint8_t g_noalloc_scratch[kNoAllocScratchBytes]
 
 int noalloc_scratch(uint8_t** ptr, std::string* err) {
     // In host code g_noalloc_scratch names a host-side stand-in; its device
-    // address is looked up once per device, with that device current.
-    static std::mutex mu;
-    static std::vector<std::pair<int, uint8_t*>> cache;
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) {
-        *err = std::string("cudaGetDevice: ") + cudaGetErrorString(e);
-        return EITHOT_STATUS_CUDA;
-    }
-    std::lock_guard<std::mutex> lock(mu);
-    for (auto& c : cache) {
-        if (c.first == dev) {
-            *ptr = c.second;
-            return 0;
-        }
-    }
+    // address is looked up on every call (a host-side table lookup, no
+    // allocation), with the caller's device current, so it follows the
+    // current device and context, also after a device reset.
     void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || p == nullptr) {
         *err = std::string("cudaGetSymbolAddress(fixed scratch): ") + cudaGetErrorString(e);
         return EITHOT_STATUS_CUDA;
     }
-    cache.emplace_back(dev, static_cast<uint8_t*>(p));
     *ptr = static_cast<uint8_t*>(p);
     return 0;
 }

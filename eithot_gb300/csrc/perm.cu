@@ -125,6 +125,165 @@ __global__ void __launch_bounds__(512) k_slab_perm(SlabPermArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// Slab permutation of narrow whole elements (E <= 16 bytes): every thread
+// writes runs of K = V / E consecutive outputs as one V-byte store.  The slab
+// is staged row by row (a row = the input's fastest axis) at a padded pitch
+// (an odd number of max(4, E)-byte granules) so that the strided gathers of
+// a warp spread over the banks; a thread finds the first element of its run
+// with one divide per axis and steps to the next ones by adding the axes'
+// strides in shared memory, carrying from axis to axis.
+// ---------------------------------------------------------------------------
+struct SlabRunArgs {
+    uint8_t* base;
+    uint64_t batches, slab_bytes;
+    uint32_t count, q, nrows, row_bytes, pitch, su;
+    bool chunks16;            // slab base, slab size and row size are 16-byte multiples
+    FastDiv32 div_upr;        // staging: unit index -> (row, unit of the row)
+    FastDiv32 od[kMaxAxes];   // output dims, output order
+    uint32_t odim[kMaxAxes];
+    uint32_t step[kMaxAxes];  // shared-memory bytes per step of output axis j
+};
+
+template <int E> struct ElemT;
+template <> struct ElemT<1> { using T = uint8_t; };
+template <> struct ElemT<2> { using T = uint16_t; };
+template <> struct ElemT<4> { using T = uint32_t; };
+template <> struct ElemT<8> { using T = uint2; };
+template <> struct ElemT<16> { using T = uint4; };
+
+template <int SU>
+__device__ __forceinline__ void stage_rows(const SlabRunArgs& a, uint8_t* smem, const uint8_t* slab) {
+    const uint32_t upr = a.row_bytes / SU;
+    const uint32_t total = a.nrows * upr;
+    for (uint32_t x = threadIdx.x; x < total; x += blockDim.x) {
+        uint32_t r, u;
+        a.div_upr.divmod(x, r, u);
+        stage_unit<SU>(smem + r * a.pitch + u * SU, slab + static_cast<uint64_t>(r) * a.row_bytes + u * SU);
+    }
+    if constexpr (SU >= 4) asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
+__device__ __forceinline__ uint32_t run_start(const SlabRunArgs& a, uint32_t o, uint32_t* c) {
+    uint32_t addr = 0;
+#pragma unroll
+    for (int j = 0; j < kMaxAxes; ++j) {
+        c[j] = 0;
+        if (j < static_cast<int>(a.q)) {
+            uint32_t qt;
+            a.od[j].divmod(o, qt, c[j]);
+            addr += c[j] * a.step[j];
+            o = qt;
+        }
+    }
+    return addr;
+}
+
+// Writes the staged slab back in output order: runs of K outputs per thread.
+template <int E, int V>
+__device__ __forceinline__ void write_runs(const SlabRunArgs& a, const uint8_t* sm, uint8_t* slab) {
+    using T = typename ElemT<E>::T;
+    constexpr int K = V / E;
+    const uint32_t runs = a.count / K;
+    for (uint32_t g = threadIdx.x; g < runs; g += blockDim.x) {
+        uint32_t c[kMaxAxes];
+        uint32_t addr = run_start(a, g * K, c);
+        T v[K];
+#pragma unroll
+        for (int t = 0; t < K; ++t) {
+            v[t] = *reinterpret_cast<const T*>(sm + addr);
+            if (t + 1 < K) {  // next output: axis 0 steps, carrying into the next axes
+                bool carry = true;
+#pragma unroll
+                for (int j = 0; j < kMaxAxes; ++j) {
+                    if (carry && j < static_cast<int>(a.q)) {
+                        addr += a.step[j];
+                        if (++c[j] == a.odim[j]) {
+                            c[j] = 0;
+                            addr -= a.odim[j] * a.step[j];
+                        } else {
+                            carry = false;
+                        }
+                    }
+                }
+            }
+        }
+        uint8_t* dst = slab + static_cast<uint64_t>(g) * V;
+        if constexpr (E >= 4) {
+#pragma unroll
+            for (int t = 0; t < K; ++t) reinterpret_cast<T*>(dst)[t] = v[t];
+        } else {
+            constexpr int W = V / 4;
+            uint32_t w[W];
+#pragma unroll
+            for (int i = 0; i < W; ++i) w[i] = 0;
+#pragma unroll
+            for (int t = 0; t < K; ++t) w[t * E / 4] |= static_cast<uint32_t>(v[t]) << (8 * ((t * E) % 4));
+            if constexpr (V == 16) *reinterpret_cast<uint4*>(dst) = make_uint4(w[0], w[1], w[2], w[3]);
+            else if constexpr (V == 8) *reinterpret_cast<uint2*>(dst) = make_uint2(w[0], w[1]);
+            else *reinterpret_cast<uint32_t*>(dst) = w[0];
+        }
+    }
+    for (uint32_t o = runs * K + threadIdx.x; o < a.count; o += blockDim.x) {
+        uint32_t c[kMaxAxes];
+        const uint32_t addr = run_start(a, o, c);
+        *reinterpret_cast<T*>(slab + static_cast<uint64_t>(o) * E) = *reinterpret_cast<const T*>(sm + addr);
+    }
+}
+
+template <int E, int V, int SU>
+__global__ void __launch_bounds__(512) k_slab_runs(SlabRunArgs a) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    for (uint64_t b = blockIdx.x; b < a.batches; b += gridDim.x) {
+        uint8_t* slab = a.base + b * a.slab_bytes;
+        stage_rows<SU>(a, smem, slab);
+        __syncthreads();
+        write_runs<E, V>(a, smem, slab);
+        __syncthreads();
+    }
+}
+
+// The same for slabs of up to kPfRegs * 16 * 512 bytes that leave room for
+// one CTA per SM only: the next slab is loaded into registers (16-byte
+// loads, kPfRegs per thread) while the current one is written back, so
+// reads and writes overlap without a second shared-memory buffer.  Rows are
+// whole 16-byte chunks (a chunk never straddles two rows).
+constexpr int kPfRegs = 16;
+
+template <int E, int V>
+__global__ void __launch_bounds__(512, 1) k_slab_runs_pf(SlabRunArgs a) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    const uint32_t chunks = static_cast<uint32_t>(a.slab_bytes / 16);
+    uint4 v[kPfRegs];
+    auto fetch = [&](uint64_t b) {
+        const uint4* src = reinterpret_cast<const uint4*>(a.base + b * a.slab_bytes) + threadIdx.x;
+#pragma unroll
+        for (int k = 0; k < kPfRegs; ++k)
+            if (threadIdx.x + k * 512u < chunks) v[k] = src[k * 512];
+    };
+    if (blockIdx.x < a.batches) fetch(blockIdx.x);
+    for (uint64_t b = blockIdx.x; b < a.batches; b += gridDim.x) {
+#pragma unroll
+        for (int k = 0; k < kPfRegs; ++k) {
+            const uint32_t ch = threadIdx.x + k * 512u;
+            if (ch < chunks) {
+                uint32_t r, cb;
+                a.div_upr.divmod(ch, r, cb);  // div_upr counts 16-byte chunks per row here
+                uint32_t* d = reinterpret_cast<uint32_t*>(smem + r * a.pitch + cb * 16);
+                d[0] = v[k].x;
+                d[1] = v[k].y;
+                d[2] = v[k].z;
+                d[3] = v[k].w;
+            }
+        }
+        __syncthreads();  // the slab is in shared memory
+        const uint64_t nxt = b + gridDim.x;
+        if (nxt < a.batches) fetch(nxt);  // in flight during the write-back
+        write_runs<E, V>(a, smem, a.base + b * a.slab_bytes);
+        __syncthreads();  // shared memory is free for the next slab
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Block permutation along cycles.  Blocks of `blk` bytes are indexed by q
 // axes; the block at output index t comes from input index src(t).  The
 // cycles are cut into segments (host table): a first launch copies the block
@@ -270,7 +429,123 @@ void out_geometry(const Pass& p, std::vector<uint64_t>* od, std::vector<uint64_t
     }
 }
 
+constexpr size_t kSlabTwoPerSmBytes = 110 * 1024;  // staged slabs above this leave one CTA per SM
+
 uint64_t table_bytes(uint64_t nseg) { return (3 * nseg * sizeof(uint64_t) + 255) / 256 * 256; }
+
+}  // namespace
+
+namespace {
+
+template <int E, int V, int SU>
+int launch_slab_runs(const SlabRunArgs& a, size_t smem, ExecContext& ctx) {
+    auto kern = k_slab_runs<E, V, SU>;
+    PM_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    int per_sm = 0;
+    PM_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 512, smem));
+    const uint64_t cap = static_cast<uint64_t>(std::max(per_sm, 1)) * device_sms(ctx);
+    const unsigned grid = static_cast<unsigned>(std::max<uint64_t>(1, std::min<uint64_t>(a.batches, cap)));
+    kern<<<grid, 512, smem, ctx.stream>>>(a);
+    PM_CHECK(cudaGetLastError());
+    ctx.launches++;
+    return 0;
+}
+
+template <int E, int V>
+int launch_slab_runs_pf(SlabRunArgs a, size_t smem, ExecContext& ctx) {
+    auto kern = k_slab_runs_pf<E, V>;
+    a.div_upr = FastDiv32::make(a.row_bytes / 16);
+    PM_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    const unsigned grid = static_cast<unsigned>(std::max<uint64_t>(1, std::min<uint64_t>(a.batches, device_sms(ctx))));
+    kern<<<grid, 512, smem, ctx.stream>>>(a);
+    PM_CHECK(cudaGetLastError());
+    ctx.launches++;
+    return 0;
+}
+
+template <int E, int V>
+int dispatch_su(const SlabRunArgs& a, size_t smem, ExecContext& ctx) {
+    // one CTA per SM: prefetch the next slab into registers instead
+    if (smem > kSlabTwoPerSmBytes && a.slab_bytes <= static_cast<uint64_t>(kPfRegs) * 16 * 512 && a.chunks16 &&
+        tuning().slab_prefetch)
+        return launch_slab_runs_pf<E, V>(a, smem, ctx);
+    switch (a.su) {
+        case 16: return launch_slab_runs<E, V, 16>(a, smem, ctx);
+        case 8: return launch_slab_runs<E, V, 8>(a, smem, ctx);
+        case 4: return launch_slab_runs<E, V, 4>(a, smem, ctx);
+        case 2: return launch_slab_runs<E, V, 2>(a, smem, ctx);
+        default: return launch_slab_runs<E, V, 1>(a, smem, ctx);
+    }
+}
+
+template <int E>
+int dispatch_v(const SlabRunArgs& a, size_t smem, uint64_t V, ExecContext& ctx) {
+    if constexpr (E <= 4) {
+        if (V == 16) return dispatch_su<E, 16>(a, smem, ctx);
+        if (V == 8) return dispatch_su<E, 8>(a, smem, ctx);
+        return dispatch_su<E, 4>(a, smem, ctx);
+    } else if constexpr (E == 8) {
+        if (V == 16) return dispatch_su<E, 16>(a, smem, ctx);
+        return dispatch_su<E, 8>(a, smem, ctx);
+    } else {
+        return dispatch_su<E, 16>(a, smem, ctx);
+    }
+}
+
+// The run kernel for whole elements of 1-16 bytes when its padded staging
+// fits; returns -1 when it does not apply.
+int try_slab_runs(uint8_t* data, const Pass& p, uint64_t count, ExecContext& ctx) {
+    const uint64_t E = p.elem;
+    if (!(E == 1 || E == 2 || E == 4 || E == 8 || E == 16) || (p.strip && p.strip != E)) return -1;
+    const int q = static_cast<int>(p.nd_dims.size());
+    const uint64_t row_bytes = p.nd_dims[0] * E;
+    const uint64_t g = std::max<uint64_t>(4, E);
+    uint64_t pitch = (row_bytes + g - 1) / g * g;
+    if ((pitch / g) % 2 == 0) pitch += g;
+    const uint64_t nrows = count / p.nd_dims[0];
+    const size_t smem = nrows * pitch;
+    if (smem > smem_cap_of(ctx.caps)) return -1;
+    uint8_t* base = data + p.offset;
+    const uint64_t addr = reinterpret_cast<uintptr_t>(base);
+    const uint64_t slab_bytes = count * E;
+    const uint64_t V = pow2_unit({addr, slab_bytes});
+    if (V < std::max<uint64_t>(4, E)) return -1;  // stores of at least a word (and a whole element)
+    SlabRunArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.base = base;
+    a.batches = p.batches;
+    a.slab_bytes = slab_bytes;
+    a.count = static_cast<uint32_t>(count);
+    a.q = static_cast<uint32_t>(q);
+    a.nrows = static_cast<uint32_t>(nrows);
+    a.row_bytes = static_cast<uint32_t>(row_bytes);
+    a.pitch = static_cast<uint32_t>(pitch);
+    a.su = static_cast<uint32_t>(pow2_unit({addr, row_bytes, pitch, slab_bytes}));
+    a.chunks16 = pow2_unit({addr, row_bytes, slab_bytes}) == 16;
+    a.div_upr = FastDiv32::make(row_bytes / a.su);
+    // input strides: axis 0 moves E bytes inside a row, axis i >= 1 moves
+    // rows (prod of dims 1..i-1 of them) of `pitch` bytes
+    std::vector<uint64_t> istep(q);
+    istep[0] = E;
+    uint64_t rows = 1;
+    for (int i = 1; i < q; ++i) {
+        istep[i] = rows * pitch;
+        rows *= p.nd_dims[i];
+    }
+    for (int j = 0; j < q; ++j) {
+        const uint64_t d = p.nd_dims[p.nd_perm[j]];
+        a.od[j] = FastDiv32::make(d);
+        a.odim[j] = static_cast<uint32_t>(d);
+        a.step[j] = static_cast<uint32_t>(istep[p.nd_perm[j]]);
+    }
+    switch (E) {
+        case 1: return dispatch_v<1>(a, smem, V, ctx);
+        case 2: return dispatch_v<2>(a, smem, V, ctx);
+        case 4: return dispatch_v<4>(a, smem, V, ctx);
+        case 8: return dispatch_v<8>(a, smem, V, ctx);
+        default: return dispatch_v<16>(a, smem, V, ctx);
+    }
+}
 
 }  // namespace
 
@@ -282,6 +557,10 @@ int run_slab_perm(uint8_t* data, const Pass& p, ExecContext& ctx) {
     }
     uint64_t count = 1;
     for (auto d : p.nd_dims) count *= d;
+    if (count < (uint64_t(1) << 31) && tuning().slab_runs) {
+        const int rc = try_slab_runs(data, p, count, ctx);
+        if (rc >= 0) return rc;
+    }
     const uint64_t w = p.strip ? p.strip : p.elem;
     const size_t smem = count * w;
     if (smem > smem_cap_of(ctx.caps) || count >= (uint64_t(1) << 31)) {

@@ -265,20 +265,21 @@ bool search_plan_uncached(const std::vector<int64_t>& dims, const std::vector<in
                     relax(u, std::move(next), xc, Move{0, i, j, k});
                 }
         // slab moves: L[i:k] into the target's order, elements of L[0:i]
-        for (int i = 0; i < r; ++i)
+        for (int i = 0; tuning().slab_perm && i < r; ++i)
             for (int k = i + 2; k <= r; ++k) {
                 std::vector<int> mid(L.begin() + i, L.begin() + k);
                 std::vector<int> sorted = by_target(mid);
                 if (sorted == mid) continue;
-                const double sc = slab_perm_cost(elem * prod(L, 0, i), prod(L, i, k), caps);
+                double sc = slab_perm_cost(elem * prod(L, 0, i), prod(L, i, k), caps);
                 if (sc < 0) continue;
+                if (tuning().slab_perm == 2) sc *= 0.25;
                 std::vector<int> next(L.begin(), L.begin() + i);
                 next.insert(next.end(), sorted.begin(), sorted.end());
                 next.insert(next.end(), L.begin() + k, L.end());
                 relax(u, std::move(next), sc, Move{1, i, 0, k});
             }
         // cycle moves: blocks of L[0:i], the rest into the target's order
-        for (int i = 1; i + 1 < r; ++i) {
+        for (int i = 1; tuning().cycle_moves && i + 1 < r; ++i) {
             std::vector<int> rest(L.begin() + i, L.end());
             std::vector<int> sorted = by_target(rest);
             if (sorted == rest) continue;

@@ -33,7 +33,7 @@ constexpr uint64_t kMinCycleBlock = 4096;
 
 // Shortest chain one segment of a cycle-following pass walks, and the most
 // segments one cycle is cut into (longer cycles get longer segments).
-constexpr uint64_t kCycleSegment = 64;
+constexpr uint64_t kCycleSegment = 128;
 constexpr uint64_t kMaxCycleSegments = 4096;
 
 // Shared memory (bytes) one CTA may use to stage a slab permutation.

@@ -144,7 +144,7 @@ int dispatch_one(eithot_server* s, int slot, bool* started) {
             return false;  // wait for workspace
         }
         *rc = eithot_transpose_ex(head.data, head.capacity, head.rank, head.dims.data(), head.perm.data(), head.elem,
-                                  head.nb, head.alpha, EITHOT_ORDER_MIXED,
+                                  head.nb, head.alpha, EITHOT_ORDER_FEWEST,
                                   head.scratch && !head.from_hbm ? s->pool_base + off : nullptr,
                                   head.from_hbm ? 0 : head.scratch, st);
         if (*rc != EITHOT_OK) {
@@ -353,7 +353,7 @@ int eithot_server_submit(eithot_server* s, void* d_data, size_t capacity_bytes, 
     Request r;
     NdPlan plan;
     std::vector<Pass> passes;
-    if (int rc = build(rank, dims, perm_1based, elem_size, num_sub_tensors, alpha, EITHOT_ORDER_MIXED, s->caps,
+    if (int rc = build(rank, dims, perm_1based, elem_size, num_sub_tensors, alpha, EITHOT_ORDER_FEWEST, s->caps,
                        &plan, &passes))
         return rc;
     r.bytes = static_cast<size_t>(plan.volume) * elem_size;

@@ -135,10 +135,11 @@ int eithot_transpose_ex(void* d_data, size_t capacity_bytes, int rank,
  * array inside the library, which every GPU that loads the library holds
  * until the process exits.  For callers that may not allocate device memory
  * during the call, e.g. because another allocator owns the device's memory.
- * Requests needing more than 32 MiB of scratch fail with EITHOT_EINVAL.  The
- * first call on a device looks up the array's address; make it before any
- * stream capture.  Calls share the array: calls whose device work overlaps
- * race on it. */
+ * Requests needing more than 32 MiB of scratch fail with EITHOT_EINVAL.  Each
+ * call looks up the array's address on the current device (no allocation;
+ * the first lookup on a device may load the library's device code, so make
+ * the first call before any stream capture).  Calls share the array: calls
+ * whose device work overlaps race on it. */
 int eithot_transpose_noalloc(void* d_data, size_t capacity_bytes, int rank,
                              const int64_t* dims, const int* perm_1based,
                              size_t elem_size, int num_sub_tensors, double alpha,
@@ -170,7 +171,10 @@ int eithot_workspace_size(int rank, const int64_t* dims, const int* perm_1based,
 /* ---- the batched form -------------------------------------------------------
  * No reference counterpart (the reference transposes one tensor per call).
  * eithot_batch_create plans `count` independent transposes once, host only:
- * tensor t has rank ranks[t]; its dims and 1-based permutation are the next
+ * every tensor is planned for the fewest modelled passes (as
+ * EITHOT_ORDER_FEWEST, without cycle-following moves, so that every pass can
+ * be captured in a graph); tensor t has rank ranks[t]; its dims and 1-based
+ * permutation are the next
  * ranks[t] entries of `dims` and `perms_1based` (tensors back to back);
  * elem_sizes[t] as for eithot_transpose; num_sub_tensors and alpha apply to
  * every tensor.  eithot_batch_run transposes all of them in place
@@ -210,7 +214,8 @@ int eithot_batch_destroy(eithot_batch* batch);
  * 256 MB free): it runs alone with scratch allocated when it starts, and
  * such requests wait for one another while free HBM cannot hold them all;
  * it is refused with EITHOT_EBUSY only when free HBM cannot hold it at
- * submission.  Requests run in arrival order; consecutive requests under
+ * submission.  Every request is planned for the fewest modelled passes
+ * (EITHOT_ORDER_FEWEST).  Requests run in arrival order; consecutive requests under
  * 64 MB at the head of the queue are run together as one batch (continuous
  * batching; a batch whose lane workspaces exceed the pool is halved until
  * it fits), larger ones alone.
@@ -302,6 +307,17 @@ int eithot_estimate_report(int rank, const int64_t* dims, const int* perm_1based
  *                 (default: the arriving CTA's loads have all landed in
  *                 shared memory), 0 release arrivals
  *   "group_per_sm" group form: 0 cost model, 1..4 resident CTAs per SM
+ *   "slab_perm"   plans for the fewest passes: 0 no on-chip slab
+ *                 permutations, 1 cost model (default), 2 preferred
+ *   "slab_runs"   1 slab permutations of 1-16 byte elements write runs of
+ *                 consecutive outputs per thread from rows staged at a padded
+ *                 pitch (default), 0 one divide chain per element
+ *   "slab_prefetch" 1 slab permutations whose padded slab leaves one CTA per
+ *                 SM prefetch the next slab into registers (up to 128 KB),
+ *                 0 not
+ *   "cycle_moves" 1 plans for the fewest passes (EITHOT_ORDER_FEWEST) may
+ *                 permute blocks along the permutation's cycles (the segment
+ *                 table is copied from the host each call), 0 not
  *   "col_bulk"    1 group passes may run double-buffered with their row pieces
  *                 staged by bulk copies (cp.async.bulk, mbarrier completion)
  *                 when every piece is whole 16-byte-aligned elements, 0 not

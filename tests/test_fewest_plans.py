@@ -50,8 +50,21 @@ def run_case(E, dims, perm, elem, alpha=0.01, seed=1, workspace=None, expect=Non
     return E.last_stats()
 
 
+@pytest.fixture(params=[(1, 1), (1, 0), (0, 0)], ids=["runs-prefetch", "runs", "per-element"])
+def slab_kernel(E, request):
+    """The slab-permutation kernels: runs of outputs per thread from padded
+    rows (with the next slab prefetched into registers when one CTA per SM
+    fits, or without), and one divide chain per element."""
+    old = (E.tune_get("slab_runs"), E.tune_get("slab_prefetch"))
+    E.tune_set("slab_runs", request.param[0])
+    E.tune_set("slab_prefetch", request.param[1])
+    yield request.param
+    E.tune_set("slab_runs", old[0])
+    E.tune_set("slab_prefetch", old[1])
+
+
 @pytest.mark.parametrize("rank", [3, 4, 5])
-def test_every_permutation(E, rank):
+def test_every_permutation(E, rank, slab_kernel):
     rng = random.Random(7 + rank)
     for perm in itertools.permutations(range(1, rank + 1)):
         for elem in (1, 2, 4, 8):
@@ -71,8 +84,27 @@ def test_every_permutation(E, rank):
     ([8, 7, 6, 5, 4, 3], [6, 4, 2, 1, 3, 5], 4, None),
     ([2, 3, 5, 7, 11, 13, 2], [7, 1, 6, 2, 5, 3, 4], 1, None),
     ([4096, 33, 65], [1, 3, 2], 1, None), ([3001, 4096], [2, 1], 4, None), ([4, 2001, 819, 2], [1, 3, 2, 4], 4, None)])
-def test_named_shapes(E, dims, perm, elem, expect):
+def test_named_shapes(E, dims, perm, elem, expect, slab_kernel):
     run_case(E, dims, perm, elem, expect=expect)
+
+
+@pytest.mark.parametrize("elem", [1, 2, 4, 8, 16, 24])
+def test_slab_permutations_forced(E, elem, slab_kernel):
+    """Slab permutations preferred over every other move (knob slab_perm=2):
+    3- to 5-axis slabs of 1- to 24-byte elements, odd and even row widths,
+    unaligned slab sizes, 128 KB slabs of 2-byte elements."""
+    old = E.tune_get("slab_perm")
+    E.tune_set("slab_perm", 2)
+    try:
+        for dims, perm in [([16, 64, 4, 9], [3, 2, 1, 4]), ([7, 33, 5, 11], [2, 3, 1, 4]),
+                           ([5, 6, 7, 8, 3], [4, 2, 1, 3, 5]), ([64, 32, 8, 5], [2, 3, 1, 4]), ([3, 1000, 7], [2, 1, 3]),
+                           ([16, 1024, 4, 5], [3, 2, 1, 4])]:
+            limit = 128 * 1024 if dims[:2] == [16, 1024] else 100 * 1024
+            while math.prod(dims[:-1]) * elem > limit:
+                dims[1] //= 2
+            run_case(E, dims, perm, elem)
+    finally:
+        E.tune_set("slab_perm", old)
 
 
 def test_cycle_permutation_in_chunks(E):

@@ -83,3 +83,26 @@ def test_noalloc_rejects_scratch_beyond_its_limit(E):
     assert "scratch" in E.lib.eithot_last_error().decode()
     torch.cuda.synchronize()
     assert torch.equal(t, before)
+
+
+def test_noalloc_without_scratch_and_on_two_streams(E):
+    """A transpose that needs no scratch at all (the array is not touched),
+    then scratch-using calls on two different streams one after the other:
+    each matches the allocating entry point and the oracle."""
+    dev = torch.device("cuda:0")
+    cases = [([37, 64, 5, 3], [3, 1, 4, 2], 4, 1, 0.01), ([4, 20011, 819, 2], [1, 3, 2, 4], 4, 1, 0.01)]
+    assert E.workspace_size(*cases[0][:3]) == 0
+    streams = [torch.cuda.Stream(dev), torch.cuda.Stream(dev)]
+    for k, (dims, perm, elem, nb, alpha) in enumerate(cases):
+        for s in streams:
+            n = math.prod(dims)
+            host = oracle.fill_hash(n, elem, 77 + k)
+            a = torch.from_numpy(host.copy()).to(dev)
+            b = a.clone()
+            torch.cuda.synchronize()
+            E.transpose_ptr(a.data_ptr(), a.numel(), dims, perm, elem, nb, alpha, E.ORDER_MIXED, s.cuda_stream)
+            assert _noalloc(E, b, b.numel(), dims, perm, elem, nb, alpha, s) == E.OK, E.lib.eithot_last_error().decode()
+            s.synchronize()
+            assert torch.equal(a, b)
+            assert np.array_equal(b.cpu().numpy(), oracle.permute(host, dims, perm, elem))
+    assert E.index_faults() == 0 and E.sync_timeouts() == 0
