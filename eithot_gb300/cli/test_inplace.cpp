@@ -15,6 +15,12 @@
 // 64-bit: there is no 22 GB limit.  Errors print a message and exit 1
 // instead of the reference's exit(-1).
 //
+// EITHOT_REORDER_TYPE=0|1|2|3 in the environment selects the decomposition
+// order the reference selects at compile time (REORDER_TYPE in
+// ITNT/src/Nd_transpose.cpp:22-28: 0 mixed, 1 pre-order, 2 post-order; its
+// README's experiment 6 rebuilds the program for each), or 3 for this
+// library's fewest-pass plans; unset, the reference's default (mixed).
+//
 // EITHOT_MEMORY_TYPE=2 in the environment selects the reference's managed
 // path, which it selects at compile time (MEMORY_TYPE 2,
 // padding_managed_transpose, ITNT/src/test_inplace.cpp:91-136): the tensor
@@ -38,6 +44,13 @@
 namespace {
 
 constexpr double kPaddingSlack = 0.03;
+
+// EITHOT_REORDER_TYPE from the environment (0 mixed when unset).
+int reorder_type() {
+    const char* v = std::getenv("EITHOT_REORDER_TYPE");
+    const int t = v ? std::atoi(v) : EITHOT_ORDER_MIXED;
+    return (t >= EITHOT_ORDER_MIXED && t <= EITHOT_ORDER_FEWEST) ? t : EITHOT_ORDER_MIXED;
+}
 
 #define CLI_CHECK(expr)                                                                   \
     do {                                                                                  \
@@ -130,7 +143,8 @@ int run(const std::vector<int64_t>& dims, const std::vector<int>& perm, int nb, 
     CLI_CHECK(cudaEventRecord(start, 0));
     CLI_CHECK(cudaMemcpy(d, h, data_size, cudaMemcpyHostToDevice));
     CLI_CHECK(cudaEventRecord(h2d, 0));
-    if (eithot_transpose(d, gpu_size, rank, dims.data(), perm.data(), sizeof(T), nb, alpha, nullptr) != EITHOT_OK) {
+    if (eithot_transpose_ex(d, gpu_size, rank, dims.data(), perm.data(), sizeof(T), nb, alpha, reorder_type(), nullptr, 0,
+                            nullptr) != EITHOT_OK) {
         std::fprintf(stderr, "test_inplace: %s\n", eithot_last_error());
         return 1;
     }
@@ -189,7 +203,8 @@ int run_managed(const std::vector<int64_t>& dims, const std::vector<int>& perm, 
     CLI_CHECK(cudaEventCreate(&start));
     CLI_CHECK(cudaEventCreate(&stop));
     CLI_CHECK(cudaEventRecord(start, 0));
-    if (eithot_transpose(m, gpu_size, rank, dims.data(), perm.data(), sizeof(T), nb, alpha, nullptr) != EITHOT_OK) {
+    if (eithot_transpose_ex(m, gpu_size, rank, dims.data(), perm.data(), sizeof(T), nb, alpha, reorder_type(), nullptr, 0,
+                            nullptr) != EITHOT_OK) {
         std::fprintf(stderr, "test_inplace: %s\n", eithot_last_error());
         return 1;
     }
