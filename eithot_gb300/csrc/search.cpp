@@ -42,17 +42,25 @@ uint64_t slab_perm_strip(uint64_t E, uint64_t count, const DeviceCaps& caps) {
 
 namespace {
 
-constexpr uint64_t kSlabTwoPerSm = 110 * 1024;
-
 // Modelled cost of a slab permutation of `count` elements of E bytes per
-// slab (gathers out of shared memory; narrow elements need more
-// instructions per byte).
+// slab: the copy rate over the rate measured on GB300 for 3- and 4-axis
+// slabs of 64-128 KB (E = 32, 16: 6.0-6.1 TB/s; 8: 3.6; 4: 2.4-3.0;
+// 2: 1.4-1.8; 1: 0.7-1.0), each element gathered out of shared memory.
 double slab_perm_cost(uint64_t E, uint64_t count, const DeviceCaps& caps) {
     const uint64_t w = slab_perm_strip(E, count, caps);
     const uint64_t bytes = count * w;
     if (bytes > slab_perm_capacity(caps)) return -1.0;
-    double c = E >= 16 ? 1.05 : E >= 4 ? 1.15 : E >= 2 ? 1.5 : 1.9;
-    if (bytes > kSlabTwoPerSm) c += 0.25;
+    return E >= 16 ? 1.08 : E >= 8 ? 1.8 : E >= 4 ? 2.4 : E >= 2 ? 4.0 : 7.5;
+}
+
+// Extra cost of a lowered 2D transpose the lowering's model underrates:
+// one-CTA slab transposes of 1- and 2-byte elements whose rows are short
+// (64 bytes or less) ran at 0.9-2.1 TB/s on GB300 against the 1.0-1.25
+// passes the model gives any slab.
+double narrow_slab_penalty(const std::vector<Pass>& ps) {
+    double c = 0;
+    for (const Pass& p : ps)
+        if (p.type == kSlabTranspose && p.elem <= 2 && p.cols * p.elem <= 64) c += p.elem == 1 ? 5.0 : 2.0;
     return c;
 }
 
@@ -210,7 +218,9 @@ bool search_plan_uncached(const std::vector<int64_t>& dims, const std::vector<in
         auto key = std::make_tuple(B, R, C, E);
         auto it = xcache.find(key);
         if (it != xcache.end()) return it->second;
-        const double c = xpose_cost(Xpose{0, B, R, C, E}, caps);
+        std::vector<Pass> ps;
+        lower_xpose(Xpose{0, B, R, C, E}, caps, &ps);
+        const double c = passes_cost_of(ps, caps) + narrow_slab_penalty(ps);
         xcache.emplace(key, c);
         return c;
     };
@@ -351,7 +361,7 @@ double passes_model_cost(const std::vector<Pass>& passes, const DeviceCaps& caps
             c += 1.0;
         } else {
             std::vector<Pass> one(1, p);
-            c += passes_cost_of(one, caps);
+            c += passes_cost_of(one, caps) + narrow_slab_penalty(one);
         }
     }
     return c;
