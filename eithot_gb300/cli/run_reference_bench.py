@@ -15,8 +15,10 @@ OUT.  --reorder-type sets EITHOT_REORDER_TYPE for test_inplace (the
 reference's compile-time REORDER_TYPE: 0 mixed, 1 pre, 2 post; 3 this
 library's fewest-pass plans), as its experiment 6 asks.  --cases N keeps the
 first N lines of every case file (a bounded run; the default keeps all).
-Prints one JSON line: cases run, cases verified correct, and the mean/std
-of the time and throughput columns per case file.
+Prints one JSON line: cases run, cases verified correct, the mean/std of
+the time and throughput columns per case file, and per case (in run order)
+its dims, sub-tensor count, size, verdict and the two times test_inplace
+prints ("Execution Time without h2d2h" and "Execution Time", ms).
 """
 from __future__ import annotations
 
@@ -24,6 +26,7 @@ import argparse
 import glob
 import json
 import os
+import re
 import shutil
 import statistics
 import subprocess
@@ -32,6 +35,20 @@ import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 BIN = os.path.join(os.path.dirname(HERE), "bin")
+
+
+CASE_RE = re.compile(r"number of sub_tensors = (\d+)\s*\nDims = ([0-9 ]+), Data size = ([0-9.]+) GB\n"
+                     r"(?:.*\n)*?(Correct|Incorrect) transpose\n"
+                     r"Execution Time without h2d2h: ([0-9.]+)ms\nExecution Time: ([0-9.]+)ms")
+
+
+def per_case(log):
+    """The test_inplace blocks of the script's console output, in order."""
+    out = []
+    for m in CASE_RE.finditer(log):
+        out.append({"nb": int(m.group(1)), "dims": [int(x) for x in m.group(2).split()], "gb": float(m.group(3)),
+                    "correct": m.group(4) == "Correct", "kernel_ms": float(m.group(5)), "e2e_ms": float(m.group(6))})
+    return out
 
 
 def main() -> int:
@@ -66,6 +83,7 @@ def main() -> int:
         summary = {"task": args.task, "reorder_type": args.reorder_type, "exit": p.returncode,
                    "cases": log.count("Execution Time:"), "correct": log.count("Correct transpose"),
                    "incorrect": log.count("Incorrect transpose"), "files": {}}
+        summary["per_case"] = per_case(log)
         for d in sorted(glob.glob(os.path.join(work, "test_cases", "exp%d" % args.task, "*"))):
             if not os.path.isdir(d):
                 continue

@@ -128,7 +128,9 @@ int apply_knob(eithot::Tuning& t, const char* key, double value) {
         if (v < 0 || v > 2) return fail(EITHOT_EINVAL, "slab_perm must be 0, 1 or 2");
         t.slab_perm = v;
     } else if (k == "slab_runs") {
-        t.slab_runs = value != 0.0 ? 1 : 0;
+        const int v = static_cast<int>(value);
+        if (v < 0 || v > 2) return fail(EITHOT_EINVAL, "slab_runs must be 0, 1 or 2");
+        t.slab_runs = v;
     } else if (k == "slab_prefetch") {
         t.slab_prefetch = value != 0.0 ? 1 : 0;
     } else if (k == "col_bulk") {

@@ -142,6 +142,16 @@ struct SlabRunArgs {
     FastDiv32 od[kMaxAxes];   // output dims, output order
     uint32_t odim[kMaxAxes];
     uint32_t step[kMaxAxes];  // shared-memory bytes per step of output axis j
+    // Aligned runs: when the output dims below axis m multiply to a divisor
+    // P of the run length K and K divides P * odim[m], every run starts at
+    // coordinate 0 of the axes below m and never carries past axis m, so
+    // the t-th output of every run lies delta[t] bytes after the run's
+    // first element, whose address only axes m.. determine (through the
+    // run index times K / P).
+    uint32_t aligned, m_axis, nhi, rmul;
+    FastDiv32 hod[kMaxAxes];  // output dims m.., output order
+    uint32_t hstep[kMaxAxes];
+    uint32_t delta[16];
 };
 
 template <int E> struct ElemT;
@@ -178,12 +188,52 @@ __device__ __forceinline__ uint32_t run_start(const SlabRunArgs& a, uint32_t o, 
     return addr;
 }
 
+// Stores the K = V / E elements of one run as one V-byte store.
+template <int E, int V>
+__device__ __forceinline__ void store_run(uint8_t* dst, const typename ElemT<E>::T* v) {
+    using T = typename ElemT<E>::T;
+    constexpr int K = V / E;
+    if constexpr (E >= 4) {
+#pragma unroll
+        for (int t = 0; t < K; ++t) reinterpret_cast<T*>(dst)[t] = v[t];
+    } else {
+        constexpr int W = V / 4;
+        uint32_t w[W];
+#pragma unroll
+        for (int i = 0; i < W; ++i) w[i] = 0;
+#pragma unroll
+        for (int t = 0; t < K; ++t) w[t * E / 4] |= static_cast<uint32_t>(v[t]) << (8 * ((t * E) % 4));
+        if constexpr (V == 16) *reinterpret_cast<uint4*>(dst) = make_uint4(w[0], w[1], w[2], w[3]);
+        else if constexpr (V == 8) *reinterpret_cast<uint2*>(dst) = make_uint2(w[0], w[1]);
+        else *reinterpret_cast<uint32_t*>(dst) = w[0];
+    }
+}
+
 // Writes the staged slab back in output order: runs of K outputs per thread.
 template <int E, int V>
 __device__ __forceinline__ void write_runs(const SlabRunArgs& a, const uint8_t* sm, uint8_t* slab) {
     using T = typename ElemT<E>::T;
     constexpr int K = V / E;
     const uint32_t runs = a.count / K;
+    if (a.aligned) {
+        for (uint32_t g = threadIdx.x; g < runs; g += blockDim.x) {
+            uint32_t x = g * a.rmul, addr = 0;
+#pragma unroll
+            for (int j = 0; j < kMaxAxes; ++j) {
+                if (j < static_cast<int>(a.nhi)) {
+                    uint32_t qt, c;
+                    a.hod[j].divmod(x, qt, c);
+                    addr += c * a.hstep[j];
+                    x = qt;
+                }
+            }
+            T v[K];
+#pragma unroll
+            for (int t = 0; t < K; ++t) v[t] = *reinterpret_cast<const T*>(sm + addr + a.delta[t]);
+            store_run<E, V>(slab + static_cast<uint64_t>(g) * V, v);
+        }
+        return;
+    }
     for (uint32_t g = threadIdx.x; g < runs; g += blockDim.x) {
         uint32_t c[kMaxAxes];
         uint32_t addr = run_start(a, g * K, c);
@@ -207,21 +257,7 @@ __device__ __forceinline__ void write_runs(const SlabRunArgs& a, const uint8_t* 
                 }
             }
         }
-        uint8_t* dst = slab + static_cast<uint64_t>(g) * V;
-        if constexpr (E >= 4) {
-#pragma unroll
-            for (int t = 0; t < K; ++t) reinterpret_cast<T*>(dst)[t] = v[t];
-        } else {
-            constexpr int W = V / 4;
-            uint32_t w[W];
-#pragma unroll
-            for (int i = 0; i < W; ++i) w[i] = 0;
-#pragma unroll
-            for (int t = 0; t < K; ++t) w[t * E / 4] |= static_cast<uint32_t>(v[t]) << (8 * ((t * E) % 4));
-            if constexpr (V == 16) *reinterpret_cast<uint4*>(dst) = make_uint4(w[0], w[1], w[2], w[3]);
-            else if constexpr (V == 8) *reinterpret_cast<uint2*>(dst) = make_uint2(w[0], w[1]);
-            else *reinterpret_cast<uint32_t*>(dst) = w[0];
-        }
+        store_run<E, V>(slab + static_cast<uint64_t>(g) * V, v);
     }
     for (uint32_t o = runs * K + threadIdx.x; o < a.count; o += blockDim.x) {
         uint32_t c[kMaxAxes];
@@ -492,6 +528,39 @@ int dispatch_v(const SlabRunArgs& a, size_t smem, uint64_t V, ExecContext& ctx) 
     }
 }
 
+// Fills the aligned-run fields when runs of K outputs qualify (see
+// SlabRunArgs); leaves `aligned` 0 otherwise.
+void set_aligned_runs(SlabRunArgs* a, uint64_t K) {
+    a->aligned = 0;
+    if (K == 0 || K > 16 || a->count % K != 0) return;
+    uint64_t P = 1;
+    for (uint32_t m = 0; m < a->q; ++m) {
+        const uint64_t P1 = P * a->odim[m];
+        if (K % P == 0 && P1 % K == 0) {
+            a->aligned = 1;
+            a->m_axis = m;
+            a->rmul = static_cast<uint32_t>(K / P);
+            a->nhi = a->q - m;
+            for (uint32_t j = m; j < a->q; ++j) {
+                a->hod[j - m] = a->od[j];
+                a->hstep[j - m] = a->step[j];
+            }
+            for (uint64_t t = 0; t < K; ++t) {
+                uint64_t off = 0, r = t;
+                for (uint32_t j = 0; j < m; ++j) {
+                    off += (r % a->odim[j]) * a->step[j];
+                    r /= a->odim[j];
+                }
+                off += r * a->step[m];  // r = t / P < K / P <= odim[m]
+                a->delta[t] = static_cast<uint32_t>(off);
+            }
+            return;
+        }
+        P = P1;
+        if (P > K) return;
+    }
+}
+
 // The run kernel for whole elements of 1-16 bytes when its padded staging
 // fits; returns -1 when it does not apply.
 int try_slab_runs(uint8_t* data, const Pass& p, uint64_t count, ExecContext& ctx) {
@@ -538,6 +607,7 @@ int try_slab_runs(uint8_t* data, const Pass& p, uint64_t count, ExecContext& ctx
         a.odim[j] = static_cast<uint32_t>(d);
         a.step[j] = static_cast<uint32_t>(istep[p.nd_perm[j]]);
     }
+    if (tuning().slab_runs == 1) set_aligned_runs(&a, V / E);
     switch (E) {
         case 1: return dispatch_v<1>(a, smem, V, ctx);
         case 2: return dispatch_v<2>(a, smem, V, ctx);

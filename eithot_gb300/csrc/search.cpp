@@ -42,15 +42,45 @@ uint64_t slab_perm_strip(uint64_t E, uint64_t count, const DeviceCaps& caps) {
 
 namespace {
 
+// True when a slab permutation's write-back runs qualify for offsets read
+// from a table (the run kernel's aligned form): with runs of K = V / E
+// outputs per V-byte store (V the largest power of two up to 16 dividing the
+// slab's bytes), the output dims below some axis m multiply to a divisor of
+// K that K times ... divides the product up to and including axis m.
+bool slab_runs_aligned(uint64_t E, const std::vector<uint64_t>& odims) {
+    if (E > 16 || (E & (E - 1)) != 0) return false;
+    uint64_t count = 1;
+    for (auto d : odims) count *= d;
+    uint64_t V = 16;
+    while (V > E && (count * E) % V != 0) V /= 2;
+    if (V < 4 || V < E) return false;
+    const uint64_t K = V / E;
+    uint64_t P = 1;
+    for (uint64_t d : odims) {
+        if (K % P == 0 && (P * d) % K == 0) return true;
+        P *= d;
+        if (P > K) return false;
+    }
+    return false;
+}
+
 // Modelled cost of a slab permutation of `count` elements of E bytes per
-// slab: the copy rate over the rate measured on GB300 for 3- and 4-axis
-// slabs of 64-128 KB (E = 32, 16: 6.0-6.1 TB/s; 8: 3.6; 4: 2.4-3.0;
-// 2: 1.4-1.8; 1: 0.7-1.0), each element gathered out of shared memory.
-double slab_perm_cost(uint64_t E, uint64_t count, const DeviceCaps& caps) {
+// slab (`odims`: the slab's dims in output order), the copy rate over the
+// rate measured on GB300.  Runs with table offsets (3- and 4-axis slabs of
+// 64-128 KB): E = 16, 32: 6.0-6.1 TB/s; 8: 4.8; 4: 4.6-5.7; 2: 4.8-6.2;
+// slabs of 110 KB or less run two CTAs per SM without register prefetch and
+// sit at the low end.  Runs stepping through the axes per element: E = 8:
+// 3.6-3.8; 4: 2.4-3.0; 2: 1.4-1.9; 1: 0.7-1.0.
+double slab_perm_cost(uint64_t E, uint64_t count, const std::vector<uint64_t>& odims, const DeviceCaps& caps) {
     const uint64_t w = slab_perm_strip(E, count, caps);
     const uint64_t bytes = count * w;
     if (bytes > slab_perm_capacity(caps)) return -1.0;
-    return E >= 16 ? 1.08 : E >= 8 ? 1.8 : E >= 4 ? 2.4 : E >= 2 ? 4.0 : 7.5;
+    if (E >= 16) return 1.08;
+    if (slab_runs_aligned(E, odims)) {
+        const double c = E >= 8 ? 1.3 : E >= 4 ? 1.15 : E >= 2 ? 1.1 : 1.6;
+        return bytes <= 110 * 1024 ? c + 0.25 : c;
+    }
+    return E >= 8 ? 1.8 : E >= 4 ? 2.4 : E >= 2 ? 4.0 : 7.5;
 }
 
 // Extra cost of a lowered 2D transpose the lowering's model underrates:
@@ -101,7 +131,9 @@ double passes_model_cost_new(const Pass& p, const DeviceCaps& caps) {
     if (p.type == kSlabPerm) {
         uint64_t count = 1;
         for (auto d : p.nd_dims) count *= d;
-        const double c = slab_perm_cost(p.elem, count, caps);
+        std::vector<uint64_t> od;
+        for (int j : p.nd_perm) od.push_back(p.nd_dims[j]);
+        const double c = slab_perm_cost(p.elem, count, od, caps);
         return c < 0 ? 3.0 : c;
     }
     if (p.type == kBlockPerm) {
@@ -280,7 +312,9 @@ bool search_plan_uncached(const std::vector<int64_t>& dims, const std::vector<in
                 std::vector<int> mid(L.begin() + i, L.begin() + k);
                 std::vector<int> sorted = by_target(mid);
                 if (sorted == mid) continue;
-                double sc = slab_perm_cost(elem * prod(L, 0, i), prod(L, i, k), caps);
+                std::vector<uint64_t> od;
+                for (int a : sorted) od.push_back(size[a]);
+                double sc = slab_perm_cost(elem * prod(L, 0, i), prod(L, i, k), od, caps);
                 if (sc < 0) continue;
                 if (tuning().slab_perm == 2) sc *= 0.25;
                 std::vector<int> next(L.begin(), L.begin() + i);

@@ -50,11 +50,12 @@ def run_case(E, dims, perm, elem, alpha=0.01, seed=1, workspace=None, expect=Non
     return E.last_stats()
 
 
-@pytest.fixture(params=[(1, 1), (1, 0), (0, 0)], ids=["runs-prefetch", "runs", "per-element"])
+@pytest.fixture(params=[(1, 1), (1, 0), (2, 1), (0, 0)], ids=["runs-prefetch", "runs", "runs-carry", "per-element"])
 def slab_kernel(E, request):
     """The slab-permutation kernels: runs of outputs per thread from padded
     rows (with the next slab prefetched into registers when one CTA per SM
-    fits, or without), and one divide chain per element."""
+    fits, or without; runs whose outputs share offsets read them from a
+    table unless slab_runs is 2), and one divide chain per element."""
     old = (E.tune_get("slab_runs"), E.tune_get("slab_prefetch"))
     E.tune_set("slab_runs", request.param[0])
     E.tune_set("slab_prefetch", request.param[1])
@@ -102,6 +103,26 @@ def test_slab_permutations_forced(E, elem, slab_kernel):
                            ([16, 1024, 4, 5], [3, 2, 1, 4])]:
             limit = 128 * 1024 if dims[:2] == [16, 1024] else 100 * 1024
             while math.prod(dims[:-1]) * elem > limit:
+                dims[1] //= 2
+            run_case(E, dims, perm, elem)
+    finally:
+        E.tune_set("slab_perm", old)
+
+
+@pytest.mark.parametrize("elem", [1, 2, 4, 8, 16])
+def test_slab_permutations_aligned_runs(E, elem, slab_kernel):
+    """Slabs whose output axes below the store width divide it (runs of
+    outputs that share their shared-memory offsets): two to four axes,
+    runs inside the fastest output axis, covering it exactly, and spanning
+    two and four of its rows; the (16, 1024, 4) 2-byte slab of the 100 GB
+    configuration's plan."""
+    old = E.tune_get("slab_perm")
+    E.tune_set("slab_perm", 2)
+    try:
+        for dims, perm in [([16, 1024, 4, 3], [3, 2, 1, 4]), ([32, 64, 16, 2], [2, 3, 1, 4]), ([8, 2, 64, 5], [2, 1, 3, 4]),
+                           ([64, 4, 16, 3], [2, 3, 1, 4]), ([2, 4, 8, 16, 3], [4, 2, 3, 1, 5]), ([128, 256, 3], [2, 1, 3]),
+                           ([4, 4, 4, 4, 4, 2], [5, 4, 3, 2, 1, 6])]:
+            while math.prod(dims[:-1]) * elem > 128 * 1024:
                 dims[1] //= 2
             run_case(E, dims, perm, elem)
     finally:
