@@ -16,7 +16,9 @@ e2e:   the same metric through the C ABI with the tensor in pinned host
        the result back; consecutive steps are pipelined over three device
        buffers (copies of one step overlap the transpose of another).
 Beside them: the 3001 x 4096 int32 matrix (perm (2 1)) timed the same way
-(device-resident and end to end), the reference's own CUDA build
+(device-resident and end to end), the (16, 3001, 1024, 256, 4) uint16 tensor
+(100.7 GB, perm (5 3 1 4 2)) device-resident under the fewest-pass plan and
+the reference's series, the reference's own CUDA build
 (test_inplace recompiled for sm_103a from baseline/_ref, when built) on both
 configurations, and the reference's own single-threaded host permutation
 next to the oracle's OpenMP restatement of it.
@@ -252,6 +254,58 @@ def reference_gpu(timeout=900):
                      "device_ms": d, "device_gbs": 2.0 * nbytes / (d / 1e3) / 1e9,
                      "e2e_ms": a, "e2e_gbs": 2.0 * nbytes / (a / 1e3) / 1e9,
                      "command": "test_inplace " + " ".join(args)}
+    return out
+
+
+C3 = ([16, 3001, 1024, 256, 4], [5, 3, 1, 4, 2], 2, 0.05)
+
+
+def time_c3(E, dev, steps=3):
+    """The (16, 3001, 1024, 256, 4) uint16 tensor (100.7 GB, larger than L2),
+    perm (5 3 1 4 2), nb 1, alpha 0.05, device-resident: the fewest-pass plan
+    (EITHOT_ORDER_FEWEST) and the reference's series (EITHOT_ORDER_MIXED, the
+    default).  Each plan's first transpose is checked on the device element
+    by element; then `steps` transposes are timed with CUDA events (each
+    re-transposes the buffer as a fresh tensor of the same shape)."""
+    import torch
+    dims, perm, elem, alpha = C3
+    n = math.prod(dims)
+    nbytes = n * elem
+    free, _ = torch.cuda.mem_get_info(dev)
+    if free < nbytes * 1.08:
+        return {"unavailable": "needs %.1f GB of free device memory, %.1f GB free" % (nbytes * 1.08 / 1e9, free / 1e9)}
+    buf = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    peak, _ = load_peaks()
+    out = {"dims": dims, "perm": perm, "elem_bytes": elem, "alpha": alpha, "bytes": nbytes}
+    for name, order in (("fewest_passes", E.ORDER_FEWEST), ("reference_series", E.ORDER_MIXED)):
+        E.fill_hash_ptr(buf.data_ptr(), n, elem, SEED, 0, stream.cuda_stream)
+        E.transpose_ptr(buf.data_ptr(), nbytes, dims, perm, elem, 1, alpha, order, stream.cuda_stream)
+        bad, _ = E.check_hash_ptr(buf.data_ptr(), dims, perm, elem, SEED, stream.cuda_stream)
+        status = E.call_status(E.last_call(), stream.cuda_stream)
+        E.profile_reset()
+        E.set_profiling(True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            E.transpose_ptr(buf.data_ptr(), nbytes, dims, perm, elem, 1, alpha, order, stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        E.set_profiling(False)
+        st = E.last_stats()
+        ms = e0.elapsed_time(e1) / steps
+        per = {}
+        for p in E.profile():
+            d = per.setdefault(p["name"], [0.0, 0, p["bytes"]])
+            d[0] += p["ms"]
+            d[1] += 1
+        E.profile_reset()
+        out[name] = {"bit_exact": bad == 0 and status == E.OK, "ms": ms, "gbs": 2.0 * nbytes / (ms / 1e3) / 1e9,
+                     "frac": 2.0 * nbytes / (ms / 1e3) / 1e9 / peak, "passes": st["n_passes"],
+                     "workspace_bytes": st["workspace_bytes"],
+                     "per_pass": {k: {"ms": v[0] / v[1], "gbs": v[2] / (v[0] / v[1] / 1e3) / 1e9} for k, v in per.items()}}
+    del buf
+    torch.cuda.empty_cache()
     return out
 
 
@@ -561,6 +615,7 @@ def run_eithot(args):
             del buf
             torch.cuda.empty_cache()
             line["reference_gpu"] = reference_gpu()
+            line["c3_16x3001x1024x256x4_u16"] = time_c3(E, dev)
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist

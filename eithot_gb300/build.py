@@ -29,7 +29,7 @@ CLI_PROGRAMS = {"test_inplace": "test_inplace.cpp", "Nd_estimation": "nd_estimat
 CLI_SCRIPTS = ["Statistic.py"]  # run by the reference's benchmark script beside the programs
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["kernels.cu", "checks.cu", "perm.cu"]
+CU_SOURCES = ["kernels.cu", "checks.cu", "perm.cu", "noalloc.cu", "status.cu"]
 CPP_SOURCES = ["plan.cpp", "lower.cpp", "search.cpp", "estimator.cpp", "capi.cpp", "batch.cpp", "server.cpp"]
 
 

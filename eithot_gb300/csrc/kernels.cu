@@ -39,10 +39,9 @@ constexpr int kThreads = 512;
 // eithot_index_faults().
 __device__ unsigned int g_index_faults = 0;
 
-// Per-call device status words: call id k owns word k mod kStatusRing.  A
-// call zeroes its word on its stream before its first pass; its kernels OR
+// Per-call device status words live in status.cu (a small module of their
+// own); kernels get their call's word as an argument and OR
 // kCallIndexFault / kCallSyncTimeout into it.
-__device__ unsigned int g_call_status[kStatusRing];
 
 __device__ __forceinline__ void raise_status(unsigned* status, unsigned bit) {
     if (status) atomicOr(status, bit);
@@ -2313,82 +2312,6 @@ int run_passes(uint8_t* data, const std::vector<Pass>& passes, ExecContext& ctx)
         }
     }
     if (ctx.profile) ctx.events_used = ev;
-    return 0;
-}
-
-// Fixed scratch for eithot_transpose_noalloc: a file-scope device array, so
-// the entry point never allocates.  Every GPU that loads the library holds
-// these bytes until the process exits; all calls share them.
-static __device__ __align__(256) uint8_t g_noalloc_scratch[kNoAllocScratchBytes];
-
-int noalloc_scratch(uint8_t** ptr, std::string* err) {
-    // In host code g_noalloc_scratch names a host-side stand-in; its device
-    // address is looked up on every call (a host-side table lookup, no
-    // allocation), with the caller's device current, so it follows the
-    // current device and context, also after a device reset.
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || p == nullptr) {
-        *err = std::string("cudaGetSymbolAddress(fixed scratch): ") + cudaGetErrorString(e);
-        return EITHOT_STATUS_CUDA;
-    }
-    *ptr = static_cast<uint8_t*>(p);
-    return 0;
-}
-
-namespace {
-std::atomic<uint64_t> g_next_call{1};
-}  // namespace
-
-uint64_t next_call_id() { return g_next_call.load(); }
-
-int begin_call(cudaStream_t stream, uint64_t* id, unsigned** status, std::string* err) {
-    // The device address is looked up on every call (a host-side table
-    // lookup), so it follows the current device and survives a device reset.
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_call_status);
-    if (e != cudaSuccess || p == nullptr) {
-        *err = std::string("cudaGetSymbolAddress(call status): ") + cudaGetErrorString(e);
-        return EITHOT_STATUS_CUDA;
-    }
-    const uint64_t k = g_next_call.fetch_add(1);
-    unsigned* word = static_cast<unsigned*>(p) + (k % kStatusRing);
-    e = cudaMemsetAsync(word, 0, sizeof(unsigned), stream);
-    if (e != cudaSuccess) {
-        *err = std::string("cudaMemsetAsync(call status): ") + cudaGetErrorString(e);
-        return EITHOT_STATUS_CUDA;
-    }
-    *id = k;
-    *status = word;
-    return 0;
-}
-
-int read_call_status(uint64_t id, cudaStream_t stream, unsigned* bits, std::string* err) {
-    const uint64_t next = g_next_call.load();
-    if (id == 0 || id >= next) {
-        *err = "unknown call id";
-        return EITHOT_STATUS_INVALID;
-    }
-    if (next - id > kStatusRing) {
-        *err = "the call's status word has been reused by a later call";
-        return EITHOT_STATUS_INVALID;
-    }
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_call_status);
-    unsigned v = 0;
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(&v, static_cast<unsigned*>(p) + (id % kStatusRing), sizeof(v), cudaMemcpyDeviceToHost,
-                            stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
-    if (e != cudaSuccess) {
-        *err = std::string("reading the call status: ") + cudaGetErrorString(e);
-        return EITHOT_STATUS_CUDA;
-    }
-    if (g_next_call.load() - id > kStatusRing) {  // reused while we read it
-        *err = "the call's status word has been reused by a later call";
-        return EITHOT_STATUS_INVALID;
-    }
-    *bits = v;
     return 0;
 }
 

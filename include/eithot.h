@@ -132,8 +132,11 @@ int eithot_transpose_ex(void* d_data, size_t capacity_bytes, int rank,
 /* No counterpart in the reference (whose kernels allocate managed temporaries
  * per pass).  As eithot_transpose, but it allocates nothing: the scratch the
  * staged passes and the padding moves need comes from a fixed 32 MiB device
- * array inside the library, which every GPU that loads the library holds
- * until the process exits.  For callers that may not allocate device memory
+ * array inside the library.  The array sits in a device module of its own:
+ * under CUDA's default lazy module loading a GPU holds it from the first
+ * eithot_transpose_noalloc call there until the process exits (with
+ * CUDA_MODULE_LOADING=EAGER, from when the library's device code is loaded,
+ * as for every module).  For callers that may not allocate device memory
  * during the call, e.g. because another allocator owns the device's memory.
  * Requests needing more than 32 MiB of scratch fail with EITHOT_EINVAL.  Each
  * call looks up the array's address on the current device (no allocation;
