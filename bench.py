@@ -68,11 +68,17 @@ def parse():
                     help="skip the 3001 x 4096 matrix and the reference's own GPU build")
     ap.add_argument("--dims", default=None,
                     help="comma-separated dims overriding the workload (small cases for ncu captures)")
-    ap.add_argument("--workload", default="transpose", choices=["transpose", "batched", "served", "study"],
+    ap.add_argument("--workload", default="transpose", choices=["transpose", "batched", "served", "study", "case"],
                     help="transpose: the default line; batched: 4096 mixed tensors through the batched form "
                          "against one call per tensor; served: Poisson-arriving requests through the server "
-                         "against serial calls; study: REORDER_TYPE pre/post/mixed and sub-tensor count sweeps")
+                         "against serial calls; study: REORDER_TYPE pre/post/mixed and sub-tensor count sweeps; "
+                         "case: one shape (--dims, --perm, --elem, --order, --knob) timed per pass")
     ap.add_argument("--count", type=int, default=0, help="tensors (batched) or requests (served); 0: default")
+    ap.add_argument("--perm", default=None, help="case: comma-separated 1-based permutation")
+    ap.add_argument("--elem", type=int, default=4, help="case: element size in bytes")
+    ap.add_argument("--order", type=int, default=0, help="case: reorder type (0 mixed, 1 pre, 2 post, 3 fewest passes)")
+    ap.add_argument("--alpha", type=float, default=0.05, help="case: extra-memory ratio")
+    ap.add_argument("--knob", action="append", default=[], help="case: tuning knob key=value (repeatable)")
     return ap.parse_args()
 
 
@@ -871,8 +877,64 @@ def run_study(args):
     return 0
 
 
+def run_case(args):
+    """One shape through the C ABI: W untimed transposes (the first checked
+    element by element on the device), then K transposes timed with CUDA
+    events on the launching stream, with per-pass times from the library's
+    profiler.  For ncu captures of one pass kind on a small case."""
+    import torch
+    import eithot_gb300 as E
+    dims = [int(x) for x in args.dims.split(",")]
+    perm = [int(x) for x in args.perm.split(",")]
+    elem = args.elem
+    for kv in args.knob:
+        k, v = kv.split("=")
+        E.tune_set(k, float(v))
+    dev = torch.device("cuda", 0)
+    n = math.prod(dims)
+    nbytes = n * elem
+    buf = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    E.fill_hash_ptr(buf.data_ptr(), n, elem, SEED, 0, stream.cuda_stream)
+
+    def step():
+        E.transpose_ptr(buf.data_ptr(), nbytes, dims, perm, elem, 1, args.alpha, args.order, stream.cuda_stream)
+
+    step()
+    bad, _ = E.check_hash_ptr(buf.data_ptr(), dims, perm, elem, SEED, stream.cuda_stream)
+    if bad or E.call_status(E.last_call(), stream.cuda_stream) != E.OK:
+        raise SystemExit("bench: case wrong (%d mismatching elements)" % bad)
+    for _ in range(max(0, args.warmup) - 1):
+        step()
+    torch.cuda.synchronize(dev)
+    E.profile_reset()
+    E.set_profiling(True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    E.set_profiling(False)
+    per = {}
+    for p in E.profile():
+        d = per.setdefault(p["name"], [0.0, 0, p["bytes"]])
+        d[0] += p["ms"]
+        d[1] += 1
+    ms = e0.elapsed_time(e1) / max(1, args.steps)
+    st = E.last_stats()
+    print(json.dumps({"workload": "case", "dims": dims, "perm": perm, "elem_bytes": elem, "order": args.order,
+                      "knobs": args.knob, "bit_exact": True, "ms": ms, "GBs": 2.0 * nbytes / (ms / 1e3) / 1e9,
+                      "passes": st["n_passes"], "launches": st["n_launches"], "workspace_bytes": st["workspace_bytes"],
+                      "per_pass": {k: {"ms": v[0] / v[1], "GBs": v[2] / (v[0] / v[1] / 1e3) / 1e9}
+                                   for k, v in per.items()}}), flush=True)
+    return 0
+
+
 def main():
     args = parse()
+    if args.workload == "case":
+        return run_case(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batched":
