@@ -29,7 +29,15 @@ CLI_PROGRAMS = {"test_inplace": "test_inplace.cpp", "Nd_estimation": "nd_estimat
 CLI_SCRIPTS = ["Statistic.py"]  # run by the reference's benchmark script beside the programs
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# Device code is stored uncompressed: the CUDA runtime inflates a compressed
+# fatbinary on the first use of its module in every process, which cost about
+# 40 ms of a process's first transpose on GB300 (49-53 ms against 8-11 ms
+# uncompressed; the library grows from 18 to 67 MB).
+NVCC_FLAGS = ARCH + ["--compress-mode=none"]
 CU_SOURCES = ["kernels.cu", "checks.cu", "perm.cu", "noalloc.cu", "status.cu"]
+# kernels.cu is compiled once for the host-side executor and once per unit
+# size (-DEITHOT_UNIT): one device module per unit size, loaded on first use.
+UNIT_SIZES = {"kernels.cu": [1, 2, 4, 8, 16]}
 CPP_SOURCES = ["plan.cpp", "lower.cpp", "search.cpp", "estimator.cpp", "capi.cpp", "batch.cpp", "server.cpp"]
 
 
@@ -66,13 +74,20 @@ def build(verbose: bool = False, force: bool = False) -> str:
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(ROOT, "include", "eithot.h"))
     jobs, objs = [], []
+    # objects built with other flags are rebuilt
+    stamp = os.path.join(BUILD, "nvcc_flags.txt")
+    flags_text = " ".join(NVCC_FLAGS)
+    if not os.path.exists(stamp) or open(stamp).read() != flags_text:
+        force = True
     for src in CU_SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src + ".o")
-        objs.append(o)
-        if force or _stale(o, [s] + headers):
-            jobs.append([nvcc] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                                         "-Xptxas", "-v" if verbose else "-O3"] + inc + ["-c", s, "-o", o])
+        for unit in [None] + UNIT_SIZES.get(src, []):
+            o = os.path.join(BUILD, src + (".u%d" % unit if unit else "") + ".o")
+            objs.append(o)
+            if force or _stale(o, [s] + headers):
+                jobs.append([nvcc] + NVCC_FLAGS + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+                                                   "-Xptxas", "-v" if verbose else "-O3"] +
+                            (["-DEITHOT_UNIT=%d" % unit] if unit else []) + inc + ["-c", s, "-o", o])
     for src in CPP_SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(BUILD, src + ".o")
@@ -85,7 +100,9 @@ def build(verbose: bool = False, force: bool = False) -> str:
             if verbose and out.strip():
                 print(out)
     if force or _stale(LIB, objs):
-        _run([nvcc] + ARCH + ["-shared", "-Xcompiler", "-fPIC", "-o", LIB] + objs)
+        _run([nvcc] + NVCC_FLAGS + ["-shared", "-Xcompiler", "-fPIC", "-o", LIB] + objs)
+        with open(stamp, "w") as fh:
+            fh.write(flags_text)
     os.makedirs(BINDIR, exist_ok=True)
     cli_jobs = []
     for name, src in CLI_PROGRAMS.items():

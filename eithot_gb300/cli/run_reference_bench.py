@@ -2,7 +2,7 @@
 drop-in programs.
 
     python eithot_gb300/cli/run_reference_bench.py --bench-dir DIR --task K
-        [--reorder-type T] [--out OUT] [--cases N]
+        [--reorder-type T] [--out OUT] [--cases N] [--test-inplace PATH]
 
 DIR holds the reference's Benchmark folder (Bench.sh and test_cases/, as
 the reference ships them).  The script expects test_inplace, Nd_estimation
@@ -15,6 +15,9 @@ OUT.  --reorder-type sets EITHOT_REORDER_TYPE for test_inplace (the
 reference's compile-time REORDER_TYPE: 0 mixed, 1 pre, 2 post; 3 this
 library's fewest-pass plans), as its experiment 6 asks.  --cases N keeps the
 first N lines of every case file (a bounded run; the default keeps all).
+--test-inplace PATH runs another test_inplace program in place of this
+library's (e.g. the reference's own build, to time both on one GPU); the
+estimator and the summary script stay this library's.
 Prints one JSON line: cases run, cases verified correct, the mean/std of
 the time and throughput columns per case file, and per case (in run order)
 its dims, sub-tensor count, size, verdict and the two times test_inplace
@@ -58,6 +61,7 @@ def main() -> int:
     ap.add_argument("--reorder-type", type=int, default=None)
     ap.add_argument("--out", default=None)
     ap.add_argument("--cases", type=int, default=0)
+    ap.add_argument("--test-inplace", default=None)
     args = ap.parse_args()
     for prog in ("test_inplace", "Nd_estimation", "Statistic.py"):
         if not os.path.exists(os.path.join(BIN, prog)):
@@ -74,13 +78,15 @@ def main() -> int:
                 with open(f, "w") as fh:
                     fh.writelines(lines)
         for prog in ("test_inplace", "Nd_estimation", "Statistic.py"):
-            os.symlink(os.path.join(BIN, prog), os.path.join(work, prog))
+            src = os.path.abspath(args.test_inplace) if prog == "test_inplace" and args.test_inplace else os.path.join(BIN, prog)
+            os.symlink(src, os.path.join(work, prog))
         env = dict(os.environ)
         if args.reorder_type is not None:
             env["EITHOT_REORDER_TYPE"] = str(args.reorder_type)
         p = subprocess.run(["bash", "Bench.sh", str(args.task)], cwd=work, env=env, capture_output=True, text=True)
         log = p.stdout + p.stderr
-        summary = {"task": args.task, "reorder_type": args.reorder_type, "exit": p.returncode,
+        summary = {"task": args.task, "reorder_type": args.reorder_type, "test_inplace": args.test_inplace or "this library's",
+                   "exit": p.returncode,
                    "cases": log.count("Execution Time:"), "correct": log.count("Correct transpose"),
                    "incorrect": log.count("Incorrect transpose"), "files": {}}
         summary["per_case"] = per_case(log)

@@ -58,6 +58,9 @@ size_t pass_workspace_ideal(const Pass& p, const DeviceCaps& caps);
 // permutation: its segment table and the saved blocks of its longest cycle
 // (ideal: of every cycle at once).
 int run_slab_perm(uint8_t* data, const Pass& p, ExecContext& ctx);
+// The run kernel of a slab permutation (whole elements of 1-16 bytes whose
+// padded slab fits one CTA); -1 when it does not apply.
+int try_slab_runs_pass(uint8_t* data, const Pass& p, ExecContext& ctx);
 int run_block_perm(uint8_t* data, const Pass& p, ExecContext& ctx);
 size_t block_perm_workspace(const Pass& p, bool ideal);
 

@@ -10,6 +10,14 @@
 // staged in global scratch by a grid-wide copy-in launch followed by a
 // copy-out launch, one group of items at a time (stream order replaces any
 // device-wide barrier).
+//
+// The file is compiled once per unit size U (-DEITHOT_UNIT=U: the kernels
+// and launchers of passes that move U-byte units, run_pass_unit_U) and once
+// without it (the host-side executor, which picks the unit of each pass and
+// calls into the matching object).  Each compilation is a device module of
+// its own, so a process only loads the device code of the unit sizes its
+// passes use (a module is loaded on its first use; loading all of this file's
+// kernels at once took about 8 ms on GB300, one unit's share 1.5-2 ms).
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
@@ -1200,9 +1208,11 @@ __global__ void __launch_bounds__(kThreads) k_col_group_bulk(ColOwnArgs a, Own o
 
 // Launch-time self-test of the bounded wait: one CTA waits on a counter
 // that nothing increments and must give up, counting one sync timeout.
+#ifndef EITHOT_UNIT
 __global__ void k_wait_selftest(unsigned* counters) {
     if (threadIdx.x == 0) group_wait(counters, 1u, counters + 1, 256, kDefaultSpinLimit, nullptr);
 }
+#endif
 
 // ---------------------------------------------------------------------------
 // Grid-staged row / column passes for items larger than shared memory.
@@ -1522,6 +1532,17 @@ int launch_slab(uint8_t* data, const Pass& p, ExecContext& ctx) {
         EI_CHECK(cudaGetLastError());
         ctx.launches++;
         return 0;
+    }
+    if (tuning().slab2d_runs && p.strip == p.elem && (p.elem == 1 || p.elem == 2 || p.elem == 4 || p.elem == 8 ||
+                                                      p.elem == 16) && (tuning().slab2d_runs == 2 || p.elem <= 2)) {
+        // The matrices as slabs of dims (C, R) written back in the order
+        // (R, C): the slab-permutation run kernel (whole 16-byte stores).
+        Pass q = p;
+        q.type = kSlabPerm;
+        q.nd_dims = {p.cols, p.rows};
+        q.nd_perm = {1, 0};
+        const int rc = try_slab_runs_pass(data, q, ctx);
+        if (rc >= 0) return rc;
     }
     SlabArgs a;
     a.base = data + p.offset;
@@ -1894,8 +1915,12 @@ cudaError_t launch_groups(void (*kernel)(ColOwnArgs, Own, GroupSync), size_t sme
 // ordered, each waits only for kernels that finish on their own.  (A stream
 // being captured into a graph is not ordered this way: the batched form,
 // which captures, never uses group passes.)
-std::mutex g_chain_mu;
-std::map<int, cudaEvent_t> g_chain;  // device -> event after its last group pass
+}  // namespace
+// One chain per process, shared by every unit's object (defined in the
+// host-side object).
+extern std::mutex g_chain_mu;
+extern std::map<int, cudaEvent_t> g_chain;  // device -> event after its last group pass
+namespace {
 
 class GroupChain {
 public:
@@ -1946,7 +1971,7 @@ private:
 // (so is the slot pitch) and the knob allows it.
 template <int US>
 bool bulk_ok(const ColOwnArgs& a, const Staging& st) {
-    if constexpr (US < 4) {
+    if constexpr (US < 16) {  // instantiated for 16-byte units only (fewer kernels to load)
         return false;
     } else {
         return st.dbuf && st.bulk && tuning().col_bulk && a.nstrips == 1 && a.w == a.E && a.pitch % 16 == 0 &&
@@ -1976,10 +2001,15 @@ int launch_col_group(uint8_t* data, const Pass& p, const Staging& st, const Own&
     GroupChain chain(ctx.stream);
     EI_CHECK(chain.before());
     cudaError_t e;
-    if (bulk_ok<US>(a, st))
-        e = kThreads % a.RU != 0 ? launch_groups(k_col_group_bulk<US, Own, false>, smem, a, own, gs, max_groups, ctx)
-                                 : launch_groups(k_col_group_bulk<US, Own, true>, smem, a, own, gs, max_groups, ctx);
-    else
+    bool bulk = false;
+    if constexpr (US == 16) {
+        if (bulk_ok<US>(a, st)) {
+            bulk = true;
+            e = kThreads % a.RU != 0 ? launch_groups(k_col_group_bulk<US, Own, false>, smem, a, own, gs, max_groups, ctx)
+                                     : launch_groups(k_col_group_bulk<US, Own, true>, smem, a, own, gs, max_groups, ctx);
+        }
+    }
+    if (!bulk)
         e = kThreads % a.RU != 0 ? launch_groups(k_col_group<US, Own, false>, smem, a, own, gs, max_groups, ctx)
                                  : launch_groups(k_col_group<US, Own, true>, smem, a, own, gs, max_groups, ctx);
     if (e == cudaErrorCooperativeLaunchTooLarge) {  // fewer CTAs resident than planned: no group form
@@ -2212,6 +2242,62 @@ uint64_t pass_unit(const uint8_t* data, const Pass& p, const DeviceCaps& caps) {
 
 }  // namespace
 
+// Reads and clears this object's counter `which` (0: index faults, 1: sync
+// timeouts).
+static int read_counter(int which, unsigned int* out) {
+    unsigned int v = 0, zero = 0;
+    cudaError_t e = which == 0 ? cudaMemcpyFromSymbol(&v, g_index_faults, sizeof(v))
+                               : cudaMemcpyFromSymbol(&v, g_sync_timeouts, sizeof(v));
+    if (e == cudaSuccess)
+        e = which == 0 ? cudaMemcpyToSymbol(g_index_faults, &zero, sizeof(zero))
+                       : cudaMemcpyToSymbol(g_sync_timeouts, &zero, sizeof(zero));
+    *out = v;
+    return e == cudaSuccess ? 0 : EITHOT_STATUS_CUDA;
+}
+
+#define EITHOT_CAT2(a, b) a##b
+#define EITHOT_CAT(a, b) EITHOT_CAT2(a, b)
+
+#ifdef EITHOT_UNIT
+
+int EITHOT_CAT(run_pass_unit_, EITHOT_UNIT)(uint8_t* data, const Pass& p, ExecContext& ctx) {
+    return run_pass_u<EITHOT_UNIT>(data, p, ctx);
+}
+
+int EITHOT_CAT(read_unit_counter_, EITHOT_UNIT)(int which, unsigned int* out) { return read_counter(which, out); }
+
+#else  // the host-side executor
+
+std::mutex g_chain_mu;
+std::map<int, cudaEvent_t> g_chain;
+
+#define EITHOT_UNIT_DECL(U)                                                          \
+    int run_pass_unit_##U(uint8_t* data, const Pass& p, ExecContext& ctx); \
+    int read_unit_counter_##U(int which, unsigned int* out);
+EITHOT_UNIT_DECL(1)
+EITHOT_UNIT_DECL(2)
+EITHOT_UNIT_DECL(4)
+EITHOT_UNIT_DECL(8)
+EITHOT_UNIT_DECL(16)
+
+// Sums and clears counter `which` over this object and every unit's (reading
+// a unit's counter loads that unit's device module).
+static int read_all_counters(int which, unsigned int* out) {
+    unsigned int total = 0, v = 0;
+    int rc = read_counter(which, &v);
+    total += v;
+    int (*const readers[])(int, unsigned int*) = {read_unit_counter_1, read_unit_counter_2, read_unit_counter_4,
+                                                   read_unit_counter_8, read_unit_counter_16};
+    for (auto* rd : readers) {
+        v = 0;
+        if (const int r = rd(which, &v)) rc = r;
+        total += v;
+    }
+    *out = total;
+    return rc;
+}
+
+
 size_t pass_workspace_bytes(const Pass& p, const DeviceCaps& caps) {
     const size_t cap = smem_cap_of(caps);
     switch (p.type) {
@@ -2292,11 +2378,11 @@ int run_passes(uint8_t* data, const std::vector<Pass>& passes, ExecContext& ctx)
         } else {
             const uint64_t U = pass_unit(data, p, ctx.caps);
             switch (U) {
-                case 16: rc = run_pass_u<16>(data, p, ctx); break;
-                case 8: rc = run_pass_u<8>(data, p, ctx); break;
-                case 4: rc = run_pass_u<4>(data, p, ctx); break;
-                case 2: rc = run_pass_u<2>(data, p, ctx); break;
-                default: rc = run_pass_u<1>(data, p, ctx); break;
+                case 16: rc = run_pass_unit_16(data, p, ctx); break;
+                case 8: rc = run_pass_unit_8(data, p, ctx); break;
+                case 4: rc = run_pass_unit_4(data, p, ctx); break;
+                case 2: rc = run_pass_unit_2(data, p, ctx); break;
+                default: rc = run_pass_unit_1(data, p, ctx); break;
             }
         }
         if (rc) return rc;
@@ -2315,21 +2401,9 @@ int run_passes(uint8_t* data, const std::vector<Pass>& passes, ExecContext& ctx)
     return 0;
 }
 
-int read_index_faults(unsigned int* out) {
-    unsigned int v = 0, zero = 0;
-    cudaError_t e = cudaMemcpyFromSymbol(&v, g_index_faults, sizeof(v));
-    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_index_faults, &zero, sizeof(zero));
-    *out = v;
-    return e == cudaSuccess ? 0 : EITHOT_STATUS_CUDA;
-}
+int read_index_faults(unsigned int* out) { return read_all_counters(0, out); }
 
-int read_sync_timeouts(unsigned int* out) {
-    unsigned int v = 0, zero = 0;
-    cudaError_t e = cudaMemcpyFromSymbol(&v, g_sync_timeouts, sizeof(v));
-    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_sync_timeouts, &zero, sizeof(zero));
-    *out = v;
-    return e == cudaSuccess ? 0 : EITHOT_STATUS_CUDA;
-}
+int read_sync_timeouts(unsigned int* out) { return read_all_counters(1, out); }
 
 int run_wait_selftest(unsigned int* timeouts, std::string* err) {
     unsigned int pending = 0;  // timeouts of earlier launches are cleared, not reported here
@@ -2368,5 +2442,7 @@ bool query_caps(int device, DeviceCaps* caps, std::string* err) {
     *caps = c;
     return true;
 }
+
+#endif  // EITHOT_UNIT
 
 }  // namespace eithot

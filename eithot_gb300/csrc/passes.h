@@ -95,8 +95,12 @@ struct Tuning {
     int cycle_moves = 1;     // fewest-pass plans may move blocks along cycles (host-built segment tables)
     int slab_perm = 1;       // fewest-pass plans: 0 no slab permutations, 1 cost model, 2 preferred
     int slab_runs = 1;       // slab permutations of 1-16 byte elements: runs of outputs per thread, padded rows
-                             // (1: runs whose outputs share offsets read them from a host table; 2: never)
+                             // (1: runs whose outputs share offsets read them from a host table, runs that
+                             // wrap the fastest output axis once step it with one jump; 2: every run steps
+                             // through the axes element by element)
     int slab_prefetch = 1;   // slab permutations at one CTA per SM: the next slab prefetched into registers
+    int slab2d_runs = 1;     // slab transposes of whole elements beyond the packed sizes through the slab-
+                             // permutation run kernel: 0 never, 1 elements of 1-2 bytes, 2 of 1-16 bytes
     int col_bulk = 0;        // group form: double-buffered CTAs staging their slots with bulk copies (slower on GB300)
     int batch_graph = 1;     // batched form: a run repeating the previous run's buffers replays a CUDA graph
 };

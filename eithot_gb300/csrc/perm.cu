@@ -149,6 +149,15 @@ struct SlabRunArgs {
     // first element, whose address only axes m.. determine (through the
     // run index times K / P).
     uint32_t aligned, m_axis, nhi, rmul;
+    // Otherwise, when the fastest output dim is at least K, a run wraps that
+    // axis at most once (`wrap`): its elements are found by stepping axis 0
+    // with one jump.
+    uint32_t wrap;
+    // Rows of 1- or 2-byte units (odd row lengths): the slab is read in
+    // 4-byte words (every slab 4-byte aligned, its size a multiple of 4) and
+    // their bytes placed into the padded rows.
+    uint32_t stage_words;
+    FastDiv32 div_rowb;       // slab byte -> (row, byte of the row)
     FastDiv32 hod[kMaxAxes];  // output dims m.., output order
     uint32_t hstep[kMaxAxes];
     uint32_t delta[16];
@@ -161,8 +170,35 @@ template <> struct ElemT<4> { using T = uint32_t; };
 template <> struct ElemT<8> { using T = uint2; };
 template <> struct ElemT<16> { using T = uint4; };
 
+__device__ __forceinline__ void stage_words(const SlabRunArgs& a, uint8_t* smem, const uint8_t* slab) {
+    const uint32_t words = static_cast<uint32_t>(a.slab_bytes / 4);
+    for (uint32_t x = threadIdx.x; x < words; x += blockDim.x) {
+        const uint32_t v = reinterpret_cast<const uint32_t*>(slab)[x];
+        uint32_t r, c;
+        a.div_rowb.divmod(x * 4, r, c);
+        if ((c & 3) == 0 && c + 4 <= a.row_bytes) {
+            *reinterpret_cast<uint32_t*>(smem + r * a.pitch + c) = v;
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                smem[r * a.pitch + c] = static_cast<uint8_t>(v >> (8 * k));
+                if (++c == a.row_bytes) {
+                    c = 0;
+                    ++r;
+                }
+            }
+        }
+    }
+}
+
 template <int SU>
 __device__ __forceinline__ void stage_rows(const SlabRunArgs& a, uint8_t* smem, const uint8_t* slab) {
+    if constexpr (SU < 4) {
+        if (a.stage_words) {
+            stage_words(a, smem, slab);
+            return;
+        }
+    }
     const uint32_t upr = a.row_bytes / SU;
     const uint32_t total = a.nrows * upr;
     for (uint32_t x = threadIdx.x; x < total; x += blockDim.x) {
@@ -234,6 +270,37 @@ __device__ __forceinline__ void write_runs(const SlabRunArgs& a, const uint8_t* 
         }
         return;
     }
+    if (a.wrap) {
+        // A run crosses at most one end of the fastest output axis: its
+        // elements lie step[0] apart, with one jump (the carry into the
+        // next axes, found once per run) after the first w of them.
+        for (uint32_t g = threadIdx.x; g < runs; g += blockDim.x) {
+            uint32_t c[kMaxAxes];
+            const uint32_t addr = run_start(a, g * K, c);
+            const uint32_t w = a.odim[0] - c[0];
+            uint32_t jump = 0;
+            if (w < K) {
+                jump = 0u - a.odim[0] * a.step[0];
+                bool carry = true;
+#pragma unroll
+                for (int j = 1; j < kMaxAxes; ++j) {
+                    if (carry && j < static_cast<int>(a.q)) {
+                        if (c[j] + 1 < a.odim[j]) {
+                            jump += a.step[j];
+                            carry = false;
+                        } else {
+                            jump -= (a.odim[j] - 1) * a.step[j];
+                        }
+                    }
+                }
+            }
+            T v[K];
+#pragma unroll
+            for (int t = 0; t < K; ++t)
+                v[t] = *reinterpret_cast<const T*>(sm + addr + t * a.step[0] + (static_cast<uint32_t>(t) >= w ? jump : 0u));
+            store_run<E, V>(slab + static_cast<uint64_t>(g) * V, v);
+        }
+    } else {
     for (uint32_t g = threadIdx.x; g < runs; g += blockDim.x) {
         uint32_t c[kMaxAxes];
         uint32_t addr = run_start(a, g * K, c);
@@ -258,6 +325,7 @@ __device__ __forceinline__ void write_runs(const SlabRunArgs& a, const uint8_t* 
             }
         }
         store_run<E, V>(slab + static_cast<uint64_t>(g) * V, v);
+    }
     }
     for (uint32_t o = runs * K + threadIdx.x; o < a.count; o += blockDim.x) {
         uint32_t c[kMaxAxes];
@@ -592,6 +660,8 @@ int try_slab_runs(uint8_t* data, const Pass& p, uint64_t count, ExecContext& ctx
     a.su = static_cast<uint32_t>(pow2_unit({addr, row_bytes, pitch, slab_bytes}));
     a.chunks16 = pow2_unit({addr, row_bytes, slab_bytes}) == 16;
     a.div_upr = FastDiv32::make(row_bytes / a.su);
+    a.div_rowb = FastDiv32::make(row_bytes);
+    a.stage_words = a.su < 4 && addr % 4 == 0 && slab_bytes % 4 == 0 && tuning().slab_runs == 1;
     // input strides: axis 0 moves E bytes inside a row, axis i >= 1 moves
     // rows (prod of dims 1..i-1 of them) of `pitch` bytes
     std::vector<uint64_t> istep(q);
@@ -607,7 +677,10 @@ int try_slab_runs(uint8_t* data, const Pass& p, uint64_t count, ExecContext& ctx
         a.odim[j] = static_cast<uint32_t>(d);
         a.step[j] = static_cast<uint32_t>(istep[p.nd_perm[j]]);
     }
-    if (tuning().slab_runs == 1) set_aligned_runs(&a, V / E);
+    if (tuning().slab_runs == 1) {
+        set_aligned_runs(&a, V / E);
+        a.wrap = !a.aligned && a.odim[0] >= V / E;
+    }
     switch (E) {
         case 1: return dispatch_v<1>(a, smem, V, ctx);
         case 2: return dispatch_v<2>(a, smem, V, ctx);
@@ -618,6 +691,13 @@ int try_slab_runs(uint8_t* data, const Pass& p, uint64_t count, ExecContext& ctx
 }
 
 }  // namespace
+
+int try_slab_runs_pass(uint8_t* data, const Pass& p, ExecContext& ctx) {
+    uint64_t count = 1;
+    for (auto d : p.nd_dims) count *= d;
+    if (count >= (uint64_t(1) << 31) || !tuning().slab_runs) return -1;
+    return try_slab_runs(data, p, count, ctx);
+}
 
 int run_slab_perm(uint8_t* data, const Pass& p, ExecContext& ctx) {
     const int q = static_cast<int>(p.nd_dims.size());

@@ -3,12 +3,10 @@
 // Call id k owns word k mod kStatusRing of a file-scope device array; a call
 // zeroes its word on its stream before its first pass and its kernels OR
 // kCallIndexFault / kCallSyncTimeout into it through the pointer they are
-// given.  The host looks the array up on every call (cudaGetSymbolAddress).
-// Such a lookup loads the whole device module that holds the variable,
-// every function of it included; kept beside the kernels (a 10 MB module of
-// several hundred kernels) it cost about 49 ms on GB300 on a process's first
-// transpose, while a kernel launch alone loads just that function (about 1
-// ms for the first one of a module).  Here the lookup loads this module only.
+// given.  The host looks the array up on every call (cudaGetSymbolAddress),
+// which needs the module holding it loaded on the device; kept in a small
+// module of its own, that lookup and the status reads never depend on the
+// module of the kernels.
 #include <cuda_runtime.h>
 
 #include <atomic>

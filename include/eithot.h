@@ -314,7 +314,15 @@ int eithot_estimate_report(int rank, const int64_t* dims, const int* perm_1based
  *                 permutations, 1 cost model (default), 2 preferred
  *   "slab_runs"   1 slab permutations of 1-16 byte elements write runs of
  *                 consecutive outputs per thread from rows staged at a padded
- *                 pitch (default), 0 one divide chain per element
+ *                 pitch, with the offsets of a run's outputs from a host-built
+ *                 table where every run shares them, else stepping the fastest
+ *                 output axis with one jump where a run wraps it at most once
+ *                 (default); 2 the runs step through every axis per element;
+ *                 0 one divide chain per element
+ *   "slab2d_runs" slab transposes of whole elements beyond the sizes packed
+ *                 several matrices to a CTA run through the slab-permutation
+ *                 run kernel: 0 never, 1 for 1- and 2-byte elements
+ *                 (default), 2 for 1- to 16-byte elements
  *   "slab_prefetch" 1 slab permutations whose padded slab leaves one CTA per
  *                 SM prefetch the next slab into registers (up to 128 KB),
  *                 0 not
@@ -323,7 +331,8 @@ int eithot_estimate_report(int rank, const int64_t* dims, const int* perm_1based
  *                 table is copied from the host each call), 0 not
  *   "col_bulk"    1 group passes may run double-buffered with their row pieces
  *                 staged by bulk copies (cp.async.bulk, mbarrier completion)
- *                 when every piece is whole 16-byte-aligned elements, 0 not
+ *                 when the pass moves 16-byte units and every piece is whole
+ *                 16-byte-aligned elements, 0 not
  *                 (default; measured slower than three single-buffered CTAs
  *                 per SM on GB300)
  *   "l2_prefetch" 1 single-buffered group passes prefetch the next item into

@@ -2,7 +2,9 @@
 (eithot_gb300/bin/Nd_estimation and eithot_gb300/bin/test_inplace): same
 argv, same stdout lines, same files appended in the working directory."""
 import json
+import math
 import os
+import re
 import subprocess
 
 import pytest
@@ -71,19 +73,29 @@ def test_cli_usage_errors(E, tmp_path):
     [16, 3001, 64, 3, 1, 2, 2, 1, 0.05],               # 16-bit elements (beyond the reference)
     [6, 4, 3401, 3, 2, 1, 1, 2, 0.01]])                # 8-bit elements, sub-tensors
 def test_test_inplace_runs_and_verifies(E, tmp_path, args):
+    """Every line the reference's driver prints (ITNT/src/test_inplace.cpp:32-76),
+    compared exactly except the two measured times, whose format is checked;
+    the two files it appends to hold the total time and 2*bytes/1e6/time."""
     p = run("test_inplace", args, tmp_path)
     assert p.returncode == 0, p.stdout + p.stderr
     lines = p.stdout.splitlines()
     rank = (len(args) - 3) // 2
-    assert lines[0].startswith("%dD Inplace " % rank) and lines[0].endswith(" transpose")
-    assert lines[1] == "number of sub_tensors = %d" % args[2 * rank + 1]
-    assert lines[2].startswith("Dims = " + " ".join(str(a) for a in args[:rank]) + ", Data size = ")
-    assert lines[3:5] == ["Inplace transpose verify_inplace", "Correct transpose"]
-    assert lines[5].startswith("Execution Time without h2d2h: ") and lines[6].startswith("Execution Time: ")
-    t = float(lines[6].split(": ")[1].rstrip("ms"))
+    dims, perm, elem = args[:rank], args[rank:2 * rank], args[2 * rank]
+    perm_int = sum(10 ** i * perm[rank - i - 1] for i in range(rank))
+    size = math.prod(dims) * elem
+    assert len(lines) == 7, lines
+    assert lines[:5] == ["%dD Inplace %d transpose" % (rank, perm_int),
+                         "number of sub_tensors = %d" % args[2 * rank + 1],
+                         "Dims = %s, Data size = %.5f GB" % (" ".join(str(d) for d in dims), size / 1e9),
+                         "Inplace transpose verify_inplace", "Correct transpose"]
+    assert re.fullmatch(r"Execution Time without h2d2h: -?\d+\.\d{5}ms", lines[5]), lines[5]
+    m = re.fullmatch(r"Execution Time: (\d+\.\d{5})ms", lines[6])
+    assert m, lines[6]
+    t = float(m.group(1))
     assert (tmp_path / "inplace_bench.txt").read_text() == "%.5f\n" % t
-    thr = float((tmp_path / "inplace_bench_throughput.txt").read_text())
-    assert thr > 0
+    thr = (tmp_path / "inplace_bench_throughput.txt").read_text()
+    assert re.fullmatch(r"\d+\.\d{5}\n", thr)
+    assert abs(float(thr) - size * 2 / 1e6 / t) <= 1e-4 * float(thr) + 1e-5
 
 
 @pytest.mark.gpu

@@ -146,9 +146,9 @@ def test_group_arrivals_and_residency(E, tuned, relaxed, per_sm):
 @pytest.mark.parametrize("per_sm", [1, 2])
 def test_group_pass_with_bulk_copies(E, tuned, per_sm):
     """Double-buffered group column passes whose row pieces are staged by
-    bulk copies completing on mbarriers (whole 16-byte-aligned elements),
-    c2r and r2c, 16-, 4- and 32-byte elements; shapes whose pieces do not
-    qualify fall back to the cp.async form."""
+    bulk copies completing on mbarriers (whole 16-byte-aligned elements
+    moved in 16-byte units), c2r and r2c, 16-, 4- and 32-byte elements;
+    shapes whose pieces do not qualify fall back to the cp.async form."""
     tuned(col_form=2, dbuf=1, col_bulk=1, group_per_sm=per_sm)
     for variant in (1, 2):
         E.tune_set("variant", variant)
