@@ -122,7 +122,9 @@ int apply_knob(eithot::Tuning& t, const char* key, double value) {
         if (value < 0 || value > 100000) return fail(EITHOT_EINVAL, "sync_sleep_ns must be 0..100000");
         t.sync_sleep_ns = static_cast<int>(value);
     } else if (k == "cycle_moves") {
-        t.cycle_moves = value != 0.0 ? 1 : 0;
+        const int v = static_cast<int>(value);
+        if (v < 0 || v > 2) return fail(EITHOT_EINVAL, "cycle_moves must be 0, 1 or 2");
+        t.cycle_moves = v;
     } else if (k == "slab_perm") {
         const int v = static_cast<int>(value);
         if (v < 0 || v > 2) return fail(EITHOT_EINVAL, "slab_perm must be 0, 1 or 2");

@@ -92,7 +92,8 @@ struct Tuning {
                              // arriving CTA has landed in shared memory before it arrives)
     int group_per_sm = 0;    // group form: 0 cost model, 1 or 2 CTAs per SM
     int l2_prefetch = 0;     // group form, single-buffered: prefetch the next item into L2 (slower on GB300)
-    int cycle_moves = 1;     // fewest-pass plans may move blocks along cycles (host-built segment tables)
+    int cycle_moves = 1;     // fewest-pass plans may move blocks along cycles (host-built segment tables):
+                             // 0 no, 1 cost model, 2 preferred
     int slab_perm = 1;       // fewest-pass plans: 0 no slab permutations, 1 cost model, 2 preferred
     int slab_runs = 1;       // slab permutations of 1-16 byte elements: runs of outputs per thread, padded rows
                              // (1: runs whose outputs share offsets read them from a host table, runs that

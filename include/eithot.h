@@ -326,9 +326,11 @@ int eithot_estimate_report(int rank, const int64_t* dims, const int* perm_1based
  *   "slab_prefetch" 1 slab permutations whose padded slab leaves one CTA per
  *                 SM prefetch the next slab into registers (up to 128 KB),
  *                 0 not
- *   "cycle_moves" 1 plans for the fewest passes (EITHOT_ORDER_FEWEST) may
- *                 permute blocks along the permutation's cycles (the segment
- *                 table is copied from the host each call), 0 not
+ *   "cycle_moves" plans for the fewest passes (EITHOT_ORDER_FEWEST): 1 may
+ *                 permute blocks along the permutation's cycles where the
+ *                 cost model expects it to pay (the segment table is copied
+ *                 from the host each call; default), 2 prefer such moves,
+ *                 0 never
  *   "col_bulk"    1 group passes may run double-buffered with their row pieces
  *                 staged by bulk copies (cp.async.bulk, mbarrier completion)
  *                 when the pass moves 16-byte units and every piece is whole

@@ -74,7 +74,7 @@ def test_every_knob_round_trips(E):
 
 
 @pytest.mark.parametrize("key,value", [("max_cluster", 3), ("variant", 3), ("col_form", 5), ("group_per_sm", 7),
-                                       ("sync_sleep_ns", -1), ("sync_spin_limit", -1), ("slab_perm", 3), ("slab_runs", 3), ("slab2d_runs", 3), ("col_chunk", 100), ("no_such_knob", 1)])
+                                       ("sync_sleep_ns", -1), ("sync_spin_limit", -1), ("slab_perm", 3), ("slab_runs", 3), ("slab2d_runs", 3), ("cycle_moves", 3), ("col_chunk", 100), ("no_such_knob", 1)])
 def test_invalid_knob_values_are_refused(E, key, value):
     old = E.tune_get(key) if key != "no_such_knob" else None
     with pytest.raises(E.EithotError) as ei:

@@ -87,7 +87,17 @@ def test_every_permutation(E, rank, slab_kernel):
     ([2, 3, 5, 7, 11, 13, 2], [7, 1, 6, 2, 5, 3, 4], 1, None),
     ([4096, 33, 65], [1, 3, 2], 1, None), ([3001, 4096], [2, 1], 4, None), ([4, 2001, 819, 2], [1, 3, 2, 4], 4, None)])
 def test_named_shapes(E, dims, perm, elem, expect, slab_kernel):
-    run_case(E, dims, perm, elem, expect=expect)
+    """Named shapes; where a cycle-following block permutation is the kind
+    under test, such moves are preferred (knob cycle_moves=2): at these sizes
+    the cost model would rather stream (a cycle segment is walked by one CTA
+    at about 2.6 GB/s)."""
+    old = E.tune_get("cycle_moves")
+    if expect == "cycle-perm":
+        E.tune_set("cycle_moves", 2)
+    try:
+        run_case(E, dims, perm, elem, expect=expect)
+    finally:
+        E.tune_set("cycle_moves", old)
 
 
 @pytest.mark.parametrize("elem", [1, 2, 4, 8, 16, 24])
@@ -132,10 +142,16 @@ def test_slab_permutations_aligned_runs(E, elem, slab_kernel):
 def test_cycle_permutation_in_chunks(E):
     """A block permutation (32 KB blocks over (301, 64, 4): 628 segments in
     44 cycles, 20.6 MB of saved blocks at once) given an 8 MB workspace: the
-    segments run in several chunks of whole cycles, two launches each."""
+    segments run in several chunks of whole cycles, two launches each
+    (cycle moves preferred, knob cycle_moves=2)."""
     dims, perm, elem = [16, 301, 1024, 64, 4], [5, 3, 1, 4, 2], 2
-    assert E.workspace_size(dims, perm, elem, 1, 0.05, FEWEST) > 16 << 20
-    st = run_case(E, dims, perm, elem, alpha=0.05, workspace=8 << 20, expect="cycle-perm")
+    old = E.tune_get("cycle_moves")
+    E.tune_set("cycle_moves", 2)
+    try:
+        assert E.workspace_size(dims, perm, elem, 1, 0.05, FEWEST) > 16 << 20
+        st = run_case(E, dims, perm, elem, alpha=0.05, workspace=8 << 20, expect="cycle-perm")
+    finally:
+        E.tune_set("cycle_moves", old)
     assert st["workspace_bytes"] == 8 << 20
     assert st["n_launches"] >= st["n_passes"] + 4
 
