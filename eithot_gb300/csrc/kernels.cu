@@ -1481,7 +1481,6 @@ cudaError_t launch_clusters(void (*kernel)(KArgs...), int K, size_t smem, uint64
 
 // Rows larger than this leave no room for a second CTA or item buffer on
 // the SM; they prefetch the next row into registers instead.
-constexpr size_t kRowSoloMinBytes = 110 * 1024;
 // Rows this short are staged k at a time (k = kRowBlockBytes / row bytes,
 // at least kRowBlockMinRows) by k_row_block.
 constexpr uint64_t kRowBlockBytes = 48 * 1024;
@@ -1687,7 +1686,8 @@ int launch_row(uint8_t* data, const Pass& p, const FnOnChip& fn, const Fn64& fn6
     constexpr int kRegs = 256 / US;  // 64 registers of prefetched data per thread
     if constexpr (US >= 4 && !kScatter) {
         const uint64_t units = static_cast<uint64_t>(a.cols) * a.upw;
-        if (st.K == 1 && !st.dbuf && a.flat && a.nstrips == 1 && smem > kRowSoloMinBytes &&
+        if (st.K == 1 && !st.dbuf && a.flat && a.nstrips == 1 &&
+            smem > static_cast<size_t>(tuning().row_solo_kb) * 1024 &&
             units <= static_cast<uint64_t>(kRegs) * kThreads && tuning().row_prefetch) {
             const void* k = reinterpret_cast<const void*>(&k_row_solo<US, FnOnChip, kRegs>);
             EI_CHECK(prep_smem(k, smem));

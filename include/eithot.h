@@ -319,6 +319,10 @@ int eithot_estimate_report(int rank, const int64_t* dims, const int* perm_1based
  *                 output axis with one jump where a run wraps it at most once
  *                 (default); 2 the runs step through every axis per element;
  *                 0 one divide chain per element
+ *   "row_solo_kb" rows held whole by one CTA that are larger than this many
+ *                 KB (16..128, default 110) run one CTA per SM with the next
+ *                 row prefetched into registers; smaller ones two or more CTAs
+ *                 per SM
  *   "slab2d_runs" slab transposes of whole elements beyond the sizes packed
  *                 several matrices to a CTA run through the slab-permutation
  *                 run kernel: 0 never, 1 for 1- and 2-byte elements
