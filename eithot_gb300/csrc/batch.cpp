@@ -12,7 +12,12 @@
 // (eithot_tune_shape_set, e.g. from the autotuner) is planned and run with
 // them.  Work is issued round-robin over the lanes so that every lane has
 // work queued from the start; a run that repeats the previous run's buffers
-// is captured once into a CUDA graph and replayed from then on.
+// is captured once into a CUDA graph and replayed from then on.  Small
+// tensors whose whole permutation fits one CTA's shared memory skip the lanes:
+// one persistent launch takes them from a device queue (an atomic counter over
+// a table of their slab-permutation arguments, in device memory the batch
+// owns), so a thousand 4-200 KB tensors cost one launch instead of one or more
+// each.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -42,8 +47,18 @@ struct eithot_batch {
         size_t scratch = 0;    // workspace its passes use
         double bytes = 0;      // tensor bytes
         int lane = 0;
+        bool queued = false;   // permuted by the queue launch (one whole-tensor slab permutation)
+        Pass whole;            // that slab permutation
     };
     std::vector<Item> items;
+    // the queue of whole-tensor slab permutations
+    std::vector<int> queue;            // tensors permuted by the queue launch
+    uint8_t* d_queue = nullptr;        // entries, then the counter (device memory the batch owns)
+    size_t queue_entry = 0, queue_smem = 0;
+    uint32_t queue_n = 0;              // entries uploaded by the last direct run
+    std::vector<int> queue_fallback;   // queued tensors whose entry did not apply on those buffers
+    cudaStream_t qstream = nullptr;
+    cudaEvent_t qdone = nullptr;
     std::vector<std::vector<int>> lane_items;
     std::vector<size_t> lane_offset, lane_bytes;
     size_t workspace = 0;
@@ -65,6 +80,8 @@ struct eithot_batch {
 namespace {
 
 constexpr int kMaxLanes = 16;
+constexpr size_t kQueueBytes = 192 * 1024;   // tensors up to this size may go to the queue
+constexpr size_t kQueueSmem = 200 * 1024;    // shared memory of one queue entry at most
 
 int make_streams(eithot_batch* b) {
     if (!b->streams.empty()) return EITHOT_OK;
@@ -78,8 +95,44 @@ int make_streams(eithot_batch* b) {
         b->streams.push_back(s);
         b->done.push_back(ev);
     }
+    if (e == cudaSuccess && !b->queue.empty()) {
+        // the queue's table lives in device memory the batch owns, allocated
+        // at its first run (planning touches no device memory)
+        void* p = nullptr;
+        e = cudaMalloc(&p, b->queue.size() * b->queue_entry + 256);
+        b->d_queue = static_cast<uint8_t*>(p);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->qstream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->qdone, cudaEventDisableTiming);
+    }
     if (e != cudaSuccess) return fail(EITHOT_ECUDA, std::string("batch streams: ") + cudaGetErrorString(e));
     return EITHOT_OK;
+}
+
+// Builds the queue's entries for these buffers and uploads them (stream
+// ordered on the queue stream, after the previous run's queue launch); a
+// queued tensor whose entry does not apply on its buffer is run through its
+// planned passes instead (queue_fallback).
+int upload_queue(eithot_batch* b, void* const* d_data) {
+    b->queue_fallback.clear();
+    std::vector<uint8_t> host(b->queue.size() * b->queue_entry);
+    uint32_t n = 0;
+    for (int t : b->queue) {
+        size_t smem = 0;
+        ScopedTuning scope(b->items[t].tuning);
+        if (slab_queue_entry(static_cast<uint8_t*>(d_data[t]), b->items[t].whole, b->caps,
+                             host.data() + n * b->queue_entry, &smem) && smem <= b->queue_smem) {
+            ++n;
+        } else {
+            b->queue_fallback.push_back(t);
+        }
+    }
+    b->queue_n = n;
+    if (n == 0) return EITHOT_OK;
+    // pageable source: the call returns once the bytes are staged
+    const cudaError_t e = cudaMemcpyAsync(b->d_queue, host.data(), n * b->queue_entry, cudaMemcpyHostToDevice, b->qstream);
+    if (e != cudaSuccess) return fail(EITHOT_ECUDA, std::string("batch queue upload: ") + cudaGetErrorString(e));
+    return cudaStreamSynchronize(b->qstream) == cudaSuccess ? EITHOT_OK
+                                                             : fail(EITHOT_ECUDA, "batch queue upload: synchronise");
 }
 
 // Forks the lanes from `from`, issues every tensor's passes on its lane
@@ -96,6 +149,33 @@ int enqueue(eithot_batch* b, void* const* d_data, uint8_t* ws, cudaStream_t from
     int rc = EITHOT_OK;
     std::string err;
     b->last_launches = 0;
+    bool qforked = false;
+    if (e == cudaSuccess && b->queue_n > 0) {
+        e = cudaStreamWaitEvent(b->qstream, b->fork, 0);
+        qforked = e == cudaSuccess;
+        if (qforked) {
+            ExecContext ctx;
+            ctx.caps = b->caps;
+            ctx.stream = b->qstream;
+            rc = launch_slab_queue(b->d_queue, b->queue_n, reinterpret_cast<unsigned*>(b->d_queue + b->queue.size() * b->queue_entry),
+                                   b->queue_smem, ctx);
+            if (rc) err = "queue: " + ctx.err;
+            b->last_launches += ctx.launches;
+        }
+    }
+    // queued tensors whose entry did not apply on these buffers: their own passes, on lane 0
+    for (size_t f = 0; f < b->queue_fallback.size() && e == cudaSuccess && rc == EITHOT_OK && lanes > 0; ++f) {
+        const int t = b->queue_fallback[f];
+        ScopedTuning scope(b->items[t].tuning);
+        ExecContext ctx;
+        ctx.caps = b->caps;
+        ctx.stream = b->streams[0];
+        ctx.scratch = ws ? ws + b->lane_offset[0] : nullptr;
+        ctx.scratch_bytes = ws ? b->lane_bytes[0] : 0;
+        rc = run_passes(static_cast<uint8_t*>(d_data[t]), b->items[t].passes, ctx);
+        if (rc) err = "tensor " + std::to_string(t) + ": " + ctx.err;
+        b->last_launches += ctx.launches;
+    }
     size_t rounds = 0;
     for (const auto& li : b->lane_items) rounds = std::max(rounds, li.size());
     for (size_t r = 0; r < rounds && e == cudaSuccess && rc == EITHOT_OK; ++r) {
@@ -117,6 +197,11 @@ int enqueue(eithot_batch* b, void* const* d_data, uint8_t* ws, cudaStream_t from
         if (!forked[l]) continue;
         const cudaError_t j = cudaEventRecord(b->done[l], b->streams[l]);
         if (j == cudaSuccess) cudaStreamWaitEvent(from, b->done[l], 0);
+        if (e == cudaSuccess) e = j;
+    }
+    if (qforked) {
+        const cudaError_t j = cudaEventRecord(b->qdone, b->qstream);
+        if (j == cudaSuccess) cudaStreamWaitEvent(from, b->qdone, 0);
         if (e == cudaSuccess) e = j;
     }
     if (rc) return fail(rc, err);
@@ -201,7 +286,35 @@ int eithot_batch_create(int count, const int* ranks, const int64_t* dims, const 
         it.need = static_cast<size_t>(plan.padded_volume) * elem_sizes[t];
         it.bytes = static_cast<double>(plan.volume) * static_cast<double>(elem_sizes[t]);
         it.scratch = choose_workspace(it.passes, b->caps, alpha, it.bytes);
+        // a small tensor whose whole permutation fits one CTA goes to the queue
+        if (b->tuning.batch_queue && num_sub_tensors <= 1 && !it.passes.empty() && ranks[t] <= 8 &&
+            it.bytes <= static_cast<double>(kQueueBytes)) {
+            Pass w;
+            w.type = kSlabPerm;
+            w.batches = 1;
+            w.elem = elem_sizes[t];
+            w.strip = elem_sizes[t];
+            for (int a = 0; a < ranks[t]; ++a) {
+                w.nd_dims.push_back(static_cast<uint64_t>(dims[off - ranks[t] + a]));
+                w.nd_perm.push_back(perms_1based[off - ranks[t] + a] - 1);
+            }
+            w.rows = static_cast<uint64_t>(it.bytes / static_cast<double>(elem_sizes[t]));
+            w.what = "queue slab-perm";
+            std::vector<uint8_t> entry(slab_queue_entry_bytes());
+            size_t smem = 0;
+            // a 256-byte aligned stand-in address: the entry is only sized here
+            if (slab_queue_entry(reinterpret_cast<uint8_t*>(uintptr_t(256)), w, b->caps, entry.data(), &smem) &&
+                smem <= kQueueSmem) {
+                it.queued = true;
+                it.whole = w;
+                b->queue.push_back(t);
+                b->queue_smem = std::max(b->queue_smem, smem);
+            }
+        }
     }
+    b->queue_entry = (slab_queue_entry_bytes() + 15) / 16 * 16;
+    // largest first: the counter hands entries out in table order
+    std::stable_sort(b->queue.begin(), b->queue.end(), [&](int x, int y) { return b->items[x].bytes > b->items[y].bytes; });
     // largest first onto the least-loaded lane
     const int lanes = std::max(1, std::min(count, kMaxLanes));
     std::vector<int> order(count);
@@ -211,6 +324,7 @@ int eithot_batch_create(int count, const int* ranks, const int64_t* dims, const 
     b->lane_items.assign(lanes, {});
     b->lane_bytes.assign(lanes, 0);
     for (int t : order) {
+        if (b->items[t].queued) continue;
         const int l = static_cast<int>(std::min_element(load.begin(), load.end()) - load.begin());
         load[l] += b->items[t].bytes + 64.0 * 1024;  // a launch's fixed cost, in bytes
         b->items[t].lane = l;
@@ -283,6 +397,12 @@ int eithot_batch_run(eithot_batch* b, void* const* d_data, const size_t* capacit
         b->prev_ws = ws;
         b->have_prev = true;
     }
+    if (!b->queue.empty()) {
+        if (int rc = upload_queue(b, d_data)) {
+            if (owned) cudaFreeAsync(ws, st);
+            return rc;
+        }
+    }
     const int rc = enqueue(b, d_data, ws, st);
     if (owned) cudaFreeAsync(ws, st);
     return rc;
@@ -301,6 +421,9 @@ int eithot_batch_destroy(eithot_batch* b) {
     for (auto s : b->streams) cudaStreamDestroy(s);
     for (auto ev : b->done) cudaEventDestroy(ev);
     if (b->fork) cudaEventDestroy(b->fork);
+    if (b->qstream) cudaStreamDestroy(b->qstream);
+    if (b->qdone) cudaEventDestroy(b->qdone);
+    if (b->d_queue) cudaFree(b->d_queue);
     delete b;
     return EITHOT_OK;
 }

@@ -61,6 +61,14 @@ int run_slab_perm(uint8_t* data, const Pass& p, ExecContext& ctx);
 // The run kernel of a slab permutation (whole elements of 1-16 bytes whose
 // padded slab fits one CTA); -1 when it does not apply.
 int try_slab_runs_pass(uint8_t* data, const Pass& p, ExecContext& ctx);
+
+// The batched form's queue of whole-tensor slab permutations: the size of one
+// entry, an entry for pass p on data (false when the run kernel does not
+// apply; *smem the shared memory it needs), and one persistent launch over n
+// entries in device memory (*d_next: a counter the launch zeroes first).
+size_t slab_queue_entry_bytes();
+bool slab_queue_entry(uint8_t* data, const Pass& p, const DeviceCaps& caps, void* entry, size_t* smem);
+int launch_slab_queue(const void* d_entries, uint32_t n, unsigned* d_next, size_t smem, ExecContext& ctx);
 int run_block_perm(uint8_t* data, const Pass& p, ExecContext& ctx);
 size_t block_perm_workspace(const Pass& p, bool ideal);
 

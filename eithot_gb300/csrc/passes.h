@@ -100,12 +100,14 @@ struct Tuning {
                              // wrap the fastest output axis once step it with one jump; 2: every run steps
                              // through the axes element by element)
     int slab_prefetch = 1;   // slab permutations at one CTA per SM: the next slab prefetched into registers
-    int row_solo_kb = 110;   // rows held by one CTA above this many KB run one CTA per SM with the next
+    int row_solo_kb = 48;    // rows held by one CTA above this many KB run one CTA per SM with the next
                              // row prefetched into registers (up to 128 KB), smaller ones two or more per SM
+                             // (96 KB rows of 32-byte elements: 6.18 TB/s against 4.81 at two per SM)
     int slab2d_runs = 1;     // slab transposes of whole elements beyond the packed sizes through the slab-
                              // permutation run kernel: 0 never, 1 elements of 1-2 bytes, 2 of 1-16 bytes
     int col_bulk = 0;        // group form: double-buffered CTAs staging their slots with bulk copies (slower on GB300)
     int batch_graph = 1;     // batched form: a run repeating the previous run's buffers replays a CUDA graph
+    int batch_queue = 1;     // batched form: small tensors permuted by one persistent launch over a device queue
 };
 Tuning& tuning();
 

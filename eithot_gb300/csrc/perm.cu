@@ -158,6 +158,7 @@ struct SlabRunArgs {
     // their bytes placed into the padded rows.
     uint32_t stage_words;
     FastDiv32 div_rowb;       // slab byte -> (row, byte of the row)
+    uint32_t kind;            // 100 * E + V (the queue kernel's dispatch)
     FastDiv32 hod[kMaxAxes];  // output dims m.., output order
     uint32_t hstep[kMaxAxes];
     uint32_t delta[16];
@@ -386,6 +387,62 @@ __global__ void __launch_bounds__(512, 1) k_slab_runs_pf(SlabRunArgs a) {
         __syncthreads();  // shared memory is free for the next slab
     }
 }
+
+// ---------------------------------------------------------------------------
+// The batched form's queue of whole-tensor slab permutations: one persistent
+// launch whose CTAs take entries from a device counter (atomicAdd) until the
+// queue is empty.  An entry is one small tensor permuted in a single slab (its
+// run-kernel arguments, built on the host); entries are independent, so no
+// CTA ever waits for another.  The entry's arguments are copied to shared
+// memory first; staging and write-back dispatch on its unit and element.
+// ---------------------------------------------------------------------------
+template <int E, int V>
+__device__ __forceinline__ void queue_write(const SlabRunArgs& a, const uint8_t* sm, uint8_t* slab) {
+    write_runs<E, V>(a, sm, slab);
+}
+
+__global__ void __launch_bounds__(512) k_slab_queue(const SlabRunArgs* entries, uint32_t n, unsigned* next) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    __shared__ __align__(16) SlabRunArgs s_a;
+    __shared__ uint32_t s_k;
+    constexpr uint32_t kWords = sizeof(SlabRunArgs) / 4;
+    for (;;) {
+        if (threadIdx.x == 0) s_k = atomicAdd(next, 1u);
+        __syncthreads();
+        const uint32_t k = s_k;
+        if (k >= n) break;
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(entries + k);
+        for (uint32_t x = threadIdx.x; x < kWords; x += blockDim.x) reinterpret_cast<uint32_t*>(&s_a)[x] = src[x];
+        __syncthreads();
+        const SlabRunArgs& a = s_a;
+        uint8_t* slab = a.base;
+        switch (a.su) {
+            case 16: stage_rows<16>(a, smem, slab); break;
+            case 8: stage_rows<8>(a, smem, slab); break;
+            case 4: stage_rows<4>(a, smem, slab); break;
+            case 2: stage_rows<2>(a, smem, slab); break;
+            default: stage_rows<1>(a, smem, slab); break;
+        }
+        __syncthreads();
+        switch (a.kind) {
+            case 104: queue_write<1, 4>(a, smem, slab); break;
+            case 108: queue_write<1, 8>(a, smem, slab); break;
+            case 116: queue_write<1, 16>(a, smem, slab); break;
+            case 204: queue_write<2, 4>(a, smem, slab); break;
+            case 208: queue_write<2, 8>(a, smem, slab); break;
+            case 216: queue_write<2, 16>(a, smem, slab); break;
+            case 404: queue_write<4, 4>(a, smem, slab); break;
+            case 408: queue_write<4, 8>(a, smem, slab); break;
+            case 416: queue_write<4, 16>(a, smem, slab); break;
+            case 808: queue_write<8, 8>(a, smem, slab); break;
+            case 816: queue_write<8, 16>(a, smem, slab); break;
+            default: queue_write<16, 16>(a, smem, slab); break;
+        }
+        __syncthreads();  // shared memory and s_k are free for the next entry
+    }
+}
+
+static_assert(sizeof(SlabRunArgs) % 4 == 0, "queue entries are copied in words");
 
 // ---------------------------------------------------------------------------
 // Block permutation along cycles.  Blocks of `blk` bytes are indexed by q
@@ -631,9 +688,12 @@ void set_aligned_runs(SlabRunArgs* a, uint64_t K) {
 
 // The run kernel for whole elements of 1-16 bytes when its padded staging
 // fits; returns -1 when it does not apply.
-int try_slab_runs(uint8_t* data, const Pass& p, uint64_t count, ExecContext& ctx) {
+// Fills the run kernel's arguments for pass p (count elements per slab);
+// false when the kernel does not apply.  *V: the store width.
+bool make_slab_runs(uint8_t* data, const Pass& p, uint64_t count, const DeviceCaps& caps, SlabRunArgs* out,
+                    size_t* smem_out, uint64_t* V_out) {
     const uint64_t E = p.elem;
-    if (!(E == 1 || E == 2 || E == 4 || E == 8 || E == 16) || (p.strip && p.strip != E)) return -1;
+    if (!(E == 1 || E == 2 || E == 4 || E == 8 || E == 16) || (p.strip && p.strip != E)) return false;
     const int q = static_cast<int>(p.nd_dims.size());
     const uint64_t row_bytes = p.nd_dims[0] * E;
     const uint64_t g = std::max<uint64_t>(4, E);
@@ -641,13 +701,13 @@ int try_slab_runs(uint8_t* data, const Pass& p, uint64_t count, ExecContext& ctx
     if ((pitch / g) % 2 == 0) pitch += g;
     const uint64_t nrows = count / p.nd_dims[0];
     const size_t smem = nrows * pitch;
-    if (smem > smem_cap_of(ctx.caps)) return -1;
+    if (smem > smem_cap_of(caps)) return false;
     uint8_t* base = data + p.offset;
     const uint64_t addr = reinterpret_cast<uintptr_t>(base);
     const uint64_t slab_bytes = count * E;
     const uint64_t V = pow2_unit({addr, slab_bytes});
-    if (V < std::max<uint64_t>(4, E)) return -1;  // stores of at least a word (and a whole element)
-    SlabRunArgs a;
+    if (V < std::max<uint64_t>(4, E)) return false;  // stores of at least a word (and a whole element)
+    SlabRunArgs& a = *out;
     std::memset(&a, 0, sizeof(a));
     a.base = base;
     a.batches = p.batches;
@@ -681,7 +741,18 @@ int try_slab_runs(uint8_t* data, const Pass& p, uint64_t count, ExecContext& ctx
         set_aligned_runs(&a, V / E);
         a.wrap = !a.aligned && a.odim[0] >= V / E;
     }
-    switch (E) {
+    a.kind = static_cast<uint32_t>(E * 100 + V);
+    *smem_out = smem;
+    *V_out = V;
+    return true;
+}
+
+int try_slab_runs(uint8_t* data, const Pass& p, uint64_t count, ExecContext& ctx) {
+    SlabRunArgs a;
+    size_t smem = 0;
+    uint64_t V = 0;
+    if (!make_slab_runs(data, p, count, ctx.caps, &a, &smem, &V)) return -1;
+    switch (p.elem) {
         case 1: return dispatch_v<1>(a, smem, V, ctx);
         case 2: return dispatch_v<2>(a, smem, V, ctx);
         case 4: return dispatch_v<4>(a, smem, V, ctx);
@@ -691,6 +762,34 @@ int try_slab_runs(uint8_t* data, const Pass& p, uint64_t count, ExecContext& ctx
 }
 
 }  // namespace
+
+size_t slab_queue_entry_bytes() { return sizeof(SlabRunArgs); }
+
+bool slab_queue_entry(uint8_t* data, const Pass& p, const DeviceCaps& caps, void* entry, size_t* smem) {
+    uint64_t count = 1;
+    for (auto d : p.nd_dims) count *= d;
+    if (p.batches != 1 || count >= (uint64_t(1) << 31) || tuning().slab_runs == 0) return false;
+    SlabRunArgs a;
+    uint64_t V = 0;
+    if (!make_slab_runs(data, p, count, caps, &a, smem, &V)) return false;
+    a.batches = 1;
+    std::memcpy(entry, &a, sizeof(a));
+    return true;
+}
+
+int launch_slab_queue(const void* d_entries, uint32_t n, unsigned* d_next, size_t smem, ExecContext& ctx) {
+    if (n == 0) return 0;
+    PM_CHECK(cudaMemsetAsync(d_next, 0, sizeof(unsigned), ctx.stream));
+    PM_CHECK(cudaFuncSetAttribute(k_slab_queue, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    int per_sm = 0;
+    PM_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_slab_queue, 512, smem));
+    const uint64_t cap = static_cast<uint64_t>(std::max(per_sm, 1)) * device_sms(ctx);
+    const unsigned grid = static_cast<unsigned>(std::max<uint64_t>(1, std::min<uint64_t>(n, cap)));
+    k_slab_queue<<<grid, 512, smem, ctx.stream>>>(static_cast<const SlabRunArgs*>(d_entries), n, d_next);
+    PM_CHECK(cudaGetLastError());
+    ctx.launches++;
+    return 0;
+}
 
 int try_slab_runs_pass(uint8_t* data, const Pass& p, ExecContext& ctx) {
     uint64_t count = 1;

@@ -191,7 +191,11 @@ int eithot_workspace_size(int rank, const int64_t* dims, const int* perm_1based,
  * on; runs of one batch must not overlap.  A run whose buffers, capacities
  * and (caller-provided) workspace repeat the previous run's is replayed from
  * a CUDA graph of that work, captured on the first repeat: one graph launch
- * instead of thousands of kernel launches from the host.  eithot_batch_launches
+ * instead of thousands of kernel launches from the host.  Small tensors whose
+ * whole permutation fits one CTA's shared memory are permuted by one
+ * persistent launch that takes them from a device queue (knob "batch_queue");
+ * the queue's table is device memory the batch allocates at its first run
+ * and frees in eithot_batch_destroy.  eithot_batch_launches
  * reports the kernel launches of the last run (the graph's kernel nodes when
  * it was replayed). */
 typedef struct eithot_batch eithot_batch;
@@ -320,7 +324,7 @@ int eithot_estimate_report(int rank, const int64_t* dims, const int* perm_1based
  *                 (default); 2 the runs step through every axis per element;
  *                 0 one divide chain per element
  *   "row_solo_kb" rows held whole by one CTA that are larger than this many
- *                 KB (16..128, default 110) run one CTA per SM with the next
+ *                 KB (16..128, default 48) run one CTA per SM with the next
  *                 row prefetched into registers; smaller ones two or more CTAs
  *                 per SM
  *   "slab2d_runs" slab transposes of whole elements beyond the sizes packed
@@ -345,7 +349,12 @@ int eithot_estimate_report(int rank, const int64_t* dims, const int* perm_1based
  *                 L2 while they wait at the barrier, 0 not (default; slower)
  *   "batch_graph" 1 a batch run on the same buffers and workspace as the
  *                 batch's previous run replays the work as a CUDA graph
- *                 (captured on the first repeat), 0 always issue directly */
+ *                 (captured on the first repeat), 0 always issue directly
+ *   "batch_queue" 1 a batch's small tensors (whole permutation in one CTA's
+ *                 shared memory, up to 192 KB) are permuted by one
+ *                 persistent launch over a device queue whose table the
+ *                 batch allocates at its first run (default), 0 every tensor
+ *                 runs its planned passes on the lanes */
 int eithot_tune_set(const char* key, double value);
 int eithot_tune_get(const char* key, double* value);
 

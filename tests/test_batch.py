@@ -39,13 +39,17 @@ def test_batch_plans_on_the_host(E):
 gpu = pytest.mark.gpu
 
 
-def run_batch(E, tensors, seed, caller_workspace=False, runs=2):
+def run_batch(E, tensors, seed, caller_workspace=False, runs=2, shifts=None):
+    """shifts: per tensor, a byte offset added to its 256-aligned base."""
     import torch
     dev = torch.device("cuda:0")
     b = E.Batch(tensors)
     sizes = [math.prod(d) * e for d, p, e in tensors]
     caps = [s + 256 for s in sizes]
-    offs = np.cumsum([0] + [(c + 255) // 256 * 256 for c in caps])
+    offs = np.cumsum([0] + [(c + 512) // 256 * 256 for c in caps])[:-1]
+    if shifts is not None:
+        offs = offs + np.array(shifts)
+    offs = np.append(offs, offs[-1] + caps[-1] + 512)
     buf = torch.zeros(int(offs[-1]), dtype=torch.uint8, device=dev)
     ws = None
     if caller_workspace and b.workspace_size:
@@ -116,3 +120,34 @@ def test_batch_repeated_runs_replay_a_graph(E, graph):
         run_batch(E, tensors, seed=41, caller_workspace=True, runs=4)
     finally:
         E.tune_set("batch_graph", saved)
+
+
+@gpu
+@pytest.mark.parametrize("queue", [1, 0])
+def test_batch_queue_of_small_tensors(E, queue):
+    """Small tensors whose whole permutation fits one CTA are permuted by one
+    persistent launch over a device queue (knob batch_queue=1; with 0 they
+    run through their planned passes in the lanes): 1- to 16-byte elements,
+    ranks 2-8, bases shifted off 16-byte boundaries (a tensor whose entry
+    does not apply on its buffer, e.g. 2-byte stores only, falls back to its
+    passes), beside larger tensors in the lanes; four runs (the second
+    captures a graph, the later ones replay it), each bit-exact."""
+    saved = E.tune_get("batch_queue")
+    try:
+        E.tune_set("batch_queue", queue)
+        rng = np.random.default_rng(51)
+        tensors, shifts = [], []
+        for t in range(200):
+            r = int(rng.integers(2, 9))
+            elem = int(rng.choice([1, 2, 4, 8, 16]))
+            dims = [int(rng.integers(1, 6)) for _ in range(r)]
+            while math.prod(dims) * elem < 2048:
+                dims[int(rng.integers(0, r))] += 1
+            perm = [int(x) + 1 for x in rng.permutation(r)]
+            tensors.append((dims, perm, elem))
+            shifts.append(int(rng.choice([0, 0, 0, 2, 4, 8, 12])) if elem <= 4 else 0)
+        tensors += [([3001, 4096], [2, 1], 4), ([60, 40, 3401], [3, 1, 2], 2)]
+        shifts += [0, 0]
+        run_batch(E, tensors, seed=61, caller_workspace=True, runs=4, shifts=shifts)
+    finally:
+        E.tune_set("batch_queue", saved)
