@@ -6,6 +6,11 @@ candidate knob settings on a scratch buffer of that shape on the current
 device, records the fastest with eithot_tune_shape_set (so every later
 eithot_transpose of exactly that shape uses it) and returns it.  Results
 can be saved to and loaded from a JSON file keyed by shape.
+
+This helper takes its scratch buffer and CUDA events from PyTorch (imported
+when `autotune` runs); the library it tunes (libeithot.so, the C ABI) has
+no PyTorch dependency, and a caller without PyTorch records knobs with
+eithot_tune_shape_set directly.
 """
 from __future__ import annotations
 
