@@ -18,7 +18,8 @@ e2e:   the same metric through the C ABI with the tensor in pinned host
 Beside them: the 3001 x 4096 int32 matrix (perm (2 1)) timed the same way
 (device-resident and end to end), the (16, 3001, 1024, 256, 4) uint16 tensor
 (100.7 GB, perm (5 3 1 4 2)) device-resident under the fewest-pass plan and
-the reference's series, the reference's own CUDA build
+the reference's series, summaries of the batched form (4096 mixed tensors)
+and the served form (200 Poisson-arriving requests), the reference's own CUDA build
 (test_inplace recompiled for sm_103a from baseline/_ref, when built) on both
 configurations, and the reference's own single-threaded host permutation
 next to the oracle's OpenMP restatement of it.
@@ -622,6 +623,13 @@ def run_eithot(args):
             torch.cuda.empty_cache()
             line["reference_gpu"] = reference_gpu()
             line["c3_16x3001x1024x256x4_u16"] = time_c3(E, dev)
+            # the batched and served forms, summarised (their own workloads print full lines)
+            bt = batched_result(args)
+            line["batched_4096_mixed"] = {k: bt[k] for k in ("value", "unit", "ms_per_batch", "one_at_a_time",
+                                                            "one_at_a_time_fewest", "speedup_vs_one_at_a_time",
+                                                            "launches_per_batch", "config")}
+            sv = served_result(args)
+            line["served_200_poisson"] = {k: sv[k] for k in ("served", "serial", "config")}
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -650,6 +658,11 @@ def mixed_tensors(count, seed, min_bytes, max_bytes, min_rank, max_rank):
 
 
 def run_batched(args):
+    print(json.dumps(batched_result(args)), flush=True)
+    return 0
+
+
+def batched_result(args):
     """4096 tensors of 4 KB-64 MB, rank 3-6: the batched form against one
     eithot_transpose call per tensor on one stream (both device-resident,
     wall-clock from the first issue to the device being idle)."""
@@ -709,8 +722,9 @@ def run_batched(args):
             "data": "synthetic (seeded counter hash per tensor, checked on the device after the first run)",
             "config": {"workload": "4096 tensors, rank U{3..6}, bytes log-uniform [4 KB, 64 MB], elem U{1,2,4,8}, "
                                    "random permutations (seed 4)", "tensors": len(ts), "bytes": total}}
-    print(json.dumps(line), flush=True)
-    return 0
+    del buf, ws
+    torch.cuda.empty_cache()
+    return line
 
 
 class _Arena:
@@ -741,6 +755,11 @@ class _Arena:
 
 
 def run_served(args):
+    print(json.dumps(served_result(args)), flush=True)
+    return 0
+
+
+def served_result(args):
     """Poisson arrivals (200 requests/s, seeded) of tensors of 1 MB-40 GB,
     rank 2-8, resident in one device arena: the server (4 streams, 5 %
     workspace pool, continuous batching) against serial eithot_transpose
@@ -823,8 +842,9 @@ def run_served(args):
             "config": {"workload": "%d requests, Poisson 200/s (seed 6), rank U{2..8}, bytes log-uniform [1 MB, 40 GB], "
                                    "elem U{1,2,4,8}, random permutations (seed 5), alpha 0.05" % count,
                        "bytes": total, "server": {"streams": 4, "workspace_pool_bytes": pool}}}
-    print(json.dumps(line), flush=True)
-    return 0
+    del arena
+    torch.cuda.empty_cache()
+    return line
 
 
 def run_study(args):
