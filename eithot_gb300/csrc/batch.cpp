@@ -1,6 +1,6 @@
 // The batched form: many independent in-place transposes planned once and
 // run together.  Each tensor's passes stay in order on one of up to 16
-// internal streams ("lanes"); every tensor is planned for the fewest
+// internal streams ("lanes", knob batch_lanes); every tensor is planned for the fewest
 // modelled passes (without cycle-following moves, whose segment tables are
 // copied from the host); tensors are spread over the lanes
 // largest-first onto the least-loaded lane, so the small passes of
@@ -79,7 +79,6 @@ struct eithot_batch {
 
 namespace {
 
-constexpr int kMaxLanes = 16;
 constexpr size_t kQueueBytes = 192 * 1024;   // tensors up to this size may go to the queue
 constexpr size_t kQueueSmem = 200 * 1024;    // shared memory of one queue entry at most
 
@@ -316,7 +315,7 @@ int eithot_batch_create(int count, const int* ranks, const int64_t* dims, const 
     // largest first: the counter hands entries out in table order
     std::stable_sort(b->queue.begin(), b->queue.end(), [&](int x, int y) { return b->items[x].bytes > b->items[y].bytes; });
     // largest first onto the least-loaded lane
-    const int lanes = std::max(1, std::min(count, kMaxLanes));
+    const int lanes = std::max(1, std::min(count, b->tuning.batch_lanes));
     std::vector<int> order(count);
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return b->items[x].bytes > b->items[y].bytes; });
@@ -331,6 +330,9 @@ int eithot_batch_create(int count, const int* ranks, const int64_t* dims, const 
         b->lane_items[l].push_back(t);
         b->lane_bytes[l] = std::max(b->lane_bytes[l], b->items[t].scratch);
     }
+    // a queued tensor whose entry does not apply on its buffers runs its own
+    // passes on lane 0, with lane 0's scratch
+    for (int t : b->queue) b->lane_bytes[0] = std::max(b->lane_bytes[0], b->items[t].scratch);
     b->lane_offset.assign(lanes, 0);
     for (int l = 0; l < lanes; ++l) {
         b->lane_offset[l] = b->workspace;

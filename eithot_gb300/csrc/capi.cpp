@@ -175,6 +175,10 @@ int apply_knob(eithot::Tuning& t, const char* key, double value) {
         if (v != 0 && v != 32 && v != 64 && v != 128 && v != 256 && v != 512)
             return fail(EITHOT_EINVAL, "col_chunk must be 0, 32, 64, 128, 256 or 512");
         t.col_chunk = v;
+    } else if (k == "batch_lanes") {
+        const int v = static_cast<int>(value);
+        if (v < 1 || v > 64) return fail(EITHOT_EINVAL, "batch_lanes must be 1..64");
+        t.batch_lanes = v;
     } else if (k == "batch_queue") {
         t.batch_queue = value != 0 ? 1 : 0;
     } else if (k == "batch_graph") {
@@ -247,6 +251,7 @@ int eithot_tune_get(const char* key, double* value) {
     else if (k == "row_solo_kb") *value = t.row_solo_kb;
     else if (k == "batch_graph") *value = t.batch_graph;
     else if (k == "batch_queue") *value = t.batch_queue;
+    else if (k == "batch_lanes") *value = t.batch_lanes;
     else if (k == "col_chunk") *value = t.col_chunk;
     else if (k == "max_cluster") *value = t.max_cluster;
     else if (k == "variant") *value = t.variant;

@@ -213,7 +213,11 @@ struct SlabClusterArgs {
     uint64_t items, mat_bytes, row_bytes;
     uint32_t R, C, E, Q, pitch, upr, upw, wpr;
     bool load4;  // rows are whole 4-byte words at a 4-byte aligned base: load words
-    FastDiv32 div_upr, div_upw, div_Qupw, div_Qpack, div_wpr;
+    // otherwise, narrow units: the band is read in aligned 4-byte words and
+    // its bytes placed into the padded rows (bytes of the words outside the
+    // band are read and dropped: a word never crosses a page)
+    bool stage_words;
+    FastDiv32 div_upr, div_upw, div_Qupw, div_Qpack, div_wpr, div_rowb;
 };
 
 template <int US, int kPack>
@@ -237,6 +241,24 @@ __global__ void __launch_bounds__(kThreads) k_slab_cluster(SlabClusterArgs a) {
                 copy_in<4, uint32_t>(smem + rr * a.pitch + cw * 4, band + static_cast<uint64_t>(x) * 4);
             }
             copy_in_wait<4>();
+        } else if (US < 4 && a.stage_words) {
+            const uint32_t nbytes = nr * static_cast<uint32_t>(a.row_bytes);
+            const uintptr_t lo = reinterpret_cast<uintptr_t>(band);
+            const uint32_t head = static_cast<uint32_t>(lo & 3u);
+            const uint32_t* wp = reinterpret_cast<const uint32_t*>(lo - head);
+            const uint32_t words = (head + nbytes + 3) / 4;
+            for (uint32_t x = threadIdx.x; x < words; x += blockDim.x) {
+                const uint32_t v = wp[x];
+                const uint32_t b0 = x * 4;  // band offset of the word's first byte is b0 - head
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const uint32_t ob = b0 + k;
+                    if (ob < head || ob - head >= nbytes) continue;
+                    uint32_t rr, cb;
+                    a.div_rowb.divmod(ob - head, rr, cb);
+                    smem[rr * a.pitch + cb] = static_cast<uint8_t>(v >> (8 * k));
+                }
+            }
         } else {
             const uint32_t in_units = nr * a.upr;
             for (uint32_t x = threadIdx.x; x < in_units; x += blockDim.x) {
@@ -1609,6 +1631,8 @@ int launch_slab_cluster(uint8_t* data, const Pass& p, ExecContext& ctx) {
     a.div_upr = FastDiv32::make(a.upr);
     a.div_upw = FastDiv32::make(a.upw);
     a.load4 = US < 4 && a.row_bytes % 4 == 0 && addr % 4 == 0;
+    a.stage_words = US < 4 && !a.load4 && tuning().slab_runs == 1;
+    a.div_rowb = FastDiv32::make(a.row_bytes);
     a.wpr = static_cast<uint32_t>(a.row_bytes / 4);
     a.div_wpr = FastDiv32::make(a.wpr ? a.wpr : 1);
     a.div_Qupw = FastDiv32::make(static_cast<uint64_t>(Q) * a.upw);

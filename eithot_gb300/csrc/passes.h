@@ -108,6 +108,7 @@ struct Tuning {
     int col_bulk = 0;        // group form: double-buffered CTAs staging their slots with bulk copies (slower on GB300)
     int batch_graph = 1;     // batched form: a run repeating the previous run's buffers replays a CUDA graph
     int batch_queue = 1;     // batched form: small tensors permuted by one persistent launch over a device queue
+    int batch_lanes = 16;    // batched form: internal streams the other tensors are spread over (1..64)
 };
 Tuning& tuning();
 

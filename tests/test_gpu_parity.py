@@ -280,6 +280,19 @@ def test_wide_elements(E):
     run_case(E, [16384, 25, 4, 3], [1, 3, 2, 4], 2)
 
 
+@pytest.mark.parametrize("dims,elem", [([1001, 300], 1), ([41125, 20], 1), ([17, 12955], 1), ([777, 333], 2),
+                                       ([5003, 61], 1), ([301, 1500], 2)])
+@pytest.mark.parametrize("offset", [0, 1, 3])
+def test_cluster_slabs_of_narrow_odd_rows(E, dims, elem, offset):
+    """Matrices of 1- and 2-byte elements beyond one CTA's shared memory (one
+    cluster-slab pass) whose rows are not whole 4-byte words: each CTA's band
+    is staged from aligned words around it (bytes outside the band dropped),
+    at bases off word boundaries; 2D transposes under the reference's series
+    and the fewest-pass plans."""
+    for order in (0, 3):
+        run_case(E, dims, [2, 1], elem, order=order, offset=offset * elem % 4 if elem == 2 else offset)
+
+
 def test_unaligned_base_and_odd_elements(E):
     run_case(E, [33, 17, 9], [2, 3, 1], 4, offset=4)
     run_case(E, [33, 17, 9], [3, 1, 2], 2, offset=2)
