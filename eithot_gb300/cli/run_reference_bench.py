@@ -42,7 +42,7 @@ BIN = os.path.join(os.path.dirname(HERE), "bin")
 
 CASE_RE = re.compile(r"number of sub_tensors = (\d+)\s*\nDims = ([0-9 ]+), Data size = ([0-9.]+) GB\n"
                      r"(?:.*\n)*?(Correct|Incorrect) transpose\n"
-                     r"Execution Time without h2d2h: ([0-9.]+)ms\nExecution Time: ([0-9.]+)ms")
+                     r"Execution Time without h2d2h: (-?[0-9.]+)ms\nExecution Time: ([0-9.]+)ms")
 
 
 def per_case(log):

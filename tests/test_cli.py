@@ -136,3 +136,23 @@ def test_statistic_summarises_the_bench_files(tmp_path):
             % (statistics.fmean([70.5, 72.25, 60.0]), statistics.pstdev([70.5, 72.25, 60.0]), 6.25, 0.25))
     assert p.stdout == want
     assert (tmp_path / "Statistic.txt").read_text() == want
+
+
+def test_benchmark_script_runner_parses_each_case():
+    """The runner of the reference's benchmark script reads every
+    test_inplace block of the script's console output (host only)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "run_reference_bench", os.path.join(ROOT, "eithot_gb300", "cli", "run_reference_bench.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    log = ("test_cases/exp2/exp2.txt\nCase 1\ninit Extra Memory size = 7.42195 MB\n\tx\n\n"
+           "Case 1\n2D Inplace 21 transpose\nnumber of sub_tensors = 4\nDims = 7248 7248, Data size = 0.21013 GB\n"
+           "Inplace transpose verify_inplace\nCorrect transpose\nExecution Time without h2d2h: 2.50000ms\n"
+           "Execution Time: 4.75000ms\n\nCase 2\n3D Inplace 132 transpose\nnumber of sub_tensors = 8\n"
+           "Dims = 368 384 384, Data size = 0.21706 GB\nInplace transpose verify_inplace\nIncorrect transpose\n"
+           "Execution Time without h2d2h: -0.10000ms\nExecution Time: 3.00000ms\n")
+    cases = mod.per_case(log)
+    assert cases == [
+        {"nb": 4, "dims": [7248, 7248], "gb": 0.21013, "correct": True, "kernel_ms": 2.5, "e2e_ms": 4.75},
+        {"nb": 8, "dims": [368, 384, 384], "gb": 0.21706, "correct": False, "kernel_ms": -0.1, "e2e_ms": 3.0}]
