@@ -301,12 +301,34 @@ __global__ void __launch_bounds__(kThreads) k_slab_cluster(SlabClusterArgs a) {
 // Copies `bytes` contiguous bytes from global memory into shared memory:
 // 16-byte cp.async chunks when both ends and the size allow it (vec16),
 // else US-byte units.  Completes before returning.
+// Copies `bytes` contiguous bytes at any alignment from global memory to
+// shared memory through the aligned 4-byte words around them (bytes of the
+// first and last word outside the range are read and dropped; a word never
+// crosses a page).  For 1- and 2-byte units: one load per 4 bytes instead of
+// one per unit.
+__device__ __forceinline__ void words_copy_in(uint8_t* sm, const uint8_t* g, uint32_t bytes) {
+    const uintptr_t lo = reinterpret_cast<uintptr_t>(g);
+    const uint32_t head = static_cast<uint32_t>(lo & 3u);
+    const uint32_t* wp = reinterpret_cast<const uint32_t*>(lo - head);
+    const uint32_t words = (head + bytes + 3) / 4;
+    for (uint32_t x = threadIdx.x; x < words; x += blockDim.x) {
+        const uint32_t v = wp[x];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t ob = x * 4 + k;
+            if (ob >= head && ob - head < bytes) sm[ob - head] = static_cast<uint8_t>(v >> (8 * k));
+        }
+    }
+}
+
 template <int US>
 __device__ __forceinline__ void block_copy_in(uint8_t* sm, const uint8_t* g, uint32_t bytes, bool vec16) {
     using U = typename UnitOf<US>::T;
     if (vec16) {
         for (uint32_t x = threadIdx.x; x < bytes / 16; x += blockDim.x) copy_in<16, uint4>(sm + x * 16, g + x * 16);
         copy_in_wait<16>();
+    } else if (US < 4 && bytes >= 64) {
+        words_copy_in(sm, g, bytes);
     } else {
         for (uint32_t x = threadIdx.x; x < bytes / US; x += blockDim.x) copy_in<US, U>(sm + x * US, g + x * US);
         copy_in_wait<US>();
@@ -442,8 +464,12 @@ __device__ __forceinline__ void row_stage_in(const RowArgs& a, const Fn& fn, uin
         }
     } else if (a.flat) {
         const uint8_t* src = row + static_cast<uint64_t>(j0) * a.E;
-        for (uint32_t x = threadIdx.x; x < my_units; x += blockDim.x)
-            copy_in<US, U>(buf + x * US, src + static_cast<uint64_t>(x) * US);
+        if (US < 4 && my_units * US >= 64) {
+            words_copy_in(buf, src, my_units * US);
+        } else {
+            for (uint32_t x = threadIdx.x; x < my_units; x += blockDim.x)
+                copy_in<US, U>(buf + x * US, src + static_cast<uint64_t>(x) * US);
+        }
     } else {
         for (uint32_t x = threadIdx.x; x < my_units; x += blockDim.x) {
             uint32_t jj, u;
