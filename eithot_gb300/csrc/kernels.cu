@@ -322,12 +322,13 @@ __device__ __forceinline__ void words_copy_in(uint8_t* sm, const uint8_t* g, uin
 }
 
 template <int US>
-__device__ __forceinline__ void block_copy_in(uint8_t* sm, const uint8_t* g, uint32_t bytes, bool vec16) {
+__device__ __forceinline__ void block_copy_in(uint8_t* sm, const uint8_t* g, uint32_t bytes, bool vec16,
+                                              bool words) {
     using U = typename UnitOf<US>::T;
     if (vec16) {
         for (uint32_t x = threadIdx.x; x < bytes / 16; x += blockDim.x) copy_in<16, uint4>(sm + x * 16, g + x * 16);
         copy_in_wait<16>();
-    } else if (US < 4 && bytes >= 64) {
+    } else if (US < 4 && words && bytes >= 64) {
         words_copy_in(sm, g, bytes);
     } else {
         for (uint32_t x = threadIdx.x; x < bytes / US; x += blockDim.x) copy_in<US, U>(sm + x * US, g + x * US);
@@ -344,6 +345,7 @@ struct SlabPackArgs {
     uint64_t batches, items, mat_bytes, E;
     uint32_t k, R, C, upw, mat_units;
     bool vec16;  // base and matrix size are 16-byte multiples
+    bool words;  // narrow units: stage from aligned 4-byte words (knob narrow_words)
     FastDiv32 div_mat_units, div_upw, div_R;
 };
 
@@ -357,7 +359,7 @@ __global__ void __launch_bounds__(kThreads) k_slab_pack(SlabPackArgs a) {
         const uint32_t nm = static_cast<uint32_t>(left < a.k ? left : a.k);
         uint8_t* blk = a.base + m0 * a.mat_bytes;
         const uint32_t units = nm * a.mat_units;
-        block_copy_in<US>(smem, blk, units * US, a.vec16 && (units * US) % 16 == 0);
+        block_copy_in<US>(smem, blk, units * US, a.vec16 && (units * US) % 16 == 0, a.words);
         __syncthreads();
         if constexpr (kPack > 1) {
             // kPack consecutive output elements (they may cross output rows
@@ -418,6 +420,7 @@ struct RowArgs {
     uint32_t rows, cols, P, w, upw, last_upw, nstrips, buf_bytes;
     bool flat;  // w == E: a CTA's pieces are contiguous bytes
     bool dbuf;  // two item buffers: the next item's loads overlap this item's write-back
+    bool words; // narrow units: stage contiguous pieces from aligned 4-byte words (knob narrow_words)
     FastDiv div_strips, div_rows;
     FastDiv32 div_upw, div_P;
 };
@@ -464,7 +467,7 @@ __device__ __forceinline__ void row_stage_in(const RowArgs& a, const Fn& fn, uin
         }
     } else if (a.flat) {
         const uint8_t* src = row + static_cast<uint64_t>(j0) * a.E;
-        if (US < 4 && my_units * US >= 64) {
+        if (US < 4 && a.words && my_units * US >= 64) {
             words_copy_in(buf, src, my_units * US);
         } else {
             for (uint32_t x = threadIdx.x; x < my_units; x += blockDim.x)
@@ -554,7 +557,8 @@ struct RowBlockArgs {
     unsigned* status;  // the call's status word
     uint64_t total_rows, items, row_bytes, E;
     uint32_t k, cols, upw, units_per_row;
-    bool vec16;                // base and row size are 16-byte multiples
+    bool vec16;
+    bool words;                // narrow units: stage from aligned 4-byte words (knob narrow_words)                // base and row size are 16-byte multiples
     FastDiv div_rows;          // global row -> row within its matrix
     FastDiv32 div_units_row;   // unit of the block -> (row of the block, unit of the row)
     FastDiv32 div_upw;
@@ -571,7 +575,7 @@ __global__ void __launch_bounds__(kThreads) k_row_block(RowBlockArgs a, Fn fn) {
         const uint32_t nr = static_cast<uint32_t>(left < a.k ? left : a.k);
         uint8_t* blk = a.base + r0 * a.row_bytes;
         const uint32_t units = nr * a.units_per_row;
-        block_copy_in<US>(smem, blk, units * US, a.vec16 && (units * US) % 16 == 0);
+        block_copy_in<US>(smem, blk, units * US, a.vec16 && (units * US) % 16 == 0, a.words);
         __syncthreads();
         for (uint32_t x0 = threadIdx.x; x0 < units; x0 += kBatch * blockDim.x) {
             U v[kBatch];
@@ -811,8 +815,13 @@ struct ColOwnArgs {
     bool dbuf;
     bool whole;      // one CTA holds all m slots of a tile: no halo, slots indexed modulo m
     uint32_t dofs;   // whole: a multiple of m above every |delta difference| of a tile
+    // narrow whole elements: each slot's row piece is staged from the aligned
+    // 4-byte words around it (wpp words per piece at most; bytes outside the
+    // piece read and dropped, a word never crosses a page)
+    bool stage_words;
+    uint32_t wpp;
     FastDiv div_strips, div_tiles;
-    FastDiv32 div_RU, div_upw, div_m;
+    FastDiv32 div_RU, div_upw, div_m, div_wpp;
 };
 
 // Staged slot holding the source of output slot ii's element at column
@@ -868,6 +877,30 @@ __device__ __forceinline__ void own_stage_in_tab(const ColOwnArgs& a, const I* s
                                                  uint32_t step) {
     using U = typename UnitOf<US>::T;
     const OwnItem ci = own_item(a, it);
+    if constexpr (US < 4) {
+        if (a.stage_words) {
+            const uint32_t pb = ci.tcols * static_cast<uint32_t>(a.E);  // bytes of a row piece
+            const uint32_t total = nstage * a.wpp;
+            for (uint32_t x = threadIdx.x; x < total; x += blockDim.x) {
+                uint32_t ii, q;
+                a.div_wpp.divmod(x, ii, q);
+                const I gr = srow[ii];
+                if (!in_range(gr, a.rows, a.status)) continue;
+                const uintptr_t lo = reinterpret_cast<uintptr_t>(ci.mat + static_cast<uint64_t>(gr) * a.row_bytes);
+                const uint32_t head = static_cast<uint32_t>(lo & 3u);
+                const uint32_t b0 = q * 4;  // offset in the aligned span; the piece starts at `head`
+                if (b0 >= head + pb) continue;
+                const uint32_t v = *reinterpret_cast<const uint32_t*>(lo - head + b0);
+                uint8_t* dst = buf + ii * a.pitch;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const uint32_t ob = b0 + k;
+                    if (ob >= head && ob - head < pb) dst[ob - head] = static_cast<uint8_t>(v >> (8 * k));
+                }
+            }
+            return;
+        }
+    }
     if constexpr (kLanes) {
         if (lc < ci.tcols && lu < ci.lim) {
             const uint8_t* src = ci.mat + static_cast<uint64_t>(lc) * a.E + lu * US;
@@ -1543,6 +1576,7 @@ int launch_slab(uint8_t* data, const Pass& p, ExecContext& ctx) {
     const uint64_t mat_bytes = p.rows * p.cols * p.elem;
     if (mat_bytes * kSlabPackMinMats <= kSlabPackBytes && tuning().slab_pack) {  // whole matrices: any strip
         SlabPackArgs b;
+        b.words = tuning().narrow_words != 0;
         b.base = data + p.offset;
         b.batches = p.batches;
         b.mat_bytes = mat_bytes;
@@ -1657,7 +1691,7 @@ int launch_slab_cluster(uint8_t* data, const Pass& p, ExecContext& ctx) {
     a.div_upr = FastDiv32::make(a.upr);
     a.div_upw = FastDiv32::make(a.upw);
     a.load4 = US < 4 && a.row_bytes % 4 == 0 && addr % 4 == 0;
-    a.stage_words = US < 4 && !a.load4 && tuning().slab_runs == 1;
+    a.stage_words = US < 4 && !a.load4 && tuning().narrow_words;
     a.div_rowb = FastDiv32::make(a.row_bytes);
     a.wpr = static_cast<uint32_t>(a.row_bytes / 4);
     a.div_wpr = FastDiv32::make(a.wpr ? a.wpr : 1);
@@ -1688,6 +1722,7 @@ int launch_row(uint8_t* data, const Pass& p, const FnOnChip& fn, const Fn64& fn6
         const uint64_t row_bytes = p.cols * p.elem;
         if (row_bytes * kRowBlockMinRows <= kRowBlockBytes && tuning().row_block) {  // whole rows: any strip
             RowBlockArgs b;
+            b.words = tuning().narrow_words != 0;
             b.status = ctx.status;
             b.base = data + p.offset;
             b.total_rows = p.batches * p.rows;
@@ -1713,6 +1748,7 @@ int launch_row(uint8_t* data, const Pass& p, const FnOnChip& fn, const Fn64& fn6
         }
     }
     RowArgs a;
+    a.words = tuning().narrow_words != 0;
     a.status = ctx.status;
     a.base = data + p.offset;
     a.E = p.elem;
@@ -1899,6 +1935,9 @@ ColOwnArgs col_owner_args(uint8_t* data, const Pass& p, const Staging& st, int U
     const uint64_t slots = static_cast<uint64_t>(a.Q) + a.Hlo + a.Hhi;
     a.buf_bytes = static_cast<uint32_t>((slots * st.pitch + 127) / 128 * 128);
     a.dbuf = st.dbuf;
+    a.stage_words = US < 4 && a.nstrips == 1 && a.w == a.E && tuning().narrow_words;
+    a.wpp = static_cast<uint32_t>((a.tw * a.E + 3) / 4 + 1);
+    a.div_wpp = FastDiv32::make(a.wpp);
     return a;
 }
 

@@ -100,6 +100,7 @@ struct Tuning {
                              // wrap the fastest output axis once step it with one jump; 2: every run steps
                              // through the axes element by element)
     int slab_prefetch = 1;   // slab permutations at one CTA per SM: the next slab prefetched into registers
+    int narrow_words = 1;    // contiguous ranges of 1- and 2-byte units are staged from aligned 4-byte words
     int row_solo_kb = 48;    // rows held by one CTA above this many KB run one CTA per SM with the next
                              // row prefetched into registers (up to 128 KB), smaller ones two or more per SM
                              // (96 KB rows of 32-byte elements: 6.18 TB/s against 4.81 at two per SM)

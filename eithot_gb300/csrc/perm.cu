@@ -721,7 +721,7 @@ bool make_slab_runs(uint8_t* data, const Pass& p, uint64_t count, const DeviceCa
     a.chunks16 = pow2_unit({addr, row_bytes, slab_bytes}) == 16;
     a.div_upr = FastDiv32::make(row_bytes / a.su);
     a.div_rowb = FastDiv32::make(row_bytes);
-    a.stage_words = a.su < 4 && addr % 4 == 0 && slab_bytes % 4 == 0 && tuning().slab_runs == 1;
+    a.stage_words = a.su < 4 && addr % 4 == 0 && slab_bytes % 4 == 0 && tuning().narrow_words;
     // input strides: axis 0 moves E bytes inside a row, axis i >= 1 moves
     // rows (prod of dims 1..i-1 of them) of `pitch` bytes
     std::vector<uint64_t> istep(q);

@@ -323,6 +323,9 @@ int eithot_estimate_report(int rank, const int64_t* dims, const int* perm_1based
  *                 output axis with one jump where a run wraps it at most once
  *                 (default); 2 the runs step through every axis per element;
  *                 0 one divide chain per element
+ *   "narrow_words" 1 contiguous ranges of 1- and 2-byte units (slabs, row
+ *                 pieces, bands, column row pieces) are staged from the aligned
+ *                 4-byte words around them (default), 0 unit by unit
  *   "row_solo_kb" rows held whole by one CTA that are larger than this many
  *                 KB (16..128, default 48) run one CTA per SM with the next
  *                 row prefetched into registers; smaller ones two or more CTAs

@@ -57,7 +57,7 @@ def test_autotune_keeps_results_exact(E):
 
 KNOB_VALUES = {"dbuf": 0, "max_cluster": 8, "variant": 1, "col_batch": 8, "col_chunk": 256, "col_owner": 0,
                "col_form": 1, "row_prefetch": 0, "row_block": 0, "slab_pack": 0, "slab_cluster": 0, "factor": 0,
-               "sync_sleep_ns": 32, "sync_spin_limit": 4096, "sync_relaxed": 0, "group_per_sm": 2, "l2_prefetch": 1, "col_bulk": 1, "cycle_moves": 0, "slab_perm": 2, "slab_runs": 0, "slab_prefetch": 0, "slab2d_runs": 2, "row_solo_kb": 64, "batch_graph": 0, "batch_queue": 0, "batch_lanes": 8}
+               "sync_sleep_ns": 32, "sync_spin_limit": 4096, "sync_relaxed": 0, "group_per_sm": 2, "l2_prefetch": 1, "col_bulk": 1, "cycle_moves": 0, "slab_perm": 2, "slab_runs": 0, "slab_prefetch": 0, "slab2d_runs": 2, "row_solo_kb": 64, "batch_graph": 0, "batch_queue": 0, "batch_lanes": 8, "narrow_words": 0}
 
 
 def test_every_knob_round_trips(E):

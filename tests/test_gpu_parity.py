@@ -87,7 +87,7 @@ def test_catanzaro_2d(E, R, C, elem):
 @pytest.fixture
 def tuned(E):
     keys = ("variant", "col_owner", "col_chunk", "max_cluster", "dbuf", "col_form", "row_prefetch", "row_block",
-            "slab_pack", "slab_cluster", "factor", "sync_relaxed", "group_per_sm", "col_bulk")
+            "slab_pack", "slab_cluster", "factor", "sync_relaxed", "group_per_sm", "col_bulk", "narrow_words")
     saved = {k: E.tune_get(k) for k in keys}
 
     def set_(**kw):
@@ -291,6 +291,20 @@ def test_cluster_slabs_of_narrow_odd_rows(E, dims, elem, offset):
     and the fewest-pass plans."""
     for order in (0, 3):
         run_case(E, dims, [2, 1], elem, order=order, offset=offset * elem % 4 if elem == 2 else offset)
+
+
+@pytest.mark.parametrize("words", [1, 0])
+def test_narrow_units_staged_from_words(E, tuned, words):
+    """1- and 2-byte elements whose rows are not whole 4-byte words, through
+    Catanzaro row and column passes, row blocks, packed and cluster slabs:
+    contiguous ranges staged from the aligned words around them (knob
+    narrow_words=1) or unit by unit (0), at bases off word boundaries."""
+    tuned(narrow_words=words)
+    for dims, perm, elem, offset in [([5003, 999], [2, 1], 1, 1), ([2001, 513], [2, 1], 2, 2), ([7, 130001], [2, 1], 1, 3),
+                                     ([130001, 7], [2, 1], 1, 0), ([33, 1000, 31], [3, 1, 2], 1, 1),
+                                     ([3, 40001, 5], [2, 3, 1], 2, 2), ([301, 77, 13], [2, 1, 3], 1, 3),
+                                     ([9, 5, 7, 11], [4, 3, 2, 1], 1, 1)]:
+        run_case(E, dims, perm, elem, offset=offset)
 
 
 def test_unaligned_base_and_odd_elements(E):
