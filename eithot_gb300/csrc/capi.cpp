@@ -133,6 +133,10 @@ int apply_knob(eithot::Tuning& t, const char* key, double value) {
         const int v = static_cast<int>(value);
         if (v < 0 || v > 2) return fail(EITHOT_EINVAL, "slab_runs must be 0, 1 or 2");
         t.slab_runs = v;
+    } else if (k == "slab_colband") {
+        const int v = static_cast<int>(value);
+        if (v < 0 || v > 4096) return fail(EITHOT_EINVAL, "slab_colband must be 0..4096");
+        t.slab_colband = v;
     } else if (k == "narrow_words") {
         t.narrow_words = value != 0.0 ? 1 : 0;
     } else if (k == "row_solo_kb") {
@@ -252,6 +256,7 @@ int eithot_tune_get(const char* key, double* value) {
     else if (k == "slab2d_runs") *value = t.slab2d_runs;
     else if (k == "row_solo_kb") *value = t.row_solo_kb;
     else if (k == "narrow_words") *value = t.narrow_words;
+    else if (k == "slab_colband") *value = t.slab_colband;
     else if (k == "batch_graph") *value = t.batch_graph;
     else if (k == "batch_queue") *value = t.batch_queue;
     else if (k == "batch_lanes") *value = t.batch_lanes;

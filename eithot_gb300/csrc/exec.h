@@ -66,6 +66,10 @@ int try_slab_runs_pass(uint8_t* data, const Pass& p, ExecContext& ctx);
 // entry, an entry for pass p on data (false when the run kernel does not
 // apply; *smem the shared memory it needs), and one persistent launch over n
 // entries in device memory (*d_next: a counter the launch zeroes first).
+// A column-band cluster slab (kSlabCluster with band > 0), at any alignment;
+// -1 when the band count is outside 2..16 (the caller runs the row bands).
+int run_slab_colband(uint8_t* data, const Pass& p, ExecContext& ctx);
+
 size_t slab_queue_entry_bytes();
 bool slab_queue_entry(uint8_t* data, const Pass& p, const DeviceCaps& caps, void* entry, size_t* smem);
 int launch_slab_queue(const void* d_entries, uint32_t n, unsigned* d_next, size_t smem, ExecContext& ctx);

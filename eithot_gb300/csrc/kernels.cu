@@ -2246,7 +2246,12 @@ template <int US>
 int run_pass_u(uint8_t* data, const Pass& p, ExecContext& ctx) {
     switch (p.type) {
         case kSlabTranspose: return launch_slab<US>(data, p, ctx);
-        case kSlabCluster: return launch_slab_cluster<US>(data, p, ctx);
+        case kSlabCluster:
+            if (p.band) {
+                const int rc = run_slab_colband(data, p, ctx);
+                if (rc >= 0) return rc;
+            }
+            return launch_slab_cluster<US>(data, p, ctx);
         case kRowGather:
         case kRowScatter: {
             // A row pass is run as a gather when one CTA holds the whole row

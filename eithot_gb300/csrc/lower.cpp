@@ -431,6 +431,31 @@ std::string geom(const char* name, uint64_t B, uint64_t r, uint64_t c, uint64_t 
 namespace {
 void lower_xpose_direct(const Xpose& x, const DeviceCaps& caps, std::vector<Pass>* passes);
 
+// Columns per CTA of a column-band cluster slab of R x C elements of E
+// bytes (0 when none applies): the fewest CTAs (2-16) whose band of every row
+// fits a CTA's shared memory in the run kernel's padded layout (rows of the
+// band at an odd number of max(4, E)-byte granules), two CTAs per SM when
+// that is possible, each band's row segments and output range starting on a
+// 16-byte boundary of its matrix (P E a multiple of 16).
+uint64_t colband_width(uint64_t R, uint64_t C, uint64_t E, const DeviceCaps& caps) {
+    if (!(E == 1 || E == 2 || E == 4 || E == 8 || E == 16)) return 0;
+    const uint64_t m = 16 / E;
+    const uint64_t cap = smem_cap_of(caps);
+    for (uint64_t budget : {static_cast<uint64_t>(kTwoPerSm), cap - 1024}) {
+        for (int K = 2; K <= std::min(16, tuning().max_cluster); ++K) {
+            uint64_t P = (C + K - 1) / K;
+            P = (P + m - 1) / m * m;
+            const uint64_t k = (C + P - 1) / P;
+            if (k < 2 || k > 16) continue;
+            const uint64_t g = std::max<uint64_t>(4, E);
+            uint64_t pitch = (P * E + g - 1) / g * g;
+            if ((pitch / g) % 2 == 0) pitch += g;
+            if (R * pitch <= budget) return P;
+        }
+    }
+    return 0;
+}
+
 // Modelled time of a pass list, in units of one streaming pass; *staged is
 // set when a pass goes through global scratch.
 double passes_cost(const std::vector<Pass>& ps, const DeviceCaps& caps, bool* staged) {
@@ -555,6 +580,30 @@ void lower_xpose_direct(const Xpose& x, const DeviceCaps& caps, std::vector<Pass
             p.strip = x.E;
             p.cluster = K;
             p.what = geom("slab-cluster", x.B, x.R, x.C, x.E);
+            // few rows: each CTA's row band would give every output row a few
+            // bytes; column bands write contiguous output ranges instead
+            if (Q * x.E < static_cast<uint64_t>(tuning().slab_colband)) {
+                p.band = colband_width(x.R, x.C, x.E, caps);
+                if (p.band) p.what = geom("slab-colband", x.B, x.R, x.C, x.E);
+            }
+            passes->push_back(p);
+            return;
+        }
+    }
+    // rows longer than one CTA's shared memory, few of them: column bands
+    // still make it one pass
+    if (tuning().slab_cluster && tuning().slab_colband && slab_smem_bytes(x.R, x.C, w0) > kTwoPerSm &&
+        x.C * x.E > cap - 4) {
+        const uint64_t P = colband_width(x.R, x.C, x.E, caps);
+        if (P) {
+            Pass p;
+            p.type = kSlabCluster;
+            p.offset = x.offset;
+            p.batches = x.B; p.rows = x.R; p.cols = x.C; p.elem = x.E;
+            p.strip = x.E;
+            p.cluster = static_cast<int>((x.C + P - 1) / P);
+            p.band = P;
+            p.what = geom("slab-colband", x.B, x.R, x.C, x.E);
             passes->push_back(p);
             return;
         }

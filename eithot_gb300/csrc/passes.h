@@ -46,6 +46,7 @@ struct Pass {
     uint64_t m = 0, n = 0, c = 1, k = 0, a = 0, b = 0, q = 0;
     uint64_t strip = 0;                  // slab passes: strip width in bytes
     int cluster = 1;                     // kSlabCluster: CTAs per matrix
+    uint64_t band = 0;                   // kSlabCluster: 0 row bands; else columns per CTA (column bands)
     // block moves
     uint64_t block = 0, n_blocks = 0, src_pitch = 0, dst_pitch = 0;
     // slab and block permutations: the permuted axes (fastest first) and the
@@ -100,6 +101,8 @@ struct Tuning {
                              // wrap the fastest output axis once step it with one jump; 2: every run steps
                              // through the axes element by element)
     int slab_prefetch = 1;   // slab permutations at one CTA per SM: the next slab prefetched into registers
+    int slab_colband = 256;  // cluster slabs whose row bands give output rows fewer bytes per CTA than this
+                             // write column bands (contiguous output ranges); 0 never
     int narrow_words = 1;    // contiguous ranges of 1- and 2-byte units are staged from aligned 4-byte words
     int row_solo_kb = 48;    // rows held by one CTA above this many KB run one CTA per SM with the next
                              // row prefetched into registers (up to 128 KB), smaller ones two or more per SM

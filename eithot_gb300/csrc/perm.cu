@@ -2,6 +2,7 @@
 // (search.cpp): the slab permutation (leading axes of every slab permuted on
 // chip) and the block permutation (blocks of leading axes moved along the
 // permutation's cycles).
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -445,6 +446,155 @@ __global__ void __launch_bounds__(512) k_slab_queue(const SlabRunArgs* entries, 
 static_assert(sizeof(SlabRunArgs) % 4 == 0, "queue entries are copied in words");
 
 // ---------------------------------------------------------------------------
+// Column-band cluster slab: B matrices of R x C elements with few rows, each
+// transposed in one pass by a cluster of K CTAs.  CTA k stages the band of
+// columns [k P, k P + w) of every row (R segments of w E bytes, from the
+// aligned 4-byte words around them), the cluster synchronises (every CTA's
+// loads of a matrix precede any CTA's writes to it), and CTA k writes output
+// rows k P .. k P + w - 1: one contiguous range of w R elements, written in
+// runs of V-byte stores from its own shared memory (the run kernel's
+// write-back of a w x R slab).  The row-band form (k_slab_cluster) writes a
+// band's Q = R / K elements into every output row instead: a few bytes each
+// when R is small.
+// ---------------------------------------------------------------------------
+struct ColBandArgs {
+    uint8_t* base;
+    uint64_t items, mat_bytes, row_bytes;
+    uint32_t R, C, E, P;
+    // su = 4, 8 or 16: every row segment (and its padded row in shared
+    // memory) starts on an su-byte boundary and is su-byte units long, staged
+    // by cp.async; su = 0: segments at any alignment, staged from the aligned
+    // 4-byte words around them.  wpr_* = staging units (or words) per row.
+    uint32_t su;
+    uint32_t wpr_full, wpr_last;
+    FastDiv32 div_full, div_last;
+    // any_align: some band's output range does not start on a store-width
+    // boundary (an odd base or matrix size): written in aligned 4-byte words
+    // gathered byte by byte (div_R: output element -> (output row, element))
+    uint32_t any_align;
+    FastDiv32 div_R;
+    SlabRunArgs full, last;       // write-back of a band of P columns / of the last band
+};
+
+// Byte b of a band's output range: output element o = b / E of the w x R
+// output block (output row j = o / R = column j of the band, element i = o % R
+// = row i), read from the staged band.
+template <int E>
+__device__ __forceinline__ uint32_t colband_byte(const ColBandArgs& a, const uint8_t* smem, uint32_t pitch,
+                                                 uint32_t b) {
+    uint32_t j, i;
+    a.div_R.divmod(b / E, j, i);
+    return smem[i * pitch + j * E + b % E];
+}
+
+// Writes a band's output range of n bytes at any alignment: the aligned words
+// inside it as whole words, the at most 3 bytes before and after one by one.
+template <int E>
+__device__ __forceinline__ void colband_write_any(const ColBandArgs& a, const uint8_t* smem, uint32_t pitch,
+                                                  uint8_t* out, uint32_t n) {
+    const uint32_t head = min(n, static_cast<uint32_t>((4 - (reinterpret_cast<uintptr_t>(out) & 3u)) & 3u));
+    const uint32_t words = (n - head) / 4;
+    for (uint32_t x = threadIdx.x; x < words; x += blockDim.x) {
+        const uint32_t b = head + 4 * x;
+        uint32_t v = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) v |= colband_byte<E>(a, smem, pitch, b + k) << (8 * k);
+        *reinterpret_cast<uint32_t*>(out + b) = v;
+    }
+    const uint32_t rest = head + (n - head - words * 4);  // bytes outside whole words
+    for (uint32_t x = threadIdx.x; x < rest; x += blockDim.x) {
+        const uint32_t b = x < head ? x : head + words * 4 + (x - head);
+        out[b] = static_cast<uint8_t>(colband_byte<E>(a, smem, pitch, b));
+    }
+}
+
+// Stages the band's R row segments of wb bytes, each starting row_bytes after
+// the previous one at `seg`, into rows of `pitch` bytes of shared memory.
+__device__ __forceinline__ void colband_stage(const ColBandArgs& a, uint8_t* smem, const uint8_t* seg,
+                                              uint32_t pitch, uint32_t wb, uint32_t wpr, const FastDiv32& dv) {
+    const uint32_t total = a.R * wpr;
+    if (a.su >= 4) {
+        for (uint32_t x = threadIdx.x; x < total; x += blockDim.x) {
+            uint32_t r, u;
+            dv.divmod(x, r, u);
+            uint8_t* sd = smem + r * pitch + u * a.su;
+            const uint8_t* gs = seg + static_cast<uint64_t>(r) * a.row_bytes + u * a.su;
+            if (a.su == 16)
+                stage_unit<16>(sd, gs);
+            else if (a.su == 8)
+                stage_unit<8>(sd, gs);
+            else
+                stage_unit<4>(sd, gs);
+        }
+        asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+        return;
+    }
+    // four word loads in flight per thread before their bytes are placed
+    constexpr int kDepth = 4;
+    for (uint32_t x0 = threadIdx.x; x0 < total; x0 += kDepth * blockDim.x) {
+        uint32_t v[kDepth], r[kDepth], b[kDepth];
+        bool ok[kDepth];
+#pragma unroll
+        for (int j = 0; j < kDepth; ++j) {
+            const uint32_t x = x0 + j * blockDim.x;
+            ok[j] = false;
+            if (x < total) {
+                uint32_t q;
+                dv.divmod(x, r[j], q);
+                const uintptr_t lo = reinterpret_cast<uintptr_t>(seg + static_cast<uint64_t>(r[j]) * a.row_bytes);
+                const uint32_t head = static_cast<uint32_t>(lo & 3u);
+                if (q * 4 < head + wb) {
+                    v[j] = *reinterpret_cast<const uint32_t*>(lo - head + q * 4);
+                    b[j] = q * 4 - head;  // byte of the segment the word starts at (wraps below 0)
+                    ok[j] = true;
+                }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < kDepth; ++j) {
+            if (!ok[j]) continue;
+            uint8_t* dst = smem + r[j] * pitch;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const uint32_t ob = b[j] + k;  // wraps below 0 for the head's bytes
+                if (ob < wb) dst[ob] = static_cast<uint8_t>(v[j] >> (8 * k));
+            }
+        }
+    }
+}
+
+template <int E, int V>
+__global__ void __launch_bounds__(512) k_slab_colband(ColBandArgs a) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    const unsigned K = cl.num_blocks(), kr = cl.block_rank();
+    const uint64_t cid = blockIdx.x / K, ncl = gridDim.x / K;
+    const uint32_t c0 = kr * a.P;
+    const uint32_t w = c0 < a.C ? min(a.P, a.C - c0) : 0;
+    const bool last = w != a.P;
+    const SlabRunArgs& s = last ? a.last : a.full;
+    const uint32_t wb = w * a.E;
+    const uint32_t wpr = last ? a.wpr_last : a.wpr_full;
+    const FastDiv32& dv = last ? a.div_last : a.div_full;
+    for (uint64_t it = cid; it < a.items; it += ncl) {
+        uint8_t* mat = a.base + it * a.mat_bytes;
+        if (w > 0) colband_stage(a, smem, mat + static_cast<uint64_t>(c0) * a.E, s.pitch, wb, wpr, dv);
+        __syncthreads();
+        asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+        asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+        if (w > 0) {
+            uint8_t* out = mat + static_cast<uint64_t>(c0) * a.R * a.E;
+            if (a.any_align)
+                colband_write_any<E>(a, smem, s.pitch, out, w * a.R * a.E);
+            else
+                write_runs<E, V>(s, smem, out);
+        }
+        __syncthreads();  // shared memory is free for the next matrix
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Block permutation along cycles.  Blocks of `blk` bytes are indexed by q
 // axes; the block at output index t comes from input index src(t).  The
 // cycles are cut into segments (host table): a first launch copies the block
@@ -691,7 +841,7 @@ void set_aligned_runs(SlabRunArgs* a, uint64_t K) {
 // Fills the run kernel's arguments for pass p (count elements per slab);
 // false when the kernel does not apply.  *V: the store width.
 bool make_slab_runs(uint8_t* data, const Pass& p, uint64_t count, const DeviceCaps& caps, SlabRunArgs* out,
-                    size_t* smem_out, uint64_t* V_out) {
+                    size_t* smem_out, uint64_t* V_out, uint64_t V_force = 0) {
     const uint64_t E = p.elem;
     if (!(E == 1 || E == 2 || E == 4 || E == 8 || E == 16) || (p.strip && p.strip != E)) return false;
     const int q = static_cast<int>(p.nd_dims.size());
@@ -705,7 +855,9 @@ bool make_slab_runs(uint8_t* data, const Pass& p, uint64_t count, const DeviceCa
     uint8_t* base = data + p.offset;
     const uint64_t addr = reinterpret_cast<uintptr_t>(base);
     const uint64_t slab_bytes = count * E;
-    const uint64_t V = pow2_unit({addr, slab_bytes});
+    // V_force: the caller has checked that the slab's start is V_force-aligned
+    // (runs of whole stores, the remainder written element by element)
+    const uint64_t V = V_force ? V_force : pow2_unit({addr, slab_bytes});
     if (V < std::max<uint64_t>(4, E)) return false;  // stores of at least a word (and a whole element)
     SlabRunArgs& a = *out;
     std::memset(&a, 0, sizeof(a));
@@ -762,6 +914,136 @@ int try_slab_runs(uint8_t* data, const Pass& p, uint64_t count, ExecContext& ctx
 }
 
 }  // namespace
+
+namespace {
+
+template <int E, int V>
+int launch_colband(const ColBandArgs& a, int K, size_t smem, ExecContext& ctx) {
+    auto kern = k_slab_colband<E, V>;
+    PM_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    if (K > 8) PM_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = K;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(512);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = ctx.stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cfg.gridDim = dim3(static_cast<unsigned>(K * 1024));
+    int max_clusters = 0;
+    PM_CHECK(cudaOccupancyMaxActiveClusters(&max_clusters, kern, &cfg));
+    if (max_clusters < 1) {
+        ctx.err = "column-band cluster slab: no cluster fits";
+        return EITHOT_STATUS_CUDA;
+    }
+    cfg.gridDim = dim3(static_cast<unsigned>(std::min<uint64_t>(a.items, static_cast<uint64_t>(max_clusters)) * K));
+    PM_CHECK(cudaLaunchKernelEx(&cfg, kern, a));
+    ctx.launches++;
+    return 0;
+}
+
+template <int E>
+int colband_v(const ColBandArgs& a, int K, size_t smem, uint64_t V, ExecContext& ctx) {
+    if constexpr (E <= 4) {
+        if (V == 16) return launch_colband<E, 16>(a, K, smem, ctx);
+        if (V == 8) return launch_colband<E, 8>(a, K, smem, ctx);
+        return launch_colband<E, 4>(a, K, smem, ctx);
+    } else if constexpr (E == 8) {
+        if (V == 16) return launch_colband<E, 16>(a, K, smem, ctx);
+        return launch_colband<E, 8>(a, K, smem, ctx);
+    } else {
+        return launch_colband<E, 16>(a, K, smem, ctx);
+    }
+}
+
+}  // namespace
+
+// The write-back arguments of a band of w columns of a matrix with R rows
+// whose output range starts at `out` (false when the run kernel does not
+// apply, e.g. stores narrower than a word).
+static bool colband_runs(uint8_t* out, uint64_t w, uint64_t R, uint64_t E, uint64_t V, const DeviceCaps& caps,
+                         SlabRunArgs* a, size_t* smem) {
+    Pass q;
+    q.type = kSlabPerm;
+    q.batches = 1;
+    q.elem = E;
+    q.strip = E;
+    q.nd_dims = {w, R};
+    q.nd_perm = {1, 0};
+    uint64_t Vo = 0;
+    return make_slab_runs(out, q, w * R, caps, a, smem, &Vo, V);
+}
+
+int run_slab_colband(uint8_t* data, const Pass& p, ExecContext& ctx) {
+    ColBandArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.base = data + p.offset;
+    a.items = p.batches;
+    a.R = static_cast<uint32_t>(p.rows);
+    a.C = static_cast<uint32_t>(p.cols);
+    a.E = static_cast<uint32_t>(p.elem);
+    a.P = static_cast<uint32_t>(p.band);
+    a.row_bytes = p.cols * p.elem;
+    a.mat_bytes = p.rows * a.row_bytes;
+    const int K = static_cast<int>((p.cols + p.band - 1) / p.band);
+    if (K < 2 || K > 16) return -1;
+    const uint64_t wl = p.cols - static_cast<uint64_t>(K - 1) * p.band;  // the last band's columns
+    size_t smem_f = 0, smem_l = 0;
+    // one store width for every band of every matrix: band k's output starts
+    // k P R E bytes into its matrix, matrix b b mat_bytes into the tensor
+    uint64_t Vf = pow2_unit({reinterpret_cast<uintptr_t>(a.base), static_cast<uint64_t>(a.P) * a.R * a.E,
+                             a.items > 1 ? a.mat_bytes : 0});
+    const uint64_t Vmin = std::max<uint64_t>(4, a.E);
+    auto runs = [&](uint64_t V) {
+        return colband_runs(a.base, a.P, a.R, a.E, V, ctx.caps, &a.full, &smem_f) &&
+               colband_runs(a.base, wl, a.R, a.E, V, ctx.caps, &a.last, &smem_l);
+    };
+    // The store width: elements of 4-16 bytes take the widest (runs of at
+    // most 4 elements: table offsets, one jump or a short carry chain).  1-
+    // and 2-byte elements take the widest whose runs have table offsets, else
+    // the widest whose runs wrap the output row once; runs that would walk a
+    // carry chain of 8-16 elements (odd or short output rows) and ranges off
+    // the store width take the any-alignment write instead.
+    if (Vf < Vmin) {
+        a.any_align = 1;
+        Vf = Vmin;
+    } else if (a.E < 4) {
+        uint64_t pick = 0;
+        for (uint64_t V = Vf; V >= Vmin && !pick; V /= 2)
+            if (runs(V) && a.full.aligned && a.last.aligned) pick = V;
+        if (!pick && runs(Vf) && a.full.wrap && a.last.wrap) pick = Vf;
+        if (pick)
+            Vf = pick;
+        else
+            a.any_align = 1;
+    }
+    a.div_R = FastDiv32::make(a.R);
+    if (!runs(Vf)) return -1;
+    const uint64_t su = pow2_unit({reinterpret_cast<uintptr_t>(a.base), a.row_bytes, static_cast<uint64_t>(a.P) * a.E,
+                                   wl * a.E, a.full.pitch, a.last.pitch, a.items > 1 ? a.mat_bytes : 0});
+    a.su = su >= 4 ? static_cast<uint32_t>(su) : 0;
+    if (a.su) {
+        a.wpr_full = a.P * a.E / a.su;
+        a.wpr_last = static_cast<uint32_t>(wl * a.E / a.su);
+    } else {
+        a.wpr_full = (a.P * a.E + 3) / 4 + 1;
+        a.wpr_last = static_cast<uint32_t>((wl * a.E + 3) / 4 + 1);
+    }
+    a.div_full = FastDiv32::make(a.wpr_full);
+    a.div_last = FastDiv32::make(a.wpr_last);
+    const size_t smem = std::max(smem_f, smem_l);
+    switch (p.elem) {
+        case 1: return colband_v<1>(a, K, smem, Vf, ctx);
+        case 2: return colband_v<2>(a, K, smem, Vf, ctx);
+        case 4: return colband_v<4>(a, K, smem, Vf, ctx);
+        case 8: return colband_v<8>(a, K, smem, Vf, ctx);
+        default: return colband_v<16>(a, K, smem, Vf, ctx);
+    }
+}
 
 size_t slab_queue_entry_bytes() { return sizeof(SlabRunArgs); }
 

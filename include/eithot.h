@@ -323,6 +323,10 @@ int eithot_estimate_report(int rank, const int64_t* dims, const int* perm_1based
  *                 output axis with one jump where a run wraps it at most once
  *                 (default); 2 the runs step through every axis per element;
  *                 0 one divide chain per element
+ *   "slab_colband" 256 cluster slabs whose row bands would give each output
+ *                 row fewer bytes per CTA than this (0..4096) take column
+ *                 bands instead (each CTA writes one contiguous range of the
+ *                 output); 0 always row bands
  *   "narrow_words" 1 contiguous ranges of 1- and 2-byte units (slabs, row
  *                 pieces, bands, column row pieces) are staged from the aligned
  *                 4-byte words around them (default), 0 unit by unit

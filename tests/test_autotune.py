@@ -57,7 +57,7 @@ def test_autotune_keeps_results_exact(E):
 
 KNOB_VALUES = {"dbuf": 0, "max_cluster": 8, "variant": 1, "col_batch": 8, "col_chunk": 256, "col_owner": 0,
                "col_form": 1, "row_prefetch": 0, "row_block": 0, "slab_pack": 0, "slab_cluster": 0, "factor": 0,
-               "sync_sleep_ns": 32, "sync_spin_limit": 4096, "sync_relaxed": 0, "group_per_sm": 2, "l2_prefetch": 1, "col_bulk": 1, "cycle_moves": 0, "slab_perm": 2, "slab_runs": 0, "slab_prefetch": 0, "slab2d_runs": 2, "row_solo_kb": 64, "batch_graph": 0, "batch_queue": 0, "batch_lanes": 8, "narrow_words": 0}
+               "sync_sleep_ns": 32, "sync_spin_limit": 4096, "sync_relaxed": 0, "group_per_sm": 2, "l2_prefetch": 1, "col_bulk": 1, "cycle_moves": 0, "slab_perm": 2, "slab_runs": 0, "slab_prefetch": 0, "slab2d_runs": 2, "row_solo_kb": 64, "batch_graph": 0, "batch_queue": 0, "batch_lanes": 8, "narrow_words": 0, "slab_colband": 0}
 
 
 def test_every_knob_round_trips(E):
@@ -74,7 +74,7 @@ def test_every_knob_round_trips(E):
 
 
 @pytest.mark.parametrize("key,value", [("max_cluster", 3), ("variant", 3), ("col_form", 5), ("group_per_sm", 7),
-                                       ("sync_sleep_ns", -1), ("sync_spin_limit", -1), ("slab_perm", 3), ("slab_runs", 3), ("slab2d_runs", 3), ("cycle_moves", 3), ("row_solo_kb", 8), ("batch_lanes", 0), ("col_chunk", 100), ("no_such_knob", 1)])
+                                       ("sync_sleep_ns", -1), ("sync_spin_limit", -1), ("slab_perm", 3), ("slab_runs", 3), ("slab2d_runs", 3), ("cycle_moves", 3), ("row_solo_kb", 8), ("slab_colband", 5000), ("batch_lanes", 0), ("col_chunk", 100), ("no_such_knob", 1)])
 def test_invalid_knob_values_are_refused(E, key, value):
     old = E.tune_get(key) if key != "no_such_knob" else None
     with pytest.raises(E.EithotError) as ei:

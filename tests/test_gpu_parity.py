@@ -87,7 +87,8 @@ def test_catanzaro_2d(E, R, C, elem):
 @pytest.fixture
 def tuned(E):
     keys = ("variant", "col_owner", "col_chunk", "max_cluster", "dbuf", "col_form", "row_prefetch", "row_block",
-            "slab_pack", "slab_cluster", "factor", "sync_relaxed", "group_per_sm", "col_bulk", "narrow_words")
+            "slab_pack", "slab_cluster", "factor", "sync_relaxed", "group_per_sm", "col_bulk", "narrow_words",
+            "slab_colband")
     saved = {k: E.tune_get(k) for k in keys}
 
     def set_(**kw):
@@ -291,6 +292,26 @@ def test_cluster_slabs_of_narrow_odd_rows(E, dims, elem, offset):
     and the fewest-pass plans."""
     for order in (0, 3):
         run_case(E, dims, [2, 1], elem, order=order, offset=offset * elem % 4 if elem == 2 else offset)
+
+
+@pytest.mark.parametrize("colband", [4096, 0])
+@pytest.mark.parametrize("offset", [0, 4, 8, 1])
+def test_cluster_slabs_in_column_bands(E, tuned, colband, offset):
+    """Matrices with few rows beyond one CTA's shared memory: each CTA of the
+    cluster stages a band of columns of every row and writes its contiguous
+    range of the output (knob slab_colband=4096: wherever a band fits; 0 keeps
+    row bands, or Catanzaro passes for rows longer than a CTA's shared
+    memory), one to three matrices, 1- to 16-byte elements, bases on 16-, 8-,
+    4- and 1-byte boundaries, odd matrix sizes (ranges off the store width:
+    the any-alignment write)."""
+    tuned(slab_colband=colband)
+    for dims, elem in [([41125, 20, 3], 1), ([20011, 8, 2], 2), ([12000, 12, 1], 4), ([9000, 6, 2], 8),
+                       ([5000, 4, 2], 16), ([70001, 9, 1], 1), ([30001, 5, 3], 2), ([5003, 61, 3], 1),
+                       ([300001, 5, 2], 1), ([130001, 6, 2], 2), ([70001, 4, 1], 4), ([40000, 3, 2], 8),
+                       ([20000, 5, 1], 16)]:
+        if offset % elem and offset < elem:
+            continue
+        run_case(E, dims, [2, 1, 3], elem, offset=offset)
 
 
 @pytest.mark.parametrize("words", [1, 0])

@@ -191,3 +191,21 @@ def test_fewest_pass_plans_named_shapes(hostsim, dims, perm, elem):
     """Shapes whose searched plans use cycle-following block permutations
     (4-32 KB blocks), slab permutations of 2-6 axes and factor splits."""
     assert run(hostsim, dims, perm, elem, order=3)
+
+
+@pytest.mark.parametrize("dims,elem", [([41125, 20, 2], 1), ([300001, 5], 1), ([130001, 6, 2], 2), ([70001, 4], 4),
+                                       ([40000, 3], 8), ([20000, 5], 16)])
+def test_column_band_slabs(hostsim, dims, elem):
+    """Few-row matrices beyond two slabs per SM are transposed in one pass by
+    a column-band cluster slab, also when a row is longer than one CTA's
+    shared memory (the row-band form cannot stage it, and the matrix would
+    otherwise take two or three Catanzaro passes); the pass list still
+    produces the oracle's permutation."""
+    r = len(dims)
+    perm = [2, 1] + list(range(3, r + 1))
+    describe = ctypes.create_string_buffer(1 << 14)
+    hostsim.hs_describe(describe, len(describe), r, (ctypes.c_int64 * r)(*dims), (ctypes.c_int * r)(*perm),
+                        elem, 1, ctypes.c_double(0.01), 0)
+    passes = describe.value.decode().splitlines()
+    assert len(passes) == 1 and passes[0].startswith("slab-colband"), passes
+    assert run(hostsim, dims, perm, elem)
