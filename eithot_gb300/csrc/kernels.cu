@@ -133,7 +133,60 @@ struct SlabArgs {
     FastDiv div_strips;
     FastDiv32 div_C, div_R, div_upw, div_rowunits;
     uint32_t nstrips;
+    // pieces (an element's strip: up to w bytes at any alignment) moved in
+    // the aligned 4-byte words around them: `slots` words per piece
+    bool words;
+    uint32_t slots;
+    FastDiv32 div_slots;
 };
+
+// Slab of 1- or 2-byte units in pieces of L bytes (piece p of the input
+// starts p*E bytes after `mat`, staged at (p / C)*pitch + (p % C)*w): every
+// piece read in the aligned words around it (bytes outside it dropped; a
+// word never crosses a page), transposed, and written as the aligned words
+// inside each output piece, the at most 3 bytes at either end one by one
+// (the words there hold other pieces' bytes).
+__device__ __forceinline__ void slab_pieces_words(const SlabArgs& a, uint8_t* smem, uint8_t* mat, uint32_t L) {
+    const uint32_t total = a.R * a.C * a.slots;
+    for (uint32_t x = threadIdx.x; x < total; x += blockDim.x) {
+        uint32_t p, k, r, c;
+        a.div_slots.divmod(x, p, k);
+        const uintptr_t lo = reinterpret_cast<uintptr_t>(mat + static_cast<uint64_t>(p) * a.E);
+        const uint32_t h = static_cast<uint32_t>(lo & 3u);
+        if (4 * k >= h + L) continue;
+        const uint32_t v = *reinterpret_cast<const uint32_t*>(lo - h + 4 * k);
+        a.div_C.divmod(p, r, c);
+        uint8_t* dst = smem + r * a.pitch + c * a.w;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t b = 4 * k + j - h;  // wraps below 0 for the bytes before the piece
+            if (b < L) dst[b] = static_cast<uint8_t>(v >> (8 * j));
+        }
+    }
+    __syncthreads();
+    for (uint32_t x = threadIdx.x; x < total; x += blockDim.x) {
+        uint32_t o, k, c, r;
+        a.div_slots.divmod(x, o, k);
+        a.div_R.divmod(o, c, r);  // output o = c*R + r holds input (r, c)
+        const uint8_t* src = smem + r * a.pitch + c * a.w;
+        const uintptr_t lo = reinterpret_cast<uintptr_t>(mat + static_cast<uint64_t>(o) * a.E);
+        const uint32_t h = static_cast<uint32_t>(lo & 3u);
+        if (4 * k >= h + L) continue;
+        const uint32_t b0 = 4 * k - h;
+        if (4 * k >= h && b0 + 4 <= L) {
+            const uint32_t v = static_cast<uint32_t>(src[b0]) | static_cast<uint32_t>(src[b0 + 1]) << 8 |
+                               static_cast<uint32_t>(src[b0 + 2]) << 16 | static_cast<uint32_t>(src[b0 + 3]) << 24;
+            *reinterpret_cast<uint32_t*>(lo - h + 4 * k) = v;
+        } else {
+            uint8_t* dst = reinterpret_cast<uint8_t*>(lo - h + 4 * k);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const uint32_t b = b0 + j;
+                if (b < L) dst[j] = src[b];
+            }
+        }
+    }
+}
 
 template <int US, int kPack>
 __global__ void __launch_bounds__(kThreads) k_slab(SlabArgs a) {
@@ -145,6 +198,13 @@ __global__ void __launch_bounds__(kThreads) k_slab(SlabArgs a) {
         a.div_strips.divmod(it, b, s);
         const uint32_t lim = (s + 1 == a.nstrips) ? a.last_upw : a.upw;
         uint8_t* mat = a.base + b * a.mat_bytes + s * a.w;
+        if constexpr (US < 4 && kPack == 1) {
+            if (a.words) {
+                slab_pieces_words(a, smem, mat, lim * US);
+                __syncthreads();
+                continue;
+            }
+        }
         if (a.flat) {
             // the slab is R*C*E contiguous bytes: row r of the staging holds
             // bytes [r*C*E, (r+1)*C*E)
@@ -1648,6 +1708,11 @@ int launch_slab(uint8_t* data, const Pass& p, ExecContext& ctx) {
     constexpr int kPack = US < 4 ? 4 / US : 1;
     const bool pack = kPack > 1 && a.flat && p.elem == US && a.nstrips == 1 &&
                       reinterpret_cast<uintptr_t>(a.base) % 4 == 0 && a.mat_bytes % 4 == 0;
+    // pieces of 16 bytes or more in words (shorter ones gain nothing: their
+    // words are mostly partial)
+    a.words = US < 4 && !pack && std::min<uint64_t>(p.strip, p.elem) >= 16 && tuning().narrow_words;
+    a.slots = (a.w + 3) / 4 + 1;
+    a.div_slots = FastDiv32::make(a.slots);
     const void* k = pack ? reinterpret_cast<const void*>(&k_slab<US, kPack>)
                          : reinterpret_cast<const void*>(&k_slab<US, 1>);
     EI_CHECK(prep_smem(k, smem));

@@ -76,6 +76,20 @@ int log2i(int K) {
 // items moved in granules of g bytes through distributed shared memory
 // (measured on GB300: 128-byte pulls lose ~10-15% per doubling, 16-byte
 // pulls 40-70%, 16-byte pushes ~30%).
+// Modelled cost, per doubling of the cluster, of a row pass that moves 1- or
+// 2-byte granules through distributed shared memory.
+constexpr double kNarrowRemote = 3.0;
+// Extra modelled cost of a Catanzaro pass whose elements move in 1-byte
+// units (odd sizes; an index map per byte: 40-600 GB/s measured on such
+// passes), half of it for 2-byte units.
+constexpr double kNarrowPass = 4.0;
+
+double narrow_pass_cost(uint64_t E) {
+    if (E % 2) return kNarrowPass;
+    if (E % 4) return kNarrowPass / 2;
+    return 0.0;
+}
+
 double dsmem_penalty(uint64_t g, bool push) {
     if (g >= 128) return 0.12;
     if (g >= 64) return 0.2;
@@ -165,8 +179,10 @@ Staging plan_row_staging(uint64_t cols, uint64_t E, size_t cap, bool scatter) {
                     s.w = w; s.K = K; s.per_cta = per; s.item_bytes = cols * w;
                     s.on_chip = true; s.dbuf = db;
                     // 16-32 byte granules are pushed whatever the pass's own
-                    // direction (the inverse map turns a gather into a scatter)
-                    s.cost = 1.0 + dsmem_penalty(w, true) * log2i(K) + (db ? 0.0 : 0.1) +
+                    // direction (the inverse map turns a gather into a scatter);
+                    // 1- and 2-byte granules cost one remote access each
+                    // (rows of 0.3-2 MB over 16 CTAs: 75-370 GB/s)
+                    s.cost = 1.0 + (w < 4 ? kNarrowRemote : dsmem_penalty(w, true)) * log2i(K) + (db ? 0.0 : 0.1) +
                              (foot > kTwoPerSm ? kOnePerSmPenalty : 0.0);
                     return s;
                 }
@@ -469,13 +485,13 @@ double passes_cost(const std::vector<Pass>& ps, const DeviceCaps& caps, bool* st
             case kRowScatter: {
                 const Staging st = plan_row_staging(p.cols, p.elem, cap, p.type == kRowScatter);
                 if (!st.on_chip) *staged = true;
-                c += st.on_chip ? st.cost : 3.0;
+                c += (st.on_chip ? st.cost : 3.0) + narrow_pass_cost(p.elem);
                 break;
             }
             case kColGather: {
                 const Staging st = plan_col_pass(p, caps);
                 if (!st.on_chip) *staged = true;
-                c += st.on_chip ? st.cost : 3.0;
+                c += (st.on_chip ? st.cost : 3.0) + narrow_pass_cost(p.elem);
                 break;
             }
             default: break;
@@ -502,9 +518,10 @@ std::vector<uint64_t> divisors(uint64_t v, size_t limit) {
 }  // namespace
 
 // A batched transpose whose Catanzaro passes would stage through global
-// scratch (a row or a column too long for on-chip staging) may instead be
-// split along a factorisation of its rows R = Ra*Rb (or columns C = Ca*Cb)
-// into two transposes that each stay on chip:
+// scratch (a row or a column too long for on-chip staging), or of elements
+// that move in 1- or 2-byte units, may instead be split along a
+// factorisation of its rows R = Ra*Rb (or columns C = Ca*Cb) into two
+// transposes of wider granules:
 //   R: Rb x C matrices (B*Ra of them), then Ra x C with elements of Rb*E bytes;
 //   C: R x Ca with elements of Cb*E bytes, then R x Cb matrices (B*Ca of them).
 void lower_xpose(const Xpose& x, const DeviceCaps& caps, std::vector<Pass>* passes) {
@@ -513,7 +530,10 @@ void lower_xpose(const Xpose& x, const DeviceCaps& caps, std::vector<Pass>* pass
     lower_xpose_direct(x, caps, &direct);
     bool staged = false;
     const double direct_cost = passes_cost(direct, caps, &staged);
-    if (!staged || !tuning().factor) {
+    bool narrow = false;  // a Catanzaro pass of 1- or 2-byte units
+    for (const Pass& p : direct)
+        narrow = narrow || ((p.type == kRowGather || p.type == kRowScatter || p.type == kColGather) && p.elem % 4);
+    if ((!staged && !narrow) || !tuning().factor) {
         passes->insert(passes->end(), direct.begin(), direct.end());
         return;
     }

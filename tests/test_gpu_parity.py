@@ -109,7 +109,8 @@ def test_column_kernels_all_forms(E, tuned, R, C, elem, variant, form):
     with owner-computed column passes synchronised by a cluster or by a
     group of co-resident CTAs, on shapes with gcd 1 and gcd > 1
     (rotations), rows fewer than a tile's halo and wide elements."""
-    tuned(variant=variant, col_owner=0 if form == "gather" else 1,
+    # factoring off: 1- and 2-byte transposes keep their Catanzaro passes
+    tuned(variant=variant, col_owner=0 if form == "gather" else 1, factor=0,
           col_form={"gather": 0, "cluster": 1, "group": 2}[form])
     run_case(E, [C, R], [2, 1], elem)
 
@@ -120,7 +121,7 @@ def test_column_kernels_all_forms(E, tuned, R, C, elem, variant, form):
 def test_column_tilings(E, tuned, chunk, max_cluster, dbuf, form):
     """Row-piece widths, cluster sizes, CTA groups and single/double
     buffering of the column passes (the autotuner's search space)."""
-    tuned(col_chunk=chunk, max_cluster=max_cluster, dbuf=dbuf, col_form=form)
+    tuned(col_chunk=chunk, max_cluster=max_cluster, dbuf=dbuf, col_form=form, factor=0)
     for variant in (1, 2):
         E.tune_set("variant", variant)
         run_case(E, [4096, 3001], [2, 1], 4)
@@ -134,7 +135,7 @@ def test_group_arrivals_and_residency(E, tuned, relaxed, per_sm):
     """Group column passes with release and with relaxed arrivals, at one to
     three CTAs per SM (row tables in shared memory sized for each), c2r and
     r2c, gcd 1 and gcd > 1, 1- to 32-byte and 3-byte elements."""
-    tuned(col_form=2, dbuf=0, sync_relaxed=relaxed, group_per_sm=per_sm)
+    tuned(col_form=2, dbuf=0, sync_relaxed=relaxed, group_per_sm=per_sm, factor=0)
     for variant in (1, 2):
         E.tune_set("variant", variant)
         run_case(E, [4096, 3001], [2, 1], 4)
@@ -167,7 +168,7 @@ def test_row_prefetch(E, tuned, dims, perm, elem, prefetch):
     """Rows of 110-128 KB (one CTA per SM) with and without the register
     prefetch of the next row, including rows that leave some threads'
     last units empty."""
-    tuned(variant=2, row_prefetch=prefetch)
+    tuned(variant=2, row_prefetch=prefetch, factor=0)
     run_case(E, dims, perm, elem)
 
 
@@ -179,7 +180,7 @@ def test_row_prefetch(E, tuned, dims, perm, elem, prefetch):
 def test_tall_skinny_rows_in_blocks(E, tuned, dims, perm, elem, variant, block):
     """Matrices of a few columns (rows of a few bytes): row passes staged as
     blocks of consecutive rows, and the one-row-per-item form."""
-    tuned(variant=variant, row_block=block)
+    tuned(variant=variant, row_block=block, factor=0)
     run_case(E, dims, perm, elem)
 
 
@@ -315,12 +316,30 @@ def test_cluster_slabs_in_column_bands(E, tuned, colband, offset):
 
 
 @pytest.mark.parametrize("words", [1, 0])
-def test_narrow_units_staged_from_words(E, tuned, words):
+@pytest.mark.parametrize("offset", [0, 1, 2, 3])
+def test_slabs_of_odd_wide_elements(E, tuned, words, offset):
+    """One-CTA slabs of wide elements whose size is odd or 2 mod 4 (1- and
+    2-byte units), whole or in strips of 128-byte multiples: every piece read
+    and written in the aligned words around it, its end bytes one by one
+    (knob narrow_words=1), or unit by unit (0); bases off word boundaries,
+    one to three matrices."""
+    tuned(narrow_words=words)
+    # the first axis stays in place: elements of its length (x elem) bytes
+    for dims, elem in [([74359, 24, 28], 1), ([22701, 230, 8], 1), ([5193, 272, 25], 2), ([4095, 17, 5, 3], 1),
+                       ([17, 300, 20], 1), ([1001, 7, 9, 2], 1)]:
+        perm = [1, 3, 2] + list(range(4, len(dims) + 1))
+        run_case(E, dims, perm, elem, offset=offset)
+
+
+@pytest.mark.parametrize("words", [1, 0])
+@pytest.mark.parametrize("factor", [0, 1])
+def test_narrow_units_staged_from_words(E, tuned, words, factor):
     """1- and 2-byte elements whose rows are not whole 4-byte words, through
-    Catanzaro row and column passes, row blocks, packed and cluster slabs:
+    Catanzaro row and column passes (factor=0), or split into transposes of
+    wider granules (factor=1), row blocks, packed and cluster slabs:
     contiguous ranges staged from the aligned words around them (knob
     narrow_words=1) or unit by unit (0), at bases off word boundaries."""
-    tuned(narrow_words=words)
+    tuned(narrow_words=words, factor=factor)
     for dims, perm, elem, offset in [([5003, 999], [2, 1], 1, 1), ([2001, 513], [2, 1], 2, 2), ([7, 130001], [2, 1], 1, 3),
                                      ([130001, 7], [2, 1], 1, 0), ([33, 1000, 31], [3, 1, 2], 1, 1),
                                      ([3, 40001, 5], [2, 3, 1], 2, 2), ([301, 77, 13], [2, 1, 3], 1, 3),

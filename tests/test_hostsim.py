@@ -96,16 +96,22 @@ def test_row_shuffle_inverse(hostsim, dims, perm, elem):
 def test_owner_maps_match_column_gathers(hostsim, dims, perm, elem):
     """Owner-computed column passes (each CTA writes whole output row pieces
     from the source rows it staged itself, plus a halo) write exactly what
-    the column gathers of both the c2r and the r2c variant write."""
+    the column gathers of both the c2r and the r2c variant write.  Factoring
+    is off, so 1- and 2-byte transposes keep their Catanzaro passes."""
     import ctypes
     r = len(dims)
+    hostsim.hs_tune.argtypes = [ctypes.c_char_p, ctypes.c_int]
     hostsim.hs_check_owner.restype = ctypes.c_long
     hostsim.hs_check_owner.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int),
                                        ctypes.c_size_t, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_long,
                                        ctypes.POINTER(ctypes.c_long)]
     visited = ctypes.c_long()
-    bad = hostsim.hs_check_owner(r, (ctypes.c_int64 * r)(*dims), (ctypes.c_int * r)(*perm), elem, 1, 0.01, 0,
-                                 300000, ctypes.byref(visited))
+    try:
+        assert hostsim.hs_tune(b"factor", 0) == 0
+        bad = hostsim.hs_check_owner(r, (ctypes.c_int64 * r)(*dims), (ctypes.c_int * r)(*perm), elem, 1, 0.01, 0,
+                                     300000, ctypes.byref(visited))
+    finally:
+        hostsim.hs_tune(b"factor", 1)
     assert bad == 0
     assert visited.value >= 1
 
