@@ -41,6 +41,10 @@ namespace eithot {
 namespace {
 
 constexpr int kThreads = 512;
+// Word loads a thread issues before placing their bytes (loops that stage
+// narrow units from aligned words): one load in flight per thread leaves
+// 2 KB in flight per CTA, far from what HBM needs.
+constexpr int kWordDepth = 4;
 
 // Set when an index map returns a position outside its row or column; the
 // access is skipped instead of faulting.  Read (and cleared) by
@@ -148,19 +152,34 @@ struct SlabArgs {
 // (the words there hold other pieces' bytes).
 __device__ __forceinline__ void slab_pieces_words(const SlabArgs& a, uint8_t* smem, uint8_t* mat, uint32_t L) {
     const uint32_t total = a.R * a.C * a.slots;
-    for (uint32_t x = threadIdx.x; x < total; x += blockDim.x) {
-        uint32_t p, k, r, c;
-        a.div_slots.divmod(x, p, k);
-        const uintptr_t lo = reinterpret_cast<uintptr_t>(mat + static_cast<uint64_t>(p) * a.E);
-        const uint32_t h = static_cast<uint32_t>(lo & 3u);
-        if (4 * k >= h + L) continue;
-        const uint32_t v = *reinterpret_cast<const uint32_t*>(lo - h + 4 * k);
-        a.div_C.divmod(p, r, c);
-        uint8_t* dst = smem + r * a.pitch + c * a.w;
+    for (uint32_t x0 = threadIdx.x; x0 < total; x0 += kWordDepth * blockDim.x) {
+        uint32_t v[kWordDepth], p[kWordDepth], b[kWordDepth];
+        bool ok[kWordDepth];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const uint32_t b = 4 * k + j - h;  // wraps below 0 for the bytes before the piece
-            if (b < L) dst[b] = static_cast<uint8_t>(v >> (8 * j));
+        for (int d = 0; d < kWordDepth; ++d) {
+            const uint32_t x = x0 + d * blockDim.x;
+            ok[d] = false;
+            if (x >= total) continue;
+            uint32_t k;
+            a.div_slots.divmod(x, p[d], k);
+            const uintptr_t lo = reinterpret_cast<uintptr_t>(mat + static_cast<uint64_t>(p[d]) * a.E);
+            const uint32_t h = static_cast<uint32_t>(lo & 3u);
+            if (4 * k >= h + L) continue;
+            v[d] = *reinterpret_cast<const uint32_t*>(lo - h + 4 * k);
+            b[d] = 4 * k - h;  // piece byte of the word's first byte (wraps below 0)
+            ok[d] = true;
+        }
+#pragma unroll
+        for (int d = 0; d < kWordDepth; ++d) {
+            if (!ok[d]) continue;
+            uint32_t r, c;
+            a.div_C.divmod(p[d], r, c);
+            uint8_t* dst = smem + r * a.pitch + c * a.w;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const uint32_t bj = b[d] + j;
+                if (bj < L) dst[bj] = static_cast<uint8_t>(v[d] >> (8 * j));
+            }
         }
     }
     __syncthreads();
@@ -307,16 +326,26 @@ __global__ void __launch_bounds__(kThreads) k_slab_cluster(SlabClusterArgs a) {
             const uint32_t head = static_cast<uint32_t>(lo & 3u);
             const uint32_t* wp = reinterpret_cast<const uint32_t*>(lo - head);
             const uint32_t words = (head + nbytes + 3) / 4;
-            for (uint32_t x = threadIdx.x; x < words; x += blockDim.x) {
-                const uint32_t v = wp[x];
-                const uint32_t b0 = x * 4;  // band offset of the word's first byte is b0 - head
+            for (uint32_t x0 = threadIdx.x; x0 < words; x0 += kWordDepth * blockDim.x) {
+                uint32_t v[kWordDepth];
 #pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    const uint32_t ob = b0 + k;
-                    if (ob < head || ob - head >= nbytes) continue;
-                    uint32_t rr, cb;
-                    a.div_rowb.divmod(ob - head, rr, cb);
-                    smem[rr * a.pitch + cb] = static_cast<uint8_t>(v >> (8 * k));
+                for (int j = 0; j < kWordDepth; ++j) {
+                    const uint32_t x = x0 + j * blockDim.x;
+                    v[j] = x < words ? wp[x] : 0u;
+                }
+#pragma unroll
+                for (int j = 0; j < kWordDepth; ++j) {
+                    const uint32_t x = x0 + j * blockDim.x;
+                    if (x >= words) break;
+                    const uint32_t b0 = x * 4;  // band offset of the word's first byte is b0 - head
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const uint32_t ob = b0 + k;
+                        if (ob < head || ob - head >= nbytes) continue;
+                        uint32_t rr, cb;
+                        a.div_rowb.divmod(ob - head, rr, cb);
+                        smem[rr * a.pitch + cb] = static_cast<uint8_t>(v[j] >> (8 * k));
+                    }
                 }
             }
         } else {
@@ -371,12 +400,22 @@ __device__ __forceinline__ void words_copy_in(uint8_t* sm, const uint8_t* g, uin
     const uint32_t head = static_cast<uint32_t>(lo & 3u);
     const uint32_t* wp = reinterpret_cast<const uint32_t*>(lo - head);
     const uint32_t words = (head + bytes + 3) / 4;
-    for (uint32_t x = threadIdx.x; x < words; x += blockDim.x) {
-        const uint32_t v = wp[x];
+    for (uint32_t x0 = threadIdx.x; x0 < words; x0 += kWordDepth * blockDim.x) {
+        uint32_t v[kWordDepth];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const uint32_t ob = x * 4 + k;
-            if (ob >= head && ob - head < bytes) sm[ob - head] = static_cast<uint8_t>(v >> (8 * k));
+        for (int j = 0; j < kWordDepth; ++j) {
+            const uint32_t x = x0 + j * blockDim.x;
+            v[j] = x < words ? wp[x] : 0u;
+        }
+#pragma unroll
+        for (int j = 0; j < kWordDepth; ++j) {
+            const uint32_t x = x0 + j * blockDim.x;
+            if (x >= words) break;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const uint32_t ob = x * 4 + k;
+                if (ob >= head && ob - head < bytes) sm[ob - head] = static_cast<uint8_t>(v[j] >> (8 * k));
+            }
         }
     }
 }
@@ -941,21 +980,34 @@ __device__ __forceinline__ void own_stage_in_tab(const ColOwnArgs& a, const I* s
         if (a.stage_words) {
             const uint32_t pb = ci.tcols * static_cast<uint32_t>(a.E);  // bytes of a row piece
             const uint32_t total = nstage * a.wpp;
-            for (uint32_t x = threadIdx.x; x < total; x += blockDim.x) {
-                uint32_t ii, q;
-                a.div_wpp.divmod(x, ii, q);
-                const I gr = srow[ii];
-                if (!in_range(gr, a.rows, a.status)) continue;
-                const uintptr_t lo = reinterpret_cast<uintptr_t>(ci.mat + static_cast<uint64_t>(gr) * a.row_bytes);
-                const uint32_t head = static_cast<uint32_t>(lo & 3u);
-                const uint32_t b0 = q * 4;  // offset in the aligned span; the piece starts at `head`
-                if (b0 >= head + pb) continue;
-                const uint32_t v = *reinterpret_cast<const uint32_t*>(lo - head + b0);
-                uint8_t* dst = buf + ii * a.pitch;
+            for (uint32_t x0 = threadIdx.x; x0 < total; x0 += kWordDepth * blockDim.x) {
+                uint32_t v[kWordDepth], ii[kWordDepth], b[kWordDepth];
+                bool ok[kWordDepth];
 #pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    const uint32_t ob = b0 + k;
-                    if (ob >= head && ob - head < pb) dst[ob - head] = static_cast<uint8_t>(v >> (8 * k));
+                for (int j = 0; j < kWordDepth; ++j) {
+                    const uint32_t x = x0 + j * blockDim.x;
+                    ok[j] = false;
+                    if (x >= total) continue;
+                    uint32_t q;
+                    a.div_wpp.divmod(x, ii[j], q);
+                    const I gr = srow[ii[j]];
+                    if (!in_range(gr, a.rows, a.status)) continue;
+                    const uintptr_t lo = reinterpret_cast<uintptr_t>(ci.mat + static_cast<uint64_t>(gr) * a.row_bytes);
+                    const uint32_t head = static_cast<uint32_t>(lo & 3u);
+                    if (q * 4 >= head + pb) continue;  // offset in the aligned span; the piece starts at `head`
+                    v[j] = *reinterpret_cast<const uint32_t*>(lo - head + q * 4);
+                    b[j] = q * 4 - head;  // piece byte of the word's first byte (wraps below 0)
+                    ok[j] = true;
+                }
+#pragma unroll
+                for (int j = 0; j < kWordDepth; ++j) {
+                    if (!ok[j]) continue;
+                    uint8_t* dst = buf + ii[j] * a.pitch;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const uint32_t ob = b[j] + k;
+                        if (ob < pb) dst[ob] = static_cast<uint8_t>(v[j] >> (8 * k));
+                    }
                 }
             }
             return;

@@ -173,20 +173,32 @@ template <> struct ElemT<8> { using T = uint2; };
 template <> struct ElemT<16> { using T = uint4; };
 
 __device__ __forceinline__ void stage_words(const SlabRunArgs& a, uint8_t* smem, const uint8_t* slab) {
+    constexpr int kDepth = 4;  // word loads in flight per thread
     const uint32_t words = static_cast<uint32_t>(a.slab_bytes / 4);
-    for (uint32_t x = threadIdx.x; x < words; x += blockDim.x) {
-        const uint32_t v = reinterpret_cast<const uint32_t*>(slab)[x];
-        uint32_t r, c;
-        a.div_rowb.divmod(x * 4, r, c);
-        if ((c & 3) == 0 && c + 4 <= a.row_bytes) {
-            *reinterpret_cast<uint32_t*>(smem + r * a.pitch + c) = v;
-        } else {
+    for (uint32_t x0 = threadIdx.x; x0 < words; x0 += kDepth * blockDim.x) {
+        uint32_t w[kDepth];
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                smem[r * a.pitch + c] = static_cast<uint8_t>(v >> (8 * k));
-                if (++c == a.row_bytes) {
-                    c = 0;
-                    ++r;
+        for (int j = 0; j < kDepth; ++j) {
+            const uint32_t x = x0 + j * blockDim.x;
+            w[j] = x < words ? reinterpret_cast<const uint32_t*>(slab)[x] : 0u;
+        }
+#pragma unroll
+        for (int j = 0; j < kDepth; ++j) {
+            const uint32_t x = x0 + j * blockDim.x;
+            if (x >= words) break;
+            const uint32_t v = w[j];
+            uint32_t r, c;
+            a.div_rowb.divmod(x * 4, r, c);
+            if ((c & 3) == 0 && c + 4 <= a.row_bytes) {
+                *reinterpret_cast<uint32_t*>(smem + r * a.pitch + c) = v;
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    smem[r * a.pitch + c] = static_cast<uint8_t>(v >> (8 * k));
+                    if (++c == a.row_bytes) {
+                        c = 0;
+                        ++r;
+                    }
                 }
             }
         }
