@@ -46,6 +46,18 @@ constexpr int kThreads = 512;
 // 2 KB in flight per CTA, far from what HBM needs.
 constexpr int kWordDepth = 4;
 
+// Places the bytes of an aligned 16-byte chunk whose first byte is byte b of
+// a range of L bytes (b wraps below 0 for chunk bytes before the range) at
+// dst[b + j], keeping only those inside the range.
+__device__ __forceinline__ void place_chunk(uint8_t* dst, const uint4& v, uint32_t b, uint32_t L) {
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+        const uint32_t bj = b + j;
+        if (bj < L) dst[bj] = static_cast<uint8_t>(w[j >> 2] >> (8 * (j & 3)));
+    }
+}
+
 // Set when an index map returns a position outside its row or column; the
 // access is skipped instead of faulting.  Read (and cleared) by
 // eithot_index_faults().
@@ -137,23 +149,25 @@ struct SlabArgs {
     FastDiv div_strips;
     FastDiv32 div_C, div_R, div_upw, div_rowunits;
     uint32_t nstrips;
-    // pieces (an element's strip: up to w bytes at any alignment) moved in
-    // the aligned 4-byte words around them: `slots` words per piece
+    // pieces (an element's strip: up to w bytes at any alignment) read in the
+    // aligned 16-byte chunks around them (`slots` per piece) and written as
+    // the aligned 4-byte words inside them (`wslots` per piece)
     bool words;
-    uint32_t slots;
-    FastDiv32 div_slots;
+    uint32_t slots, wslots;
+    FastDiv32 div_slots, div_wslots;
 };
 
 // Slab of 1- or 2-byte units in pieces of L bytes (piece p of the input
 // starts p*E bytes after `mat`, staged at (p / C)*pitch + (p % C)*w): every
-// piece read in the aligned words around it (bytes outside it dropped; a
-// word never crosses a page), transposed, and written as the aligned words
+// piece read in the aligned 16-byte chunks around it (bytes outside it
+// dropped; a chunk never crosses a page), transposed, and written as the aligned words
 // inside each output piece, the at most 3 bytes at either end one by one
 // (the words there hold other pieces' bytes).
 __device__ __forceinline__ void slab_pieces_words(const SlabArgs& a, uint8_t* smem, uint8_t* mat, uint32_t L) {
     const uint32_t total = a.R * a.C * a.slots;
     for (uint32_t x0 = threadIdx.x; x0 < total; x0 += kWordDepth * blockDim.x) {
-        uint32_t v[kWordDepth], p[kWordDepth], b[kWordDepth];
+        uint4 v[kWordDepth];
+        uint32_t p[kWordDepth], b[kWordDepth];
         bool ok[kWordDepth];
 #pragma unroll
         for (int d = 0; d < kWordDepth; ++d) {
@@ -163,10 +177,10 @@ __device__ __forceinline__ void slab_pieces_words(const SlabArgs& a, uint8_t* sm
             uint32_t k;
             a.div_slots.divmod(x, p[d], k);
             const uintptr_t lo = reinterpret_cast<uintptr_t>(mat + static_cast<uint64_t>(p[d]) * a.E);
-            const uint32_t h = static_cast<uint32_t>(lo & 3u);
-            if (4 * k >= h + L) continue;
-            v[d] = *reinterpret_cast<const uint32_t*>(lo - h + 4 * k);
-            b[d] = 4 * k - h;  // piece byte of the word's first byte (wraps below 0)
+            const uint32_t h = static_cast<uint32_t>(lo & 15u);
+            if (16 * k >= h + L) continue;
+            v[d] = *reinterpret_cast<const uint4*>(lo - h + 16 * k);
+            b[d] = 16 * k - h;  // piece byte of the chunk's first byte (wraps below 0)
             ok[d] = true;
         }
 #pragma unroll
@@ -174,18 +188,14 @@ __device__ __forceinline__ void slab_pieces_words(const SlabArgs& a, uint8_t* sm
             if (!ok[d]) continue;
             uint32_t r, c;
             a.div_C.divmod(p[d], r, c);
-            uint8_t* dst = smem + r * a.pitch + c * a.w;
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const uint32_t bj = b[d] + j;
-                if (bj < L) dst[bj] = static_cast<uint8_t>(v[d] >> (8 * j));
-            }
+            place_chunk(smem + r * a.pitch + c * a.w, v[d], b[d], L);
         }
     }
     __syncthreads();
-    for (uint32_t x = threadIdx.x; x < total; x += blockDim.x) {
+    const uint32_t wtotal = a.R * a.C * a.wslots;
+    for (uint32_t x = threadIdx.x; x < wtotal; x += blockDim.x) {
         uint32_t o, k, c, r;
-        a.div_slots.divmod(x, o, k);
+        a.div_wslots.divmod(x, o, k);
         a.div_R.divmod(o, c, r);  // output o = c*R + r holds input (r, c)
         const uint8_t* src = smem + r * a.pitch + c * a.w;
         const uintptr_t lo = reinterpret_cast<uintptr_t>(mat + static_cast<uint64_t>(o) * a.E);
@@ -292,9 +302,9 @@ struct SlabClusterArgs {
     uint64_t items, mat_bytes, row_bytes;
     uint32_t R, C, E, Q, pitch, upr, upw, wpr;
     bool load4;  // rows are whole 4-byte words at a 4-byte aligned base: load words
-    // otherwise, narrow units: the band is read in aligned 4-byte words and
-    // its bytes placed into the padded rows (bytes of the words outside the
-    // band are read and dropped: a word never crosses a page)
+    // otherwise, narrow units: the band is read in aligned 16-byte chunks and
+    // its bytes placed into the padded rows (bytes of the chunks outside the
+    // band are read and dropped: a chunk never crosses a page)
     bool stage_words;
     FastDiv32 div_upr, div_upw, div_Qupw, div_Qpack, div_wpr, div_rowb;
 };
@@ -323,28 +333,29 @@ __global__ void __launch_bounds__(kThreads) k_slab_cluster(SlabClusterArgs a) {
         } else if (US < 4 && a.stage_words) {
             const uint32_t nbytes = nr * static_cast<uint32_t>(a.row_bytes);
             const uintptr_t lo = reinterpret_cast<uintptr_t>(band);
-            const uint32_t head = static_cast<uint32_t>(lo & 3u);
-            const uint32_t* wp = reinterpret_cast<const uint32_t*>(lo - head);
-            const uint32_t words = (head + nbytes + 3) / 4;
-            for (uint32_t x0 = threadIdx.x; x0 < words; x0 += kWordDepth * blockDim.x) {
-                uint32_t v[kWordDepth];
+            const uint32_t head = static_cast<uint32_t>(lo & 15u);
+            const uint4* cp = reinterpret_cast<const uint4*>(lo - head);
+            const uint32_t chunks = (head + nbytes + 15) / 16;
+            for (uint32_t x0 = threadIdx.x; x0 < chunks; x0 += kWordDepth * blockDim.x) {
+                uint4 v[kWordDepth];
 #pragma unroll
                 for (int j = 0; j < kWordDepth; ++j) {
                     const uint32_t x = x0 + j * blockDim.x;
-                    v[j] = x < words ? wp[x] : 0u;
+                    if (x < chunks) v[j] = cp[x];
                 }
 #pragma unroll
                 for (int j = 0; j < kWordDepth; ++j) {
                     const uint32_t x = x0 + j * blockDim.x;
-                    if (x >= words) break;
-                    const uint32_t b0 = x * 4;  // band offset of the word's first byte is b0 - head
+                    if (x >= chunks) break;
+                    const uint32_t w[4] = {v[j].x, v[j].y, v[j].z, v[j].w};
+                    const uint32_t b0 = x * 16;  // band offset of the chunk's first byte is b0 - head
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) {
+                    for (int k = 0; k < 16; ++k) {
                         const uint32_t ob = b0 + k;
                         if (ob < head || ob - head >= nbytes) continue;
                         uint32_t rr, cb;
                         a.div_rowb.divmod(ob - head, rr, cb);
-                        smem[rr * a.pitch + cb] = static_cast<uint8_t>(v[j] >> (8 * k));
+                        smem[rr * a.pitch + cb] = static_cast<uint8_t>(w[k >> 2] >> (8 * (k & 3)));
                     }
                 }
             }
@@ -391,31 +402,28 @@ __global__ void __launch_bounds__(kThreads) k_slab_cluster(SlabClusterArgs a) {
 // 16-byte cp.async chunks when both ends and the size allow it (vec16),
 // else US-byte units.  Completes before returning.
 // Copies `bytes` contiguous bytes at any alignment from global memory to
-// shared memory through the aligned 4-byte words around them (bytes of the
-// first and last word outside the range are read and dropped; a word never
-// crosses a page).  For 1- and 2-byte units: one load per 4 bytes instead of
+// shared memory through the aligned 16-byte chunks around them (bytes of the
+// first and last chunk outside the range are read and dropped; a chunk never
+// crosses a page).  For 1- and 2-byte units: one load per 16 bytes instead of
 // one per unit.
 __device__ __forceinline__ void words_copy_in(uint8_t* sm, const uint8_t* g, uint32_t bytes) {
     const uintptr_t lo = reinterpret_cast<uintptr_t>(g);
-    const uint32_t head = static_cast<uint32_t>(lo & 3u);
-    const uint32_t* wp = reinterpret_cast<const uint32_t*>(lo - head);
-    const uint32_t words = (head + bytes + 3) / 4;
-    for (uint32_t x0 = threadIdx.x; x0 < words; x0 += kWordDepth * blockDim.x) {
-        uint32_t v[kWordDepth];
+    const uint32_t head = static_cast<uint32_t>(lo & 15u);
+    const uint4* cp = reinterpret_cast<const uint4*>(lo - head);
+    const uint32_t chunks = (head + bytes + 15) / 16;
+    constexpr int kDepth = 2;  // chunks in flight per thread (register-bound callers)
+    for (uint32_t x0 = threadIdx.x; x0 < chunks; x0 += kDepth * blockDim.x) {
+        uint4 v[kDepth];
 #pragma unroll
-        for (int j = 0; j < kWordDepth; ++j) {
+        for (int j = 0; j < kDepth; ++j) {
             const uint32_t x = x0 + j * blockDim.x;
-            v[j] = x < words ? wp[x] : 0u;
+            if (x < chunks) v[j] = cp[x];
         }
 #pragma unroll
-        for (int j = 0; j < kWordDepth; ++j) {
+        for (int j = 0; j < kDepth; ++j) {
             const uint32_t x = x0 + j * blockDim.x;
-            if (x >= words) break;
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const uint32_t ob = x * 4 + k;
-                if (ob >= head && ob - head < bytes) sm[ob - head] = static_cast<uint8_t>(v[j] >> (8 * k));
-            }
+            if (x >= chunks) break;
+            place_chunk(sm, v[j], x * 16 - head, bytes);
         }
     }
 }
@@ -915,8 +923,8 @@ struct ColOwnArgs {
     bool whole;      // one CTA holds all m slots of a tile: no halo, slots indexed modulo m
     uint32_t dofs;   // whole: a multiple of m above every |delta difference| of a tile
     // narrow whole elements: each slot's row piece is staged from the aligned
-    // 4-byte words around it (wpp words per piece at most; bytes outside the
-    // piece read and dropped, a word never crosses a page)
+    // 16-byte chunks around it (wpp chunks per piece at most; bytes outside
+    // the piece read and dropped, a chunk never crosses a page)
     bool stage_words;
     uint32_t wpp;
     FastDiv div_strips, div_tiles;
@@ -981,7 +989,8 @@ __device__ __forceinline__ void own_stage_in_tab(const ColOwnArgs& a, const I* s
             const uint32_t pb = ci.tcols * static_cast<uint32_t>(a.E);  // bytes of a row piece
             const uint32_t total = nstage * a.wpp;
             for (uint32_t x0 = threadIdx.x; x0 < total; x0 += kWordDepth * blockDim.x) {
-                uint32_t v[kWordDepth], ii[kWordDepth], b[kWordDepth];
+                uint4 v[kWordDepth];
+                uint32_t ii[kWordDepth], b[kWordDepth];
                 bool ok[kWordDepth];
 #pragma unroll
                 for (int j = 0; j < kWordDepth; ++j) {
@@ -993,22 +1002,15 @@ __device__ __forceinline__ void own_stage_in_tab(const ColOwnArgs& a, const I* s
                     const I gr = srow[ii[j]];
                     if (!in_range(gr, a.rows, a.status)) continue;
                     const uintptr_t lo = reinterpret_cast<uintptr_t>(ci.mat + static_cast<uint64_t>(gr) * a.row_bytes);
-                    const uint32_t head = static_cast<uint32_t>(lo & 3u);
-                    if (q * 4 >= head + pb) continue;  // offset in the aligned span; the piece starts at `head`
-                    v[j] = *reinterpret_cast<const uint32_t*>(lo - head + q * 4);
-                    b[j] = q * 4 - head;  // piece byte of the word's first byte (wraps below 0)
+                    const uint32_t head = static_cast<uint32_t>(lo & 15u);
+                    if (q * 16 >= head + pb) continue;  // offset in the aligned span; the piece starts at `head`
+                    v[j] = *reinterpret_cast<const uint4*>(lo - head + q * 16);
+                    b[j] = q * 16 - head;  // piece byte of the chunk's first byte (wraps below 0)
                     ok[j] = true;
                 }
 #pragma unroll
-                for (int j = 0; j < kWordDepth; ++j) {
-                    if (!ok[j]) continue;
-                    uint8_t* dst = buf + ii[j] * a.pitch;
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        const uint32_t ob = b[j] + k;
-                        if (ob < pb) dst[ob] = static_cast<uint8_t>(v[j] >> (8 * k));
-                    }
-                }
+                for (int j = 0; j < kWordDepth; ++j)
+                    if (ok[j]) place_chunk(buf + ii[j] * a.pitch, v[j], b[j], pb);
             }
             return;
         }
@@ -1763,8 +1765,10 @@ int launch_slab(uint8_t* data, const Pass& p, ExecContext& ctx) {
     // pieces of 16 bytes or more in words (shorter ones gain nothing: their
     // words are mostly partial)
     a.words = US < 4 && !pack && std::min<uint64_t>(p.strip, p.elem) >= 16 && tuning().narrow_words;
-    a.slots = (a.w + 3) / 4 + 1;
+    a.slots = (a.w + 15) / 16 + 1;
     a.div_slots = FastDiv32::make(a.slots);
+    a.wslots = (a.w + 3) / 4 + 1;
+    a.div_wslots = FastDiv32::make(a.wslots);
     const void* k = pack ? reinterpret_cast<const void*>(&k_slab<US, kPack>)
                          : reinterpret_cast<const void*>(&k_slab<US, 1>);
     EI_CHECK(prep_smem(k, smem));
@@ -2053,7 +2057,7 @@ ColOwnArgs col_owner_args(uint8_t* data, const Pass& p, const Staging& st, int U
     a.buf_bytes = static_cast<uint32_t>((slots * st.pitch + 127) / 128 * 128);
     a.dbuf = st.dbuf;
     a.stage_words = US < 4 && a.nstrips == 1 && a.w == a.E && tuning().narrow_words;
-    a.wpp = static_cast<uint32_t>((a.tw * a.E + 3) / 4 + 1);
+    a.wpp = static_cast<uint32_t>((a.tw * a.E + 15) / 16 + 1);
     a.div_wpp = FastDiv32::make(a.wpp);
     return a;
 }
