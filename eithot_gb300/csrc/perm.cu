@@ -57,6 +57,11 @@ struct SlabPermArgs {
     uint32_t count, E, w, upw, last_upw, nstrips, q;
     FastDiv div_strips;
     FastDiv32 div_upw;
+    // 1- and 2-byte units: every element's piece (its strip, up to w bytes)
+    // read in the aligned 16-byte chunks around it (`slots` per piece) and
+    // written as the aligned 4-byte words inside it (`wslots` per piece)
+    uint32_t words, slots, wslots;
+    FastDiv32 div_slots, div_wslots;
     FastDiv32 od[kMaxAxes];   // output dims, output order
     uint32_t istr[kMaxAxes];  // input stride (elements) of output axis j
 };
@@ -74,6 +79,71 @@ __device__ __forceinline__ uint32_t slab_src(const SlabPermArgs& a, uint32_t o) 
     return idx;
 }
 
+// Places the bytes of an aligned 16-byte chunk whose first byte is byte b of
+// a range of L bytes (b wraps below 0 for chunk bytes before the range) at
+// dst[b + j], keeping only those inside the range.
+__device__ __forceinline__ void place_chunk16(uint8_t* dst, const uint4& v, uint32_t b, uint32_t L) {
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+        const uint32_t bj = b + j;
+        if (bj < L) dst[bj] = static_cast<uint8_t>(w[j >> 2] >> (8 * (j & 3)));
+    }
+}
+
+// The word path of k_slab_perm (pieces of L bytes at any alignment; chunks
+// and words never cross a page; bytes outside a piece are read and dropped,
+// never written).
+__device__ __forceinline__ void slab_perm_words(const SlabPermArgs& a, uint8_t* smem, uint8_t* slab, uint32_t L) {
+    constexpr int kDepth = 4;  // chunk loads in flight per thread
+    const uint32_t total = a.count * a.slots;
+    for (uint32_t x0 = threadIdx.x; x0 < total; x0 += kDepth * blockDim.x) {
+        uint4 v[kDepth];
+        uint32_t e[kDepth], b[kDepth];
+        bool ok[kDepth];
+#pragma unroll
+        for (int d = 0; d < kDepth; ++d) {
+            const uint32_t x = x0 + d * blockDim.x;
+            ok[d] = false;
+            if (x >= total) continue;
+            uint32_t k;
+            a.div_slots.divmod(x, e[d], k);
+            const uintptr_t lo = reinterpret_cast<uintptr_t>(slab + static_cast<uint64_t>(e[d]) * a.E);
+            const uint32_t h = static_cast<uint32_t>(lo & 15u);
+            if (16 * k >= h + L) continue;
+            v[d] = *reinterpret_cast<const uint4*>(lo - h + 16 * k);
+            b[d] = 16 * k - h;
+            ok[d] = true;
+        }
+#pragma unroll
+        for (int d = 0; d < kDepth; ++d)
+            if (ok[d]) place_chunk16(smem + e[d] * a.w, v[d], b[d], L);
+    }
+    __syncthreads();
+    const uint32_t wtotal = a.count * a.wslots;
+    for (uint32_t x = threadIdx.x; x < wtotal; x += blockDim.x) {
+        uint32_t o, k;
+        a.div_wslots.divmod(x, o, k);
+        const uintptr_t lo = reinterpret_cast<uintptr_t>(slab + static_cast<uint64_t>(o) * a.E);
+        const uint32_t h = static_cast<uint32_t>(lo & 3u);
+        if (4 * k >= h + L) continue;
+        const uint8_t* src = smem + slab_src(a, o) * a.w;
+        const uint32_t b0 = 4 * k - h;
+        if (4 * k >= h && b0 + 4 <= L) {
+            const uint32_t v = static_cast<uint32_t>(src[b0]) | static_cast<uint32_t>(src[b0 + 1]) << 8 |
+                               static_cast<uint32_t>(src[b0 + 2]) << 16 | static_cast<uint32_t>(src[b0 + 3]) << 24;
+            *reinterpret_cast<uint32_t*>(lo - h + 4 * k) = v;
+        } else {
+            uint8_t* dst = reinterpret_cast<uint8_t*>(lo - h + 4 * k);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const uint32_t bj = b0 + j;
+                if (bj < L) dst[j] = src[bj];
+            }
+        }
+    }
+}
+
 template <int US, int kPack>
 __global__ void __launch_bounds__(512) k_slab_perm(SlabPermArgs a) {
     using U = typename UnitT<US>::T;
@@ -83,6 +153,13 @@ __global__ void __launch_bounds__(512) k_slab_perm(SlabPermArgs a) {
         a.div_strips.divmod(it, b, s);
         const uint32_t lim = (s + 1 == a.nstrips) ? a.last_upw : a.upw;
         uint8_t* slab = a.base + b * a.slab_bytes + s * a.w;
+        if constexpr (US < 4 && kPack == 1) {
+            if (a.words) {
+                slab_perm_words(a, smem, slab, lim * US);
+                __syncthreads();
+                continue;
+            }
+        }
         const uint32_t units = a.count * a.upw;
         if (a.w == a.E) {  // whole elements: the slab is contiguous
             for (uint32_t x = threadIdx.x; x < units; x += blockDim.x)
@@ -1134,6 +1211,12 @@ int run_slab_perm(uint8_t* data, const Pass& p, ExecContext& ctx) {
     a.last_upw = static_cast<uint32_t>(last / US);
     a.div_upw = FastDiv32::make(a.upw);
     const bool whole = a.nstrips == 1;
+    // pieces of 8 bytes or more in chunks and words (shorter ones gain little)
+    a.words = US < 4 && w >= 8 && tuning().narrow_words;
+    a.slots = static_cast<uint32_t>((w + 15) / 16 + 1);
+    a.div_slots = FastDiv32::make(a.slots);
+    a.wslots = static_cast<uint32_t>((w + 3) / 4 + 1);
+    a.div_wslots = FastDiv32::make(a.wslots);
     switch (US) {
         case 16: return launch_slab_perm<16, 1>(a, smem, ctx);
         case 8: return launch_slab_perm<8, 1>(a, smem, ctx);

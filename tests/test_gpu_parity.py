@@ -332,6 +332,22 @@ def test_slabs_of_odd_wide_elements(E, tuned, words, offset):
 
 
 @pytest.mark.parametrize("words", [1, 0])
+@pytest.mark.parametrize("offset", [0, 1, 2, 3])
+def test_slab_permutations_of_odd_elements(E, tuned, words, offset):
+    """Slab permutations (fewest-pass plans) of elements of 9-351 bytes whose
+    size is odd or 2 mod 4: pieces read in aligned 16-byte chunks and written
+    as the aligned words inside them (knob narrow_words=1) or unit by unit
+    (0); whole elements and strips, one to three slabs, bases off word
+    boundaries."""
+    tuned(narrow_words=words)
+    for dims, perm, elem in [([9, 33, 3, 3, 21, 4], [1, 4, 6, 3, 5, 2], 1), ([35, 8, 10, 47, 3], [1, 4, 3, 2, 5], 1),
+                             ([307, 3, 116, 2], [1, 4, 3, 2], 1), ([351, 14, 26, 2, 2], [1, 5, 3, 2, 4], 1),
+                             ([11, 19, 13, 4, 5, 3], [1, 6, 4, 2, 5, 3], 1), ([65, 18, 6, 3, 8], [1, 3, 2, 5, 4], 1),
+                             ([5, 7, 9, 11, 13], [1, 5, 4, 3, 2], 3), ([9, 33, 3, 3, 21, 4], [1, 4, 6, 3, 5, 2], 2)]:
+        run_case(E, dims, perm, elem, order=3, offset=offset)
+
+
+@pytest.mark.parametrize("words", [1, 0])
 @pytest.mark.parametrize("factor", [0, 1])
 def test_narrow_units_staged_from_words(E, tuned, words, factor):
     """1- and 2-byte elements whose rows are not whole 4-byte words, through
