@@ -155,7 +155,64 @@ struct SlabArgs {
     bool words;
     uint32_t slots, wslots;
     FastDiv32 div_slots, div_wslots;
+    // whole narrow elements (sizes not a multiple of 4, up to 16 bytes) at
+    // any alignment: the contiguous matrix read in aligned 16-byte chunks,
+    // the output written as aligned 4-byte words gathered byte by byte
+    bool flat_words;
+    FastDiv32 div_E, div_rowb;
 };
+
+// The flat word path of k_slab: matrix bytes [0, n) at `mat` (rows of C*E
+// bytes staged at `pitch`); output byte b holds byte b % E of input element
+// (r, c), (c, r) = divmod(b / E, R).
+__device__ __forceinline__ void slab_flat_words(const SlabArgs& a, uint8_t* smem, uint8_t* mat) {
+    const uint32_t n = static_cast<uint32_t>(a.mat_bytes);
+    const uintptr_t lo = reinterpret_cast<uintptr_t>(mat);
+    const uint32_t head = static_cast<uint32_t>(lo & 15u);
+    const uint4* cp = reinterpret_cast<const uint4*>(lo - head);
+    const uint32_t chunks = (head + n + 15) / 16;
+    for (uint32_t x0 = threadIdx.x; x0 < chunks; x0 += kWordDepth * blockDim.x) {
+        uint4 v[kWordDepth];
+#pragma unroll
+        for (int j = 0; j < kWordDepth; ++j) {
+            const uint32_t x = x0 + j * blockDim.x;
+            if (x < chunks) v[j] = cp[x];
+        }
+#pragma unroll
+        for (int j = 0; j < kWordDepth; ++j) {
+            const uint32_t x = x0 + j * blockDim.x;
+            if (x >= chunks) break;
+            const uint32_t w[4] = {v[j].x, v[j].y, v[j].z, v[j].w};
+#pragma unroll
+            for (int k = 0; k < 16; ++k) {
+                const uint32_t ob = x * 16 + k - head;  // wraps below 0 before the matrix
+                if (ob >= n) continue;
+                uint32_t r, cb;
+                a.div_rowb.divmod(ob, r, cb);
+                smem[r * a.pitch + cb] = static_cast<uint8_t>(w[k >> 2] >> (8 * (k & 3)));
+            }
+        }
+    }
+    __syncthreads();
+    auto byte_of = [&](uint32_t b) -> uint32_t {
+        uint32_t o, e, c, r;
+        a.div_E.divmod(b, o, e);
+        a.div_R.divmod(o, c, r);
+        return smem[r * a.pitch + c * a.E + e];
+    };
+    const uint32_t hw = min(n, static_cast<uint32_t>((4 - (lo & 3u)) & 3u));
+    const uint32_t words = (n - hw) / 4;
+    for (uint32_t x = threadIdx.x; x < words; x += blockDim.x) {
+        const uint32_t b = hw + 4 * x;
+        const uint32_t v = byte_of(b) | byte_of(b + 1) << 8 | byte_of(b + 2) << 16 | byte_of(b + 3) << 24;
+        *reinterpret_cast<uint32_t*>(mat + b) = v;
+    }
+    const uint32_t rest = n - words * 4;  // bytes outside whole words: hw before, the tail after
+    for (uint32_t x = threadIdx.x; x < rest; x += blockDim.x) {
+        const uint32_t b = x < hw ? x : hw + words * 4 + (x - hw);
+        mat[b] = static_cast<uint8_t>(byte_of(b));
+    }
+}
 
 // Slab of 1- or 2-byte units in pieces of L bytes (piece p of the input
 // starts p*E bytes after `mat`, staged at (p / C)*pitch + (p % C)*w): every
@@ -230,6 +287,11 @@ __global__ void __launch_bounds__(kThreads) k_slab(SlabArgs a) {
         if constexpr (US < 4 && kPack == 1) {
             if (a.words) {
                 slab_pieces_words(a, smem, mat, lim * US);
+                __syncthreads();
+                continue;
+            }
+            if (a.flat_words) {
+                slab_flat_words(a, smem, mat);
                 __syncthreads();
                 continue;
             }
@@ -1762,9 +1824,12 @@ int launch_slab(uint8_t* data, const Pass& p, ExecContext& ctx) {
     constexpr int kPack = US < 4 ? 4 / US : 1;
     const bool pack = kPack > 1 && a.flat && p.elem == US && a.nstrips == 1 &&
                       reinterpret_cast<uintptr_t>(a.base) % 4 == 0 && a.mat_bytes % 4 == 0;
-    // pieces of 16 bytes or more in words (shorter ones gain nothing: their
-    // words are mostly partial)
+    // pieces of 16 bytes or more in chunks and words; whole shorter elements
+    // through the flat word path
     a.words = US < 4 && !pack && std::min<uint64_t>(p.strip, p.elem) >= 16 && tuning().narrow_words;
+    a.flat_words = US < 4 && !pack && !a.words && a.flat && tuning().narrow_words;
+    a.div_E = FastDiv32::make(p.elem);
+    a.div_rowb = FastDiv32::make(p.cols * p.elem);
     a.slots = (a.w + 15) / 16 + 1;
     a.div_slots = FastDiv32::make(a.slots);
     a.wslots = (a.w + 3) / 4 + 1;

@@ -333,6 +333,20 @@ def test_slabs_of_odd_wide_elements(E, tuned, words, offset):
 
 @pytest.mark.parametrize("words", [1, 0])
 @pytest.mark.parametrize("offset", [0, 1, 2, 3])
+def test_flat_narrow_slabs(E, tuned, words, offset):
+    """One-CTA slabs of whole 1-, 3- and 2-mod-4-byte elements at any
+    alignment (odd matrix sizes in a batch: no packed stores): the matrix read
+    in aligned 16-byte chunks, the output written as aligned words gathered
+    byte by byte (knob narrow_words=1), or unit by unit (0)."""
+    tuned(narrow_words=words)
+    for dims, perm, elem in [([31535, 3, 20], [2, 1, 3], 1), ([10023, 7, 30], [2, 1, 3], 1), ([341, 67, 50], [2, 1, 3], 1),
+                             ([3, 5001, 7, 4], [1, 3, 2, 4], 1), ([3, 301, 77, 5], [1, 3, 2, 4], 1),
+                             ([3, 1001, 9, 2], [1, 3, 2, 4], 2)]:
+        run_case(E, dims, perm, elem, offset=offset)
+
+
+@pytest.mark.parametrize("words", [1, 0])
+@pytest.mark.parametrize("offset", [0, 1, 2, 3])
 def test_slab_permutations_of_odd_elements(E, tuned, words, offset):
     """Slab permutations (fewest-pass plans) of elements of 9-351 bytes whose
     size is odd or 2 mod 4: pieces read in aligned 16-byte chunks and written
