@@ -170,7 +170,7 @@ __device__ __forceinline__ void slab_flat_words(const SlabArgs& a, uint8_t* smem
     const uintptr_t lo = reinterpret_cast<uintptr_t>(mat);
     const uint32_t head = static_cast<uint32_t>(lo & 15u);
     const uint4* cp = reinterpret_cast<const uint4*>(lo - head);
-    const uint32_t chunks = (head + n + 15) / 16;
+    const uint32_t chunks = n ? (head + n + 15) / 16 : 0;
     for (uint32_t x0 = threadIdx.x; x0 < chunks; x0 += kWordDepth * blockDim.x) {
         uint4 v[kWordDepth];
 #pragma unroll
@@ -369,6 +369,11 @@ struct SlabClusterArgs {
     // band are read and dropped: a chunk never crosses a page)
     bool stage_words;
     FastDiv32 div_upr, div_upw, div_Qupw, div_Qpack, div_wpr, div_rowb;
+    // wide elements of 1- or 2-byte units: each output row's segment (the
+    // band's nr elements, contiguous) written by one warp as the aligned
+    // 4-byte words inside it, gathered byte by byte
+    bool write_words;
+    FastDiv32 div_E;
 };
 
 template <int US, int kPack>
@@ -397,7 +402,10 @@ __global__ void __launch_bounds__(kThreads) k_slab_cluster(SlabClusterArgs a) {
             const uintptr_t lo = reinterpret_cast<uintptr_t>(band);
             const uint32_t head = static_cast<uint32_t>(lo & 15u);
             const uint4* cp = reinterpret_cast<const uint4*>(lo - head);
-            const uint32_t chunks = (head + nbytes + 15) / 16;
+            // a CTA past the last row (K Q > R) has no band: its band pointer
+            // lies beyond the matrix, possibly beyond the allocation, and
+            // must not be read
+            const uint32_t chunks = nbytes ? (head + nbytes + 15) / 16 : 0;
             for (uint32_t x0 = threadIdx.x; x0 < chunks; x0 += kWordDepth * blockDim.x) {
                 uint4 v[kWordDepth];
 #pragma unroll
@@ -445,6 +453,30 @@ __global__ void __launch_bounds__(kThreads) k_slab_cluster(SlabClusterArgs a) {
                             << (8 * US * k);
                 *reinterpret_cast<uint32_t*>(mat + (static_cast<uint64_t>(c) * a.R + r0 + rr) * US) = word;
             }
+        } else if (US < 4 && a.write_words) {
+            const uint32_t segb = nr * a.E;
+            const uint32_t lane = threadIdx.x & 31u, nw = blockDim.x / 32;
+            for (uint32_t c = threadIdx.x / 32; c < a.C && segb; c += nw) {
+                uint8_t* dst = mat + (static_cast<uint64_t>(c) * a.R + r0) * a.E;
+                const uint8_t* col = smem + c * a.E;
+                auto byte_of = [&](uint32_t s) -> uint32_t {
+                    uint32_t rr, e;
+                    a.div_E.divmod(s, rr, e);
+                    return col[rr * a.pitch + e];
+                };
+                const uint32_t hw = min(segb, static_cast<uint32_t>((4 - (reinterpret_cast<uintptr_t>(dst) & 3u)) & 3u));
+                const uint32_t words = (segb - hw) / 4;
+                for (uint32_t k = lane; k < words; k += 32) {
+                    const uint32_t s = hw + 4 * k;
+                    *reinterpret_cast<uint32_t*>(dst + s) =
+                        byte_of(s) | byte_of(s + 1) << 8 | byte_of(s + 2) << 16 | byte_of(s + 3) << 24;
+                }
+                const uint32_t rest = segb - words * 4;  // hw bytes before the words, the tail after
+                for (uint32_t x = lane; x < rest; x += 32) {
+                    const uint32_t s = x < hw ? x : hw + words * 4 + (x - hw);
+                    dst[s] = static_cast<uint8_t>(byte_of(s));
+                }
+            }
         } else {
             const uint32_t out_units = a.C * a.Q * a.upw;
             for (uint32_t x = threadIdx.x; x < out_units; x += blockDim.x) {
@@ -472,7 +504,7 @@ __device__ __forceinline__ void words_copy_in(uint8_t* sm, const uint8_t* g, uin
     const uintptr_t lo = reinterpret_cast<uintptr_t>(g);
     const uint32_t head = static_cast<uint32_t>(lo & 15u);
     const uint4* cp = reinterpret_cast<const uint4*>(lo - head);
-    const uint32_t chunks = (head + bytes + 15) / 16;
+    const uint32_t chunks = bytes ? (head + bytes + 15) / 16 : 0;  // nothing read for an empty range
     constexpr int kDepth = 2;  // chunks in flight per thread (register-bound callers)
     for (uint32_t x0 = threadIdx.x; x0 < chunks; x0 += kDepth * blockDim.x) {
         uint4 v[kDepth];
@@ -1878,6 +1910,8 @@ int launch_slab_cluster(uint8_t* data, const Pass& p, ExecContext& ctx) {
     a.div_upw = FastDiv32::make(a.upw);
     a.load4 = US < 4 && a.row_bytes % 4 == 0 && addr % 4 == 0;
     a.stage_words = US < 4 && !a.load4 && tuning().narrow_words;
+    a.write_words = US < 4 && p.elem >= 16 && tuning().narrow_words;
+    a.div_E = FastDiv32::make(p.elem);
     a.div_rowb = FastDiv32::make(a.row_bytes);
     a.wpr = static_cast<uint32_t>(a.row_bytes / 4);
     a.div_wpr = FastDiv32::make(a.wpr ? a.wpr : 1);

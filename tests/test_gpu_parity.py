@@ -333,6 +333,19 @@ def test_slabs_of_odd_wide_elements(E, tuned, words, offset):
 
 @pytest.mark.parametrize("words", [1, 0])
 @pytest.mark.parametrize("offset", [0, 1, 2, 3])
+def test_cluster_slabs_of_wide_odd_elements(E, tuned, words, offset):
+    """Cluster slabs of 17-1001-byte elements whose size is odd or 2 mod 4:
+    each output row's segment written by one warp as the aligned words inside
+    it, gathered byte by byte (knob narrow_words=1), or unit by unit (0)."""
+    tuned(narrow_words=words)
+    for dims, perm, elem in [([707, 61, 51, 3], [1, 3, 2, 4], 1), ([17, 7, 5572, 3], [1, 3, 2, 4], 1),
+                             ([19, 3, 8769, 2], [1, 3, 2, 4], 1), ([1001, 40, 30], [1, 3, 2], 1),
+                             ([35, 60, 70], [1, 3, 2], 1), ([9, 100, 90], [1, 3, 2], 2)]:
+        run_case(E, dims, perm, elem, offset=offset)
+
+
+@pytest.mark.parametrize("words", [1, 0])
+@pytest.mark.parametrize("offset", [0, 1, 2, 3])
 def test_flat_narrow_slabs(E, tuned, words, offset):
     """One-CTA slabs of whole 1-, 3- and 2-mod-4-byte elements at any
     alignment (odd matrix sizes in a batch: no packed stores): the matrix read
