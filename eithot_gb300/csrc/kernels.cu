@@ -35,6 +35,7 @@
 #include "fn_build.h"
 #include "index_math.cuh"
 #include "passes.h"
+#include "span.cuh"
 
 namespace eithot {
 
@@ -149,9 +150,9 @@ struct SlabArgs {
     FastDiv div_strips;
     FastDiv32 div_C, div_R, div_upw, div_rowunits;
     uint32_t nstrips;
-    // pieces (an element's strip: up to w bytes at any alignment) read in the
-    // aligned 16-byte chunks around them (`slots` per piece) and written as
-    // the aligned 4-byte words inside them (`wslots` per piece)
+    // pieces (an element's strip: up to w bytes at any alignment) staged 16
+    // bytes per thread from the aligned words they span (`slots` per piece)
+    // and written as the aligned 4-byte words inside them (`wslots` per piece)
     bool words;
     uint32_t slots, wslots;
     FastDiv32 div_slots, div_wslots;
@@ -160,38 +161,22 @@ struct SlabArgs {
     // the output written as aligned 4-byte words gathered byte by byte
     bool flat_words;
     FastDiv32 div_E, div_rowb;
+    uint32_t rowchunks;  // 16-byte staging units per row (C*E bytes)
+    FastDiv32 div_rowchunks;
 };
 
 // The flat word path of k_slab: matrix bytes [0, n) at `mat` (rows of C*E
-// bytes staged at `pitch`); output byte b holds byte b % E of input element
-// (r, c), (c, r) = divmod(b / E, R).
+// bytes staged at `pitch` from the aligned words they span); output byte b
+// holds byte b % E of input element (r, c), (c, r) = divmod(b / E, R).
 __device__ __forceinline__ void slab_flat_words(const SlabArgs& a, uint8_t* smem, uint8_t* mat) {
     const uint32_t n = static_cast<uint32_t>(a.mat_bytes);
     const uintptr_t lo = reinterpret_cast<uintptr_t>(mat);
-    const uint32_t head = static_cast<uint32_t>(lo & 15u);
-    const uint4* cp = reinterpret_cast<const uint4*>(lo - head);
-    const uint32_t chunks = n ? (head + n + 15) / 16 : 0;
-    for (uint32_t x0 = threadIdx.x; x0 < chunks; x0 += kWordDepth * blockDim.x) {
-        uint4 v[kWordDepth];
-#pragma unroll
-        for (int j = 0; j < kWordDepth; ++j) {
-            const uint32_t x = x0 + j * blockDim.x;
-            if (x < chunks) v[j] = cp[x];
-        }
-#pragma unroll
-        for (int j = 0; j < kWordDepth; ++j) {
-            const uint32_t x = x0 + j * blockDim.x;
-            if (x >= chunks) break;
-            const uint32_t w[4] = {v[j].x, v[j].y, v[j].z, v[j].w};
-#pragma unroll
-            for (int k = 0; k < 16; ++k) {
-                const uint32_t ob = x * 16 + k - head;  // wraps below 0 before the matrix
-                if (ob >= n) continue;
-                uint32_t r, cb;
-                a.div_rowb.divmod(ob, r, cb);
-                smem[r * a.pitch + cb] = static_cast<uint8_t>(w[k >> 2] >> (8 * (k & 3)));
-            }
-        }
+    const uint32_t rowb = a.C * static_cast<uint32_t>(a.E);
+    const uint32_t total = a.R * a.rowchunks;  // rows staged 16 bytes per thread
+    for (uint32_t x = threadIdx.x; x < total; x += blockDim.x) {
+        uint32_t r, t;
+        a.div_rowchunks.divmod(x, r, t);
+        span_chunk(smem + r * a.pitch, mat + static_cast<uint64_t>(r) * rowb, rowb, t);
     }
     __syncthreads();
     auto byte_of = [&](uint32_t b) -> uint32_t {
@@ -216,37 +201,18 @@ __device__ __forceinline__ void slab_flat_words(const SlabArgs& a, uint8_t* smem
 
 // Slab of 1- or 2-byte units in pieces of L bytes (piece p of the input
 // starts p*E bytes after `mat`, staged at (p / C)*pitch + (p % C)*w): every
-// piece read in the aligned 16-byte chunks around it (bytes outside it
-// dropped; a chunk never crosses a page), transposed, and written as the aligned words
+// piece staged from the aligned words it spans (funnel shifts), transposed,
+// and written as the aligned words
 // inside each output piece, the at most 3 bytes at either end one by one
 // (the words there hold other pieces' bytes).
 __device__ __forceinline__ void slab_pieces_words(const SlabArgs& a, uint8_t* smem, uint8_t* mat, uint32_t L) {
     const uint32_t total = a.R * a.C * a.slots;
-    for (uint32_t x0 = threadIdx.x; x0 < total; x0 += kWordDepth * blockDim.x) {
-        uint4 v[kWordDepth];
-        uint32_t p[kWordDepth], b[kWordDepth];
-        bool ok[kWordDepth];
-#pragma unroll
-        for (int d = 0; d < kWordDepth; ++d) {
-            const uint32_t x = x0 + d * blockDim.x;
-            ok[d] = false;
-            if (x >= total) continue;
-            uint32_t k;
-            a.div_slots.divmod(x, p[d], k);
-            const uintptr_t lo = reinterpret_cast<uintptr_t>(mat + static_cast<uint64_t>(p[d]) * a.E);
-            const uint32_t h = static_cast<uint32_t>(lo & 15u);
-            if (16 * k >= h + L) continue;
-            v[d] = *reinterpret_cast<const uint4*>(lo - h + 16 * k);
-            b[d] = 16 * k - h;  // piece byte of the chunk's first byte (wraps below 0)
-            ok[d] = true;
-        }
-#pragma unroll
-        for (int d = 0; d < kWordDepth; ++d) {
-            if (!ok[d]) continue;
-            uint32_t r, c;
-            a.div_C.divmod(p[d], r, c);
-            place_chunk(smem + r * a.pitch + c * a.w, v[d], b[d], L);
-        }
+    for (uint32_t x = threadIdx.x; x < total; x += blockDim.x) {
+        uint32_t p, t, r, c;
+        a.div_slots.divmod(x, p, t);
+        if (16 * t >= L) continue;
+        a.div_C.divmod(p, r, c);
+        span_chunk(smem + r * a.pitch + c * a.w, mat + static_cast<uint64_t>(p) * a.E, L, t);
     }
     __syncthreads();
     const uint32_t wtotal = a.R * a.C * a.wslots;
@@ -364,10 +330,11 @@ struct SlabClusterArgs {
     uint64_t items, mat_bytes, row_bytes;
     uint32_t R, C, E, Q, pitch, upr, upw, wpr;
     bool load4;  // rows are whole 4-byte words at a 4-byte aligned base: load words
-    // otherwise, narrow units: the band is read in aligned 16-byte chunks and
-    // its bytes placed into the padded rows (bytes of the chunks outside the
-    // band are read and dropped: a chunk never crosses a page)
+    // otherwise, narrow units: each row of the band is staged from the
+    // aligned words it spans (funnel shifts; rowchunks 16-byte units a row)
     bool stage_words;
+    uint32_t rowchunks;
+    FastDiv32 div_rowchunks;
     FastDiv32 div_upr, div_upw, div_Qupw, div_Qpack, div_wpr, div_rowb;
     // wide elements of 1- or 2-byte units: each output row's segment (the
     // band's nr elements, contiguous) written by one warp as the aligned
@@ -398,36 +365,16 @@ __global__ void __launch_bounds__(kThreads) k_slab_cluster(SlabClusterArgs a) {
             }
             copy_in_wait<4>();
         } else if (US < 4 && a.stage_words) {
-            const uint32_t nbytes = nr * static_cast<uint32_t>(a.row_bytes);
-            const uintptr_t lo = reinterpret_cast<uintptr_t>(band);
-            const uint32_t head = static_cast<uint32_t>(lo & 15u);
-            const uint4* cp = reinterpret_cast<const uint4*>(lo - head);
-            // a CTA past the last row (K Q > R) has no band: its band pointer
-            // lies beyond the matrix, possibly beyond the allocation, and
-            // must not be read
-            const uint32_t chunks = nbytes ? (head + nbytes + 15) / 16 : 0;
-            for (uint32_t x0 = threadIdx.x; x0 < chunks; x0 += kWordDepth * blockDim.x) {
-                uint4 v[kWordDepth];
-#pragma unroll
-                for (int j = 0; j < kWordDepth; ++j) {
-                    const uint32_t x = x0 + j * blockDim.x;
-                    if (x < chunks) v[j] = cp[x];
-                }
-#pragma unroll
-                for (int j = 0; j < kWordDepth; ++j) {
-                    const uint32_t x = x0 + j * blockDim.x;
-                    if (x >= chunks) break;
-                    const uint32_t w[4] = {v[j].x, v[j].y, v[j].z, v[j].w};
-                    const uint32_t b0 = x * 16;  // band offset of the chunk's first byte is b0 - head
-#pragma unroll
-                    for (int k = 0; k < 16; ++k) {
-                        const uint32_t ob = b0 + k;
-                        if (ob < head || ob - head >= nbytes) continue;
-                        uint32_t rr, cb;
-                        a.div_rowb.divmod(ob - head, rr, cb);
-                        smem[rr * a.pitch + cb] = static_cast<uint8_t>(w[k >> 2] >> (8 * (k & 3)));
-                    }
-                }
+            // each row staged 16 bytes per thread from the aligned words it
+            // spans; a CTA past the last row (K Q > R) has no band (its band
+            // pointer lies beyond the matrix, possibly beyond the allocation)
+            // and reads nothing
+            const uint32_t rowb = static_cast<uint32_t>(a.row_bytes);
+            const uint32_t total = nr * a.rowchunks;
+            for (uint32_t x = threadIdx.x; x < total; x += blockDim.x) {
+                uint32_t rr, t;
+                a.div_rowchunks.divmod(x, rr, t);
+                span_chunk(smem + rr * a.pitch, band + static_cast<uint64_t>(rr) * rowb, rowb, t);
             }
         } else {
             const uint32_t in_units = nr * a.upr;
@@ -1856,13 +1803,15 @@ int launch_slab(uint8_t* data, const Pass& p, ExecContext& ctx) {
     constexpr int kPack = US < 4 ? 4 / US : 1;
     const bool pack = kPack > 1 && a.flat && p.elem == US && a.nstrips == 1 &&
                       reinterpret_cast<uintptr_t>(a.base) % 4 == 0 && a.mat_bytes % 4 == 0;
-    // pieces of 16 bytes or more in chunks and words; whole shorter elements
-    // through the flat word path
-    a.words = US < 4 && !pack && std::min<uint64_t>(p.strip, p.elem) >= 16 && tuning().narrow_words;
+    // strips of 16 bytes or more (word-aligned slots of w bytes in shared
+    // memory) as pieces; whole elements through the flat word path
+    a.words = US < 4 && !pack && std::min<uint64_t>(p.strip, p.elem) >= 16 && a.w % 4 == 0 && tuning().narrow_words;
     a.flat_words = US < 4 && !pack && !a.words && a.flat && tuning().narrow_words;
     a.div_E = FastDiv32::make(p.elem);
     a.div_rowb = FastDiv32::make(p.cols * p.elem);
-    a.slots = (a.w + 15) / 16 + 1;
+    a.rowchunks = static_cast<uint32_t>((p.cols * p.elem + 15) / 16);
+    a.div_rowchunks = FastDiv32::make(a.rowchunks);
+    a.slots = (a.w + 15) / 16;
     a.div_slots = FastDiv32::make(a.slots);
     a.wslots = (a.w + 3) / 4 + 1;
     a.div_wslots = FastDiv32::make(a.wslots);
@@ -1910,6 +1859,8 @@ int launch_slab_cluster(uint8_t* data, const Pass& p, ExecContext& ctx) {
     a.div_upw = FastDiv32::make(a.upw);
     a.load4 = US < 4 && a.row_bytes % 4 == 0 && addr % 4 == 0;
     a.stage_words = US < 4 && !a.load4 && tuning().narrow_words;
+    a.rowchunks = static_cast<uint32_t>((p.cols * p.elem + 15) / 16);
+    a.div_rowchunks = FastDiv32::make(a.rowchunks);
     a.write_words = US < 4 && p.elem >= 16 && tuning().narrow_words;
     a.div_E = FastDiv32::make(p.elem);
     a.div_rowb = FastDiv32::make(a.row_bytes);

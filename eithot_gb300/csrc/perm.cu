@@ -14,6 +14,7 @@
 #include "index_math.cuh"
 #include "passes.h"
 #include "search.h"
+#include "span.cuh"
 
 namespace eithot {
 
@@ -552,8 +553,8 @@ struct ColBandArgs {
     uint32_t R, C, E, P;
     // su = 4, 8 or 16: every row segment (and its padded row in shared
     // memory) starts on an su-byte boundary and is su-byte units long, staged
-    // by cp.async; su = 0: segments at any alignment, staged from the aligned
-    // 4-byte words around them.  wpr_* = staging units (or words) per row.
+    // by cp.async; su = 0: segments at any alignment, staged 16 bytes per
+    // thread from the aligned words they span.  wpr_* = staging units per row.
     uint32_t su;
     uint32_t wpr_full, wpr_last;
     FastDiv32 div_full, div_last;
@@ -618,37 +619,11 @@ __device__ __forceinline__ void colband_stage(const ColBandArgs& a, uint8_t* sme
         asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
         return;
     }
-    // four word loads in flight per thread before their bytes are placed
-    constexpr int kDepth = 4;
-    for (uint32_t x0 = threadIdx.x; x0 < total; x0 += kDepth * blockDim.x) {
-        uint32_t v[kDepth], r[kDepth], b[kDepth];
-        bool ok[kDepth];
-#pragma unroll
-        for (int j = 0; j < kDepth; ++j) {
-            const uint32_t x = x0 + j * blockDim.x;
-            ok[j] = false;
-            if (x < total) {
-                uint32_t q;
-                dv.divmod(x, r[j], q);
-                const uintptr_t lo = reinterpret_cast<uintptr_t>(seg + static_cast<uint64_t>(r[j]) * a.row_bytes);
-                const uint32_t head = static_cast<uint32_t>(lo & 3u);
-                if (q * 4 < head + wb) {
-                    v[j] = *reinterpret_cast<const uint32_t*>(lo - head + q * 4);
-                    b[j] = q * 4 - head;  // byte of the segment the word starts at (wraps below 0)
-                    ok[j] = true;
-                }
-            }
-        }
-#pragma unroll
-        for (int j = 0; j < kDepth; ++j) {
-            if (!ok[j]) continue;
-            uint8_t* dst = smem + r[j] * pitch;
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const uint32_t ob = b[j] + k;  // wraps below 0 for the head's bytes
-                if (ob < wb) dst[ob] = static_cast<uint8_t>(v[j] >> (8 * k));
-            }
-        }
+    // each row segment 16 bytes per thread from the aligned words it spans
+    for (uint32_t x = threadIdx.x; x < total; x += blockDim.x) {
+        uint32_t r, t;
+        dv.divmod(x, r, t);
+        span_chunk(smem + r * pitch, seg + static_cast<uint64_t>(r) * a.row_bytes, wb, t);
     }
 }
 
@@ -1118,9 +1093,9 @@ int run_slab_colband(uint8_t* data, const Pass& p, ExecContext& ctx) {
     if (a.su) {
         a.wpr_full = a.P * a.E / a.su;
         a.wpr_last = static_cast<uint32_t>(wl * a.E / a.su);
-    } else {
-        a.wpr_full = (a.P * a.E + 3) / 4 + 1;
-        a.wpr_last = static_cast<uint32_t>((wl * a.E + 3) / 4 + 1);
+    } else {  // 16-byte staging units per row segment
+        a.wpr_full = (a.P * a.E + 15) / 16;
+        a.wpr_last = static_cast<uint32_t>((wl * a.E + 15) / 16);
     }
     a.div_full = FastDiv32::make(a.wpr_full);
     a.div_last = FastDiv32::make(a.wpr_last);
