@@ -189,7 +189,21 @@ __device__ __forceinline__ void slab_flat_words(const SlabArgs& a, uint8_t* smem
     const uint32_t words = (n - hw) / 4;
     for (uint32_t x = threadIdx.x; x < words; x += blockDim.x) {
         const uint32_t b = hw + 4 * x;
-        const uint32_t v = byte_of(b) | byte_of(b + 1) << 8 | byte_of(b + 2) << 16 | byte_of(b + 3) << 24;
+        uint32_t o, e, c, r;  // the word's first byte: byte e of output element o = c*R + r
+        a.div_E.divmod(b, o, e);
+        a.div_R.divmod(o, c, r);
+        uint32_t v = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            v |= static_cast<uint32_t>(smem[r * a.pitch + c * a.E + e]) << (8 * k);
+            if (++e == a.E) {  // next output element: next input row, wrapping to the next column
+                e = 0;
+                if (++r == a.R) {
+                    r = 0;
+                    ++c;
+                }
+            }
+        }
         *reinterpret_cast<uint32_t*>(mat + b) = v;
     }
     const uint32_t rest = n - words * 4;  // bytes outside whole words: hw before, the tail after
@@ -415,8 +429,18 @@ __global__ void __launch_bounds__(kThreads) k_slab_cluster(SlabClusterArgs a) {
                 const uint32_t words = (segb - hw) / 4;
                 for (uint32_t k = lane; k < words; k += 32) {
                     const uint32_t s = hw + 4 * k;
-                    *reinterpret_cast<uint32_t*>(dst + s) =
-                        byte_of(s) | byte_of(s + 1) << 8 | byte_of(s + 2) << 16 | byte_of(s + 3) << 24;
+                    uint32_t rr, e;  // byte e of the segment's element rr
+                    a.div_E.divmod(s, rr, e);
+                    uint32_t v = 0;
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        v |= static_cast<uint32_t>(col[rr * a.pitch + e]) << (8 * j);
+                        if (++e == a.E) {
+                            e = 0;
+                            ++rr;
+                        }
+                    }
+                    *reinterpret_cast<uint32_t*>(dst + s) = v;
                 }
                 const uint32_t rest = segb - words * 4;  // hw bytes before the words, the tail after
                 for (uint32_t x = lane; x < rest; x += 32) {

@@ -586,9 +586,21 @@ __device__ __forceinline__ void colband_write_any(const ColBandArgs& a, const ui
     const uint32_t words = (n - head) / 4;
     for (uint32_t x = threadIdx.x; x < words; x += blockDim.x) {
         const uint32_t b = head + 4 * x;
+        uint32_t j, i;  // the word's first byte: output row j, element i (input row i)
+        a.div_R.divmod(b / E, j, i);
+        uint32_t e = b % E;
         uint32_t v = 0;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) v |= colband_byte<E>(a, smem, pitch, b + k) << (8 * k);
+        for (int k = 0; k < 4; ++k) {
+            v |= static_cast<uint32_t>(smem[i * pitch + j * E + e]) << (8 * k);
+            if (++e == E) {
+                e = 0;
+                if (++i == a.R) {
+                    i = 0;
+                    ++j;
+                }
+            }
+        }
         *reinterpret_cast<uint32_t*>(out + b) = v;
     }
     const uint32_t rest = head + (n - head - words * 4);  // bytes outside whole words
