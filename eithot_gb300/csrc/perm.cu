@@ -563,6 +563,11 @@ struct ColBandArgs {
     // gathered byte by byte (div_R: output element -> (output row, element))
     uint32_t any_align;
     FastDiv32 div_R;
+    // tiles: 1-byte elements, R a multiple of 4, ranges word-aligned: 4 x 4
+    // byte tiles transposed in registers (div_rt: tile index -> (column
+    // group, row group), R / 4 row groups)
+    uint32_t tiles;
+    FastDiv32 div_rt;
     SlabRunArgs full, last;       // write-back of a band of P columns / of the last band
 };
 
@@ -639,6 +644,39 @@ __device__ __forceinline__ void colband_stage(const ColBandArgs& a, uint8_t* sme
     }
 }
 
+// Writes a band's w output rows of R 1-byte elements (R a multiple of 4, the
+// range word-aligned) from its staged rows: a thread loads the 4 x 4 byte
+// tile of rows i0..i0+3, columns j0..j0+3 as four words, transposes it with
+// byte permutes and stores four words, one into each of output rows j0..j0+3
+// (row groups fastest across threads); the last w % 4 columns byte by byte.
+__device__ __forceinline__ void colband_write_tiles(const ColBandArgs& a, const uint8_t* smem, uint32_t pitch,
+                                                    uint8_t* out, uint32_t w) {
+    const uint32_t R = a.R, w4 = w & ~3u, tiles = (w4 / 4) * (R / 4);
+    for (uint32_t x = threadIdx.x; x < tiles; x += blockDim.x) {
+        uint32_t jt, it;
+        a.div_rt.divmod(x, jt, it);
+        const uint32_t j0 = jt * 4, i0 = it * 4;
+        const uint8_t* s0 = smem + i0 * pitch + j0;
+        const uint32_t w0 = *reinterpret_cast<const uint32_t*>(s0);
+        const uint32_t w1 = *reinterpret_cast<const uint32_t*>(s0 + pitch);
+        const uint32_t w2 = *reinterpret_cast<const uint32_t*>(s0 + 2 * pitch);
+        const uint32_t w3 = *reinterpret_cast<const uint32_t*>(s0 + 3 * pitch);
+        const uint32_t t0 = __byte_perm(w0, w1, 0x5140), t1 = __byte_perm(w2, w3, 0x5140);
+        const uint32_t t2 = __byte_perm(w0, w1, 0x7362), t3 = __byte_perm(w2, w3, 0x7362);
+        uint8_t* o = out + j0 * R + i0;
+        *reinterpret_cast<uint32_t*>(o) = __byte_perm(t0, t1, 0x5410);
+        *reinterpret_cast<uint32_t*>(o + R) = __byte_perm(t0, t1, 0x7632);
+        *reinterpret_cast<uint32_t*>(o + 2 * R) = __byte_perm(t2, t3, 0x5410);
+        *reinterpret_cast<uint32_t*>(o + 3 * R) = __byte_perm(t2, t3, 0x7632);
+    }
+    const uint32_t rest = (w - w4) * R;
+    for (uint32_t x = threadIdx.x; x < rest; x += blockDim.x) {
+        uint32_t jj, i;
+        a.div_R.divmod(x, jj, i);
+        out[(w4 + jj) * R + i] = smem[i * pitch + w4 + jj];
+    }
+}
+
 template <int E, int V>
 __global__ void __launch_bounds__(512) k_slab_colband(ColBandArgs a) {
     extern __shared__ __align__(16) uint8_t smem[];
@@ -663,6 +701,8 @@ __global__ void __launch_bounds__(512) k_slab_colband(ColBandArgs a) {
             uint8_t* out = mat + static_cast<uint64_t>(c0) * a.R * a.E;
             if (a.any_align)
                 colband_write_any<E>(a, smem, s.pitch, out, w * a.R * a.E);
+            else if (E == 1 && a.tiles)
+                colband_write_tiles(a, smem, s.pitch, out, w);
             else
                 write_runs<E, V>(s, smem, out);
         }
@@ -1098,6 +1138,8 @@ int run_slab_colband(uint8_t* data, const Pass& p, ExecContext& ctx) {
             a.any_align = 1;
     }
     a.div_R = FastDiv32::make(a.R);
+    a.tiles = a.E == 1 && a.R % 4 == 0 && !a.any_align && tuning().narrow_words;
+    a.div_rt = FastDiv32::make(std::max<uint32_t>(1, a.R / 4));
     if (!runs(Vf)) return -1;
     const uint64_t su = pow2_unit({reinterpret_cast<uintptr_t>(a.base), a.row_bytes, static_cast<uint64_t>(a.P) * a.E,
                                    wl * a.E, a.full.pitch, a.last.pitch, a.items > 1 ? a.mat_bytes : 0});

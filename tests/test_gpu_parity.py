@@ -316,6 +316,18 @@ def test_cluster_slabs_in_column_bands(E, tuned, colband, offset):
 
 
 @pytest.mark.parametrize("words", [1, 0])
+@pytest.mark.parametrize("offset", [0, 4, 1])
+def test_column_bands_in_byte_tiles(E, tuned, words, offset):
+    """1-byte column bands with a multiple of 4 rows: 4 x 4 byte tiles
+    transposed in registers (knob narrow_words=1) or runs of stores (0), the
+    last columns of a band byte by byte; one to three matrices, bases on and
+    off word boundaries (off: the any-alignment write)."""
+    tuned(narrow_words=words)
+    for dims in ([50001, 16, 2], [70000, 12, 1], [30003, 8, 3], [41125, 20, 3], [20001, 36, 2]):
+        run_case(E, dims, [2, 1, 3], 1, offset=offset)
+
+
+@pytest.mark.parametrize("words", [1, 0])
 @pytest.mark.parametrize("offset", [0, 1, 2, 3])
 def test_slabs_of_odd_wide_elements(E, tuned, words, offset):
     """One-CTA slabs of wide elements whose size is odd or 2 mod 4 (1- and
