@@ -238,6 +238,10 @@ struct SlabRunArgs {
     uint32_t stage_words;
     FastDiv32 div_rowb;       // slab byte -> (row, byte of the row)
     uint32_t kind;            // 100 * E + V (the queue kernel's dispatch)
+    // 2D transposes of 1-byte elements (slab dims (C, R) written as (R, C)),
+    // R a multiple of 4, slabs word-aligned: written as 4 x 4 byte tiles
+    uint32_t tiles, tile_R, tile_w;
+    FastDiv32 div_rt, div_tR;
     FastDiv32 hod[kMaxAxes];  // output dims m.., output order
     uint32_t hstep[kMaxAxes];
     uint32_t delta[16];
@@ -338,10 +342,51 @@ __device__ __forceinline__ void store_run(uint8_t* dst, const typename ElemT<E>:
 }
 
 // Writes the staged slab back in output order: runs of K outputs per thread.
+// Writes the transpose of a staged w x R block of 1-byte elements (row i of
+// R rows at smem + i * pitch, column j at byte j; R a multiple of 4) as w
+// output rows of R bytes at `out` (word-aligned): a thread loads the 4 x 4
+// byte tile of rows i0..i0+3, columns j0..j0+3 as four words, transposes it
+// with byte permutes and stores one word into each of output rows j0..j0+3
+// (row groups fastest across threads); the last w % 4 columns byte by byte.
+// div_rt divides by R / 4, div_R by R.
+__device__ __forceinline__ void write_byte_tiles(const uint8_t* smem, uint32_t pitch, uint8_t* out, uint32_t w,
+                                                 uint32_t R, const FastDiv32& div_rt, const FastDiv32& div_R) {
+    const uint32_t w4 = w & ~3u, tiles = (w4 / 4) * (R / 4);
+    for (uint32_t x = threadIdx.x; x < tiles; x += blockDim.x) {
+        uint32_t jt, it;
+        div_rt.divmod(x, jt, it);
+        const uint32_t j0 = jt * 4, i0 = it * 4;
+        const uint8_t* s0 = smem + i0 * pitch + j0;
+        const uint32_t w0 = *reinterpret_cast<const uint32_t*>(s0);
+        const uint32_t w1 = *reinterpret_cast<const uint32_t*>(s0 + pitch);
+        const uint32_t w2 = *reinterpret_cast<const uint32_t*>(s0 + 2 * pitch);
+        const uint32_t w3 = *reinterpret_cast<const uint32_t*>(s0 + 3 * pitch);
+        const uint32_t t0 = __byte_perm(w0, w1, 0x5140), t1 = __byte_perm(w2, w3, 0x5140);
+        const uint32_t t2 = __byte_perm(w0, w1, 0x7362), t3 = __byte_perm(w2, w3, 0x7362);
+        uint8_t* o = out + j0 * R + i0;
+        *reinterpret_cast<uint32_t*>(o) = __byte_perm(t0, t1, 0x5410);
+        *reinterpret_cast<uint32_t*>(o + R) = __byte_perm(t0, t1, 0x7632);
+        *reinterpret_cast<uint32_t*>(o + 2 * R) = __byte_perm(t2, t3, 0x5410);
+        *reinterpret_cast<uint32_t*>(o + 3 * R) = __byte_perm(t2, t3, 0x7632);
+    }
+    const uint32_t rest = (w - w4) * R;
+    for (uint32_t x = threadIdx.x; x < rest; x += blockDim.x) {
+        uint32_t jj, i;
+        div_R.divmod(x, jj, i);
+        out[(w4 + jj) * R + i] = smem[i * pitch + w4 + jj];
+    }
+}
+
 template <int E, int V>
 __device__ __forceinline__ void write_runs(const SlabRunArgs& a, const uint8_t* sm, uint8_t* slab) {
     using T = typename ElemT<E>::T;
     constexpr int K = V / E;
+    if constexpr (E == 1) {
+        if (a.tiles) {
+            write_byte_tiles(sm, a.pitch, slab, a.tile_w, a.tile_R, a.div_rt, a.div_tR);
+            return;
+        }
+    }
     const uint32_t runs = a.count / K;
     if (a.aligned) {
         for (uint32_t g = threadIdx.x; g < runs; g += blockDim.x) {
@@ -644,39 +689,6 @@ __device__ __forceinline__ void colband_stage(const ColBandArgs& a, uint8_t* sme
     }
 }
 
-// Writes a band's w output rows of R 1-byte elements (R a multiple of 4, the
-// range word-aligned) from its staged rows: a thread loads the 4 x 4 byte
-// tile of rows i0..i0+3, columns j0..j0+3 as four words, transposes it with
-// byte permutes and stores four words, one into each of output rows j0..j0+3
-// (row groups fastest across threads); the last w % 4 columns byte by byte.
-__device__ __forceinline__ void colband_write_tiles(const ColBandArgs& a, const uint8_t* smem, uint32_t pitch,
-                                                    uint8_t* out, uint32_t w) {
-    const uint32_t R = a.R, w4 = w & ~3u, tiles = (w4 / 4) * (R / 4);
-    for (uint32_t x = threadIdx.x; x < tiles; x += blockDim.x) {
-        uint32_t jt, it;
-        a.div_rt.divmod(x, jt, it);
-        const uint32_t j0 = jt * 4, i0 = it * 4;
-        const uint8_t* s0 = smem + i0 * pitch + j0;
-        const uint32_t w0 = *reinterpret_cast<const uint32_t*>(s0);
-        const uint32_t w1 = *reinterpret_cast<const uint32_t*>(s0 + pitch);
-        const uint32_t w2 = *reinterpret_cast<const uint32_t*>(s0 + 2 * pitch);
-        const uint32_t w3 = *reinterpret_cast<const uint32_t*>(s0 + 3 * pitch);
-        const uint32_t t0 = __byte_perm(w0, w1, 0x5140), t1 = __byte_perm(w2, w3, 0x5140);
-        const uint32_t t2 = __byte_perm(w0, w1, 0x7362), t3 = __byte_perm(w2, w3, 0x7362);
-        uint8_t* o = out + j0 * R + i0;
-        *reinterpret_cast<uint32_t*>(o) = __byte_perm(t0, t1, 0x5410);
-        *reinterpret_cast<uint32_t*>(o + R) = __byte_perm(t0, t1, 0x7632);
-        *reinterpret_cast<uint32_t*>(o + 2 * R) = __byte_perm(t2, t3, 0x5410);
-        *reinterpret_cast<uint32_t*>(o + 3 * R) = __byte_perm(t2, t3, 0x7632);
-    }
-    const uint32_t rest = (w - w4) * R;
-    for (uint32_t x = threadIdx.x; x < rest; x += blockDim.x) {
-        uint32_t jj, i;
-        a.div_R.divmod(x, jj, i);
-        out[(w4 + jj) * R + i] = smem[i * pitch + w4 + jj];
-    }
-}
-
 template <int E, int V>
 __global__ void __launch_bounds__(512) k_slab_colband(ColBandArgs a) {
     extern __shared__ __align__(16) uint8_t smem[];
@@ -702,7 +714,7 @@ __global__ void __launch_bounds__(512) k_slab_colband(ColBandArgs a) {
             if (a.any_align)
                 colband_write_any<E>(a, smem, s.pitch, out, w * a.R * a.E);
             else if (E == 1 && a.tiles)
-                colband_write_tiles(a, smem, s.pitch, out, w);
+                write_byte_tiles(smem, s.pitch, out, w, a.R, a.div_rt, a.div_R);
             else
                 write_runs<E, V>(s, smem, out);
         }
@@ -1009,6 +1021,13 @@ bool make_slab_runs(uint8_t* data, const Pass& p, uint64_t count, const DeviceCa
         set_aligned_runs(&a, V / E);
         a.wrap = !a.aligned && a.odim[0] >= V / E;
     }
+    // V >= 4: every slab starts on a word and is whole words long
+    a.tiles = E == 1 && q == 2 && p.nd_perm[0] == 1 && p.nd_dims[1] % 4 == 0 && V >= 4 && V_force == 0 &&
+              tuning().narrow_words;
+    a.tile_R = static_cast<uint32_t>(q == 2 ? p.nd_dims[1] : 1);
+    a.tile_w = static_cast<uint32_t>(p.nd_dims[0]);
+    a.div_rt = FastDiv32::make(std::max<uint32_t>(1, a.tile_R / 4));
+    a.div_tR = FastDiv32::make(a.tile_R);
     a.kind = static_cast<uint32_t>(E * 100 + V);
     *smem_out = smem;
     *V_out = V;

@@ -328,6 +328,19 @@ def test_column_bands_in_byte_tiles(E, tuned, words, offset):
 
 
 @pytest.mark.parametrize("words", [1, 0])
+@pytest.mark.parametrize("offset", [0, 4, 1])
+def test_two_d_byte_slabs_in_tiles(E, tuned, words, offset):
+    """2D transposes of 1-byte elements through the slab run kernel (one CTA
+    per slab, and the fewest-pass plan's slab permutation of 160-byte slabs)
+    with a multiple of 4 rows: 4 x 4 byte tiles (knob narrow_words=1) or runs
+    of stores (0); odd column counts; bases off word boundaries take the
+    runs."""
+    tuned(narrow_words=words)
+    for dims, order in [([1000, 100, 20], 0), ([999, 64, 30], 0), ([1001, 36, 20], 0), ([20, 8, 4000], 3)]:
+        run_case(E, dims, [2, 1, 3], 1, order=order, offset=offset)
+
+
+@pytest.mark.parametrize("words", [1, 0])
 @pytest.mark.parametrize("offset", [0, 1, 2, 3])
 def test_slabs_of_odd_wide_elements(E, tuned, words, offset):
     """One-CTA slabs of wide elements whose size is odd or 2 mod 4 (1- and
