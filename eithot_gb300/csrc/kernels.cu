@@ -172,12 +172,11 @@ __device__ __forceinline__ void slab_flat_words(const SlabArgs& a, uint8_t* smem
     const uint32_t n = static_cast<uint32_t>(a.mat_bytes);
     const uintptr_t lo = reinterpret_cast<uintptr_t>(mat);
     const uint32_t rowb = a.C * static_cast<uint32_t>(a.E);
-    const uint32_t total = a.R * a.rowchunks;  // rows staged 16 bytes per thread
-    for (uint32_t x = threadIdx.x; x < total; x += blockDim.x) {
+    span_stage(a.R * a.rowchunks, [&](uint32_t x) {  // rows staged 16 bytes per unit
         uint32_t r, t;
         a.div_rowchunks.divmod(x, r, t);
-        span_chunk(smem + r * a.pitch, mat + static_cast<uint64_t>(r) * rowb, rowb, t);
-    }
+        return SpanUnit{smem + r * a.pitch, mat + static_cast<uint64_t>(r) * rowb, rowb, t, true};
+    });
     __syncthreads();
     auto byte_of = [&](uint32_t b) -> uint32_t {
         uint32_t o, e, c, r;
@@ -220,14 +219,12 @@ __device__ __forceinline__ void slab_flat_words(const SlabArgs& a, uint8_t* smem
 // inside each output piece, the at most 3 bytes at either end one by one
 // (the words there hold other pieces' bytes).
 __device__ __forceinline__ void slab_pieces_words(const SlabArgs& a, uint8_t* smem, uint8_t* mat, uint32_t L) {
-    const uint32_t total = a.R * a.C * a.slots;
-    for (uint32_t x = threadIdx.x; x < total; x += blockDim.x) {
+    span_stage(a.R * a.C * a.slots, [&](uint32_t x) {
         uint32_t p, t, r, c;
         a.div_slots.divmod(x, p, t);
-        if (16 * t >= L) continue;
         a.div_C.divmod(p, r, c);
-        span_chunk(smem + r * a.pitch + c * a.w, mat + static_cast<uint64_t>(p) * a.E, L, t);
-    }
+        return SpanUnit{smem + r * a.pitch + c * a.w, mat + static_cast<uint64_t>(p) * a.E, L, t, 16 * t < L};
+    });
     __syncthreads();
     const uint32_t wtotal = a.R * a.C * a.wslots;
     for (uint32_t x = threadIdx.x; x < wtotal; x += blockDim.x) {
@@ -384,12 +381,11 @@ __global__ void __launch_bounds__(kThreads) k_slab_cluster(SlabClusterArgs a) {
             // pointer lies beyond the matrix, possibly beyond the allocation)
             // and reads nothing
             const uint32_t rowb = static_cast<uint32_t>(a.row_bytes);
-            const uint32_t total = nr * a.rowchunks;
-            for (uint32_t x = threadIdx.x; x < total; x += blockDim.x) {
+            span_stage(nr * a.rowchunks, [&](uint32_t x) {
                 uint32_t rr, t;
                 a.div_rowchunks.divmod(x, rr, t);
-                span_chunk(smem + rr * a.pitch, band + static_cast<uint64_t>(rr) * rowb, rowb, t);
-            }
+                return SpanUnit{smem + rr * a.pitch, band + static_cast<uint64_t>(rr) * rowb, rowb, t, true};
+            });
         } else {
             const uint32_t in_units = nr * a.upr;
             for (uint32_t x = threadIdx.x; x < in_units; x += blockDim.x) {

@@ -681,12 +681,12 @@ __device__ __forceinline__ void colband_stage(const ColBandArgs& a, uint8_t* sme
         asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
         return;
     }
-    // each row segment 16 bytes per thread from the aligned words it spans
-    for (uint32_t x = threadIdx.x; x < total; x += blockDim.x) {
+    // each row segment 16 bytes per unit from the aligned words it spans
+    span_stage(total, [&](uint32_t x) {
         uint32_t r, t;
         dv.divmod(x, r, t);
-        span_chunk(smem + r * pitch, seg + static_cast<uint64_t>(r) * a.row_bytes, wb, t);
-    }
+        return SpanUnit{smem + r * pitch, seg + static_cast<uint64_t>(r) * a.row_bytes, wb, t, true};
+    });
 }
 
 template <int E, int V>
