@@ -414,6 +414,7 @@ int hs_tune(const char* key, int value) {
     else if (k == "dbuf") t.dbuf = value;
     else if (k == "factor") t.factor = value;
     else if (k == "slab_cluster") t.slab_cluster = value;
+    else if (k == "slab_colband") t.slab_colband = value;
     else return -1;
     return 0;
 }

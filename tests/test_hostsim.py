@@ -215,3 +215,56 @@ def test_column_band_slabs(hostsim, dims, elem):
     passes = describe.value.decode().splitlines()
     assert len(passes) == 1 and passes[0].startswith("slab-colband"), passes
     assert run(hostsim, dims, perm, elem)
+
+
+def test_column_bands_follow_their_knob(hostsim):
+    """slab_colband = 0 keeps the row-band cluster slab for few-row matrices
+    whose rows fit one CTA, and the Catanzaro passes for rows that do not."""
+    hostsim.hs_tune.argtypes = [ctypes.c_char_p, ctypes.c_int]
+    describe = ctypes.create_string_buffer(1 << 14)
+
+    def kinds(dims):
+        r = len(dims)
+        hostsim.hs_describe(describe, len(describe), r, (ctypes.c_int64 * r)(*dims),
+                            (ctypes.c_int * r)(*([2, 1] + list(range(3, r + 1)))), 1, 1, ctypes.c_double(0.01), 0)
+        return [line.split()[0] for line in describe.value.decode().splitlines()]
+
+    try:
+        assert kinds([41125, 20, 2]) == ["slab-colband"]
+        assert kinds([300001, 5]) == ["slab-colband"]
+        assert hostsim.hs_tune(b"slab_colband", 0) == 0
+        assert kinds([41125, 20, 2]) == ["slab-cluster"]
+        assert "slab-colband" not in kinds([300001, 5])
+    finally:
+        hostsim.hs_tune(b"slab_colband", 256)
+
+
+@pytest.mark.parametrize("dims,perm,elem", [([1784616, 28], [2, 1], 1), ([2003328, 8], [2, 1], 1),
+                                            ([4096, 3001], [2, 1], 2), ([6000, 4000], [2, 1], 1)])
+def test_narrow_transposes_split_into_wider_granules(hostsim, dims, perm, elem):
+    """1- and 2-byte transposes whose Catanzaro passes would move 1- or 2-byte
+    units are split along a factor of R or C into a transpose of wider
+    granules and small transposes (factor=1); factor=0 keeps the direct
+    passes.  Both pass lists produce the oracle's permutation."""
+    hostsim.hs_tune.argtypes = [ctypes.c_char_p, ctypes.c_int]
+    describe = ctypes.create_string_buffer(1 << 14)
+    r = len(dims)
+
+    def passes():
+        hostsim.hs_describe(describe, len(describe), r, (ctypes.c_int64 * r)(*dims), (ctypes.c_int * r)(*perm),
+                            elem, 1, ctypes.c_double(0.01), 0)
+        return describe.value.decode().splitlines()
+
+    def catanzaro_elems(ps):
+        return [int(p.split("E=")[1].split()[0]) for p in ps if p.startswith(("c2r-", "r2c-"))]
+
+    factored = passes()
+    assert all(e % 4 == 0 for e in catanzaro_elems(factored)), factored  # no pass of narrow units
+    assert run(hostsim, dims, perm, elem)
+    try:
+        assert hostsim.hs_tune(b"factor", 0) == 0
+        direct = passes()
+        assert catanzaro_elems(direct) and all(e == elem for e in catanzaro_elems(direct)), direct
+        assert run(hostsim, dims, perm, elem)
+    finally:
+        hostsim.hs_tune(b"factor", 1)
