@@ -268,3 +268,16 @@ def test_narrow_transposes_split_into_wider_granules(hostsim, dims, perm, elem):
         assert run(hostsim, dims, perm, elem)
     finally:
         hostsim.hs_tune(b"factor", 1)
+
+
+@pytest.mark.parametrize("order", [0, 3])
+def test_mixed_tensors_through_the_kernel_maps(hostsim, order):
+    """Tensors drawn like the batched workload's mix (rank 3-6, 1-8 byte
+    elements, random permutations; 4 KB-8 MB here), planned under the
+    reference's series (0) and the fewest-pass search (3), with column bands,
+    the factoring of narrow passes and every other lowering in play: the pass
+    lists, applied on the CPU with the kernels' index maps, reproduce the
+    oracle's permutation."""
+    import bench
+    for dims, perm, elem in bench.mixed_tensors(150, 11, 4096, 8 << 20, 3, 6):
+        assert run(hostsim, dims, perm, elem, order=order), (dims, perm, elem, order)
