@@ -237,8 +237,12 @@ __device__ __forceinline__ void slab_pieces_words(const SlabArgs& a, uint8_t* sm
         if (4 * k >= h + L) continue;
         const uint32_t b0 = 4 * k - h;
         if (4 * k >= h && b0 + 4 <= L) {
-            const uint32_t v = static_cast<uint32_t>(src[b0]) | static_cast<uint32_t>(src[b0 + 1]) << 8 |
-                               static_cast<uint32_t>(src[b0 + 2]) << 16 | static_cast<uint32_t>(src[b0 + 3]) << 24;
+            // the piece's slot is word-aligned: the output word is the funnel
+            // shift of the two slot words it spans (the second only when the
+            // word is misaligned, so that it starts inside the piece)
+            const uint32_t* sw = reinterpret_cast<const uint32_t*>(src);
+            const uint32_t q = b0 >> 2, m = b0 & 3u;
+            const uint32_t v = m ? __funnelshift_r(sw[q], sw[q + 1], 8 * m) : sw[q];
             *reinterpret_cast<uint32_t*>(lo - h + 4 * k) = v;
         } else {
             uint8_t* dst = reinterpret_cast<uint8_t*>(lo - h + 4 * k);
