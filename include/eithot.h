@@ -327,9 +327,12 @@ int eithot_estimate_report(int rank, const int64_t* dims, const int* perm_1based
  *                 row fewer bytes per CTA than this (0..4096) take column
  *                 bands instead (each CTA writes one contiguous range of the
  *                 output); 0 always row bands
- *   "narrow_words" 1 contiguous ranges of 1- and 2-byte units (slabs, row
- *                 pieces, bands, column row pieces) are staged from the aligned
- *                 4-byte words around them (default), 0 unit by unit
+ *   "narrow_words" 1 ranges of 1- and 2-byte units (slabs, strips of wide
+ *                 odd-sized elements, row pieces, bands, column row pieces)
+ *                 are staged from the aligned words or 16-byte chunks around
+ *                 them and written as aligned words; 1-byte 2D transposes and
+ *                 column bands of 4k rows as 4 x 4 byte tiles (default); 0
+ *                 unit by unit
  *   "row_solo_kb" rows held whole by one CTA that are larger than this many
  *                 KB (16..128, default 48) run one CTA per SM with the next
  *                 row prefetched into registers; smaller ones two or more CTAs
